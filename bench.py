@@ -1,0 +1,360 @@
+"""Benchmark of the GB300 CNAB immersed-boundary step (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
+
+A step is one ``advance!`` of the workload (every level of the multilevel grid, the Schur
+force solve and the projection).  ``value`` is cell-steps/s (cells = nlevels * nx * ny per
+step) over all ranks with the state resident on the device; ``e2e`` is the same metric
+through the public ``solve`` API with a per-step host callback reading C_D / C_L.  Under
+torchrun each rank advances an independent replica on its own GPU (the step has no
+data-parallel split).
+
+``--impl reference`` times the CPU implementation of the same step on this host's cores (the
+FP64 restatement of the reference; Julia is not available) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = None  # read from the benchmark spec when present
+
+
+def baseline_metric() -> str:
+    try:
+        return json.loads((ROOT / "BASELINE.json").read_text())["metric"]
+    except Exception:
+        return "cell-steps/s on 1 GB300"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks through torch.distributed (only when WORLD_SIZE > 1)."""
+
+    def __init__(self, world: int, local: int, backend: str):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.dist, self.torch = dist, torch
+            self.backend = backend
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+def make_workload(ib, name: str):
+    w = ib.workloads
+    table = {"two_body_large": w.two_body_large, "cylinder_small": w.cylinder_small,
+             "four_cylinders": w.four_cylinders}
+    return table[name]()
+
+
+def describe(wl) -> str:
+    bodies = ", ".join(f"{b.npoints()} pts" for b in wl.bodies)
+    return (f"{wl.name}: {wl.nx}x{wl.ny} finest grid h={wl.h}, {wl.nlevels} levels, bodies [{bodies}], "
+            f"Re={wl.Re:g}, dt={wl.dt:g}, CNAB")
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"ibgb300_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.device)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU baseline: the FP64 restatement of the reference on this host's cores
+# ----------------------------------------------------------------------------------------------
+def cpu_reference(ib, wl, nsteps: int, warmup: int):
+    from oracle import ib_oracle as O
+    cores = os.cpu_count() or 1
+    O.WORKERS = cores
+    g = O.grid_from_limits(wl.h, wl.xlims, wl.ylims, wl.nlevels)
+    bodies = wl.bodies
+    xb = np.concatenate([b.xb for b in bodies])
+    ds = np.concatenate([b.ds for b in bodies])
+    op = O.Problem(g, wl.dt, wl.Re, xb, ds, [b.npoints() for b in bodies], freestream=wl.freestream)
+    st = O.init_state(op)
+    st.gamma[0] = wl.initial_gamma()[0].reshape(g.gshape)
+    st.psi, st.q = O.vort2flux(st.gamma, g, O.lap_eigs(g))
+    sol = O.Solver(op, assemble=False)
+    for i in range(warmup):
+        sol.advance(st, i * wl.dt)
+    t0 = time.perf_counter()
+    for i in range(nsteps):
+        sol.advance(st, (warmup + i) * wl.dt)
+    dt = time.perf_counter() - t0
+    return wl.cells_per_step * nsteps / dt, dt / nsteps, cores
+
+
+# ----------------------------------------------------------------------------------------------
+# algorithmic bytes / flops of the sine-transform passes (per step), see the design doc
+# ----------------------------------------------------------------------------------------------
+def pass_model(wl):
+    nG = (wl.nx - 1) * (wl.ny - 1)
+    L = wl.nlevels
+    w = 8
+    # y passes: one CN pass over L levels (reads Gamma and rhs transforms + 2 multipliers,
+    # writes 1) and 2L+1 Poisson passes (reads 1 + multiplier, writes 1)
+    y_bytes = w * nG * (5 * L + 3 * (2 * L + 1))
+    y_launches = 1 + 2 * L + 1
+    # x passes: 3 launches of L arrays in the trial solve, 2 per level in each of the two
+    # Vort2Flux chains, 2 in the projection (the second also reads the trial Gamma)
+    x_bytes = w * nG * (2 * 3 * L + 2 * 4 * L + 2 * 2 + 1)
+    x_launches = 3 + 4 * L + 2
+    # flops: a length-n sine line costs ~2.5 n log2 n (real FFT of length n)
+    fx = 2.5 * wl.nx * np.log2(wl.nx) * (wl.ny - 1)
+    fy = 2.5 * wl.ny * np.log2(wl.ny) * (wl.nx - 1)
+    y_flops = fy * (3 * L + 2 * (2 * L + 1))  # CN: 3 transforms per level; Poisson: 2
+    x_flops = fx * (3 * L + 4 * L + 2)
+    return {"x": (x_bytes, x_launches, x_flops), "y": (y_bytes, y_launches, y_flops)}
+
+
+def run_ours(args, rank, world, local):
+    import __graft_entry__ as ge
+    ib = ge.package()
+    ge.build()
+    lib = ib.load_library()
+    from ibgb300 import _lib as L
+    dist = Dist(world, local, "nccl")
+    wl = make_workload(ib, args.workload)
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = wl.initial_gamma()
+    solver = ib.initsolver(prob, st, device=local)
+    solver.vort2flux(st)
+    info = L.IbInfo()
+    lib.ib_get_info(solver.handle, C.byref(info))
+    K, W = args.steps, args.warmup
+    ts = np.ascontiguousarray(np.arange(W + K + 64, dtype=np.float64) * wl.dt)
+    uv = np.ascontiguousarray(np.tile(np.array(wl.freestream, dtype=np.float64), W + K + 64))
+
+    def tptr(a, off):
+        return a[off:].ctypes.data_as(C.POINTER(C.c_double))
+
+    # warm-up
+    solver._check(lib.ib_advance_n(solver.handle, W, tptr(ts, 0), tptr(uv, 0)))
+    # timed region (device time with CUDA events on the library's stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    dist.barrier()
+    lib.ib_synchronize(solver.handle)
+    if args.profile_range:
+        lib.ib_profiler_start()
+    dev_ms = C.c_double()
+    h0 = time.perf_counter()
+    solver._check(lib.ib_advance_n_timed(solver.handle, K, tptr(ts, W), tptr(uv, 2 * W), C.byref(dev_ms)))
+    host_s = time.perf_counter() - h0
+    if args.profile_range:
+        lib.ib_profiler_stop()
+    dist.barrier()
+    ck = clocks.stop()
+    t_max = dist.max(dev_ms.value / 1e3)
+    value = wl.cells_per_step * K * world / t_max
+    ms_per_step = t_max / K * 1e3
+    out = {
+        "metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
+        "config": {"workload": describe(wl), "cells_per_step": wl.cells_per_step, "parallelism": "replicas",
+                   "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),
+                   "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": host_s / K * 1e3},
+        "gpu_launches": int(info.kernels_per_step) * K,
+    }
+    if ck:
+        out["clocks"] = {"sm_mhz": ck["sm_mhz"], "sm_max_mhz": ck["sm_max_mhz"], "reasons": ck["reasons"],
+                         "samples": ck["samples"], "power_w_max": ck["power_w_max"]}
+    if args.profile_range:
+        print(json.dumps(out), flush=True)
+        return
+    # dominant kernel class: event-timed launches over a second run of K steps
+    model = pass_model(wl)
+    prof = {}
+    npf = min(K, 20)
+    base = W + K
+    for cls, key in ((0, "x"), (1, "y")):
+        tot, nl = C.c_double(), C.c_int64()
+        solver._check(lib.ib_profile_steps(solver.handle, npf, tptr(ts, base), tptr(uv, 2 * base), cls,
+                                           C.byref(tot), C.byref(nl)))
+        base += npf
+        prof[key] = (tot.value, nl.value)
+    dom = max(prof, key=lambda k: prof[k][0])
+    tot_ms, nlaunch = prof[dom]
+    b_step, l_step, f_step = model[dom]
+    per_launch_s = tot_ms / 1e3 / nlaunch
+    bytes_per_launch = b_step / l_step
+    flops_per_launch = f_step / l_step
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    fp64, fp32 = C.c_double(), C.c_double()
+    lib.ib_measure_fp_peaks(local, C.byref(fp64), C.byref(fp32))
+    achieved = bytes_per_launch / per_launch_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(args.workload, {}).get(dom)
+        except Exception:
+            traffic = None
+    out["roofline"] = {
+        "kernel": {"x": "k_xpass (x-direction sine pass)", "y": "k_ypass (y-direction sine pass + spectral op)"}[dom],
+        "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+        "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
+        "avg_launch_ms": per_launch_s * 1e3, "launches_profiled": nlaunch,
+        "share_of_step": tot_ms / npf / ms_per_step,
+        "fp64": {"achieved_tflops": flops_per_launch / per_launch_s / 1e12, "peak_tflops": fp64.value,
+                 "frac": flops_per_launch / per_launch_s / 1e12 / fp64.value if fp64.value > 0 else None,
+                 "peak_source": "measured FMA-chain probe on this GPU"},
+        "other_pass": {k: {"total_ms": prof[k][0], "launches": prof[k][1]} for k in prof},
+    }
+    # end to end through the public API: solve_ with a per-step callback reading C_D / C_L
+    nb = solver.nb
+    t0 = float(ts[base])
+    cbs = (ib.each_timestep(lambda s: [(b.CD, b.CL) for b in s.qty.stress]),)
+    dist.barrier()
+    e0 = time.perf_counter()
+    res = ib.solve_(st, prob, (t0, t0 + (K - 1) * wl.dt), save=cbs, solver=solver)
+    e2e_s = dist.max(time.perf_counter() - e0)
+    assert len(res[0]) == K
+    out["e2e"] = {"value": wl.cells_per_step * K * world / e2e_s, "unit": "cell-steps/s",
+                  "h2d_bytes_per_step": 8 * 2 * wl.nlevels,
+                  "d2h_bytes_per_step": 4 * 3 + 8 * 2 * solver.nbodies + 8 * 2 * nb,
+                  "api": "solve_(state, prob, (t0, tf); save=(each_timestep(C_D, C_L),)) per-step advance!"}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, sec, cores = cpu_reference(ib, wl, args.cpu_steps, 1)
+        out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+                               "sample": f"{args.cpu_steps} advance! steps of the same workload at full size "
+                                         f"({sec:.2f} s/step; FP64 NumPy/SciPy restatement, scipy.fft workers="
+                                         f"{cores}; setup excluded, Schur inverse replaced by a same-size matrix)"}
+    solver.close()
+    dist.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+    ib = ge.package()
+    wl = make_workload(ib, args.workload)
+    v, sec, cores = cpu_reference(ib, wl, args.steps, args.warmup)
+    out = {
+        "impl": "reference", "metric": baseline_metric(), "value": v, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
+        "config": {"workload": describe(wl), "cells_per_step": wl.cells_per_step, "parallelism": "cpu"},
+        "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} advance! steps of the full workload after {args.warmup} warm-up "
+                                   "steps; FP64 NumPy/SciPy restatement of the reference (Julia is not installed); "
+                                   "setup excluded"},
+        "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="two_body_large")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl != "reference" else args.warmup
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,496 @@
+// Batched 2-D DST-I passes: the Poisson / Crank-Nicolson solves of the IBPM step.
+//
+// Replaces the FFTW RODFT00 plan + `LaplacianInv` call of the reference
+// (src/streamfcn/fluid-ops.jl:19-56) and the CN multipliers of `A_Ainv_linearmaps`
+// (src/streamfcn/cnab/ops.jl:14-42).
+//
+// One warp transforms one line (a row for the x pass, a column for the y pass) held in
+// shared memory.  The DST-I of the n-1 interior values of an n-cell axis,
+//     F_k = sum_{j=1}^{n-1} y_j sin(pi j k / n),
+// is computed without the 2x padding of an odd extension:
+//   1. u_j = sin(pi j/n)(y_j + y_{n-j}) + (y_j - y_{n-j})/2         (in place, pairs j, n-j)
+//   2. U = real DFT_n(u) through a complex Stockham FFT of length M = n/2
+//      (mixed radix 8/4/2/3/5, register-staged stages, twiddles from a table)
+//   3. split: F_{2k} = -Im U_k,  D_k = Re U_k                         (pairs k, M-k)
+//   4. F_{2k+1} = D_0/2 + D_1 + ... + D_k                             (warp prefix sum)
+// (the half-length sine transform of Numerical Recipes "sinft", restated for a warp).
+// F is half of FFTW's RODFT00 output; the factor 2 per axis is folded into the
+// spectral multipliers, which are multiplied by 16 (exact in binary floating point).
+#include "ib_common.cuh"
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+
+namespace ib {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------------------------------------------
+// small forward DFTs
+// ------------------------------------------------------------------------------------------
+template <typename T, int R> struct Dft;
+
+template <typename T> struct Dft<T, 2> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    V a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <typename T> struct Dft<T, 4> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+    V t2 = cadd(v[1], v[3]), t3 = cmul_mi(csub(v[1], v[3]));
+    v[0] = cadd(t0, t2);
+    v[2] = csub(t0, t2);
+    v[1] = cadd(t1, t3);
+    v[3] = csub(t1, t3);
+  }
+};
+
+template <typename T> struct Dft<T, 8> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    const T r2 = T(0.70710678118654752440);
+    V e[4] = {v[0], v[2], v[4], v[6]};
+    V o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<T, 4>::run(e);
+    Dft<T, 4>::run(o);
+    // o1 *= (1 - i)/sqrt2 ; o2 *= -i ; o3 *= (-1 - i)/sqrt2
+    V o1 = mk<V>(r2 * (o[1].x + o[1].y), r2 * (o[1].y - o[1].x));
+    V o2 = cmul_mi(o[2]);
+    V o3 = mk<V>(r2 * (o[3].y - o[3].x), -r2 * (o[3].x + o[3].y));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);
+    v[7] = csub(e[3], o3);
+  }
+};
+
+template <typename T> struct Dft<T, 3> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    const T s = T(0.86602540378443864676);
+    V t1 = cadd(v[1], v[2]);
+    V d = csub(v[1], v[2]);
+    V t2 = mk<V>(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
+    V t3 = mk<V>(s * d.y, -s * d.x);  // -i s (x1 - x2)
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(t2, t3);
+    v[2] = csub(t2, t3);
+  }
+};
+
+template <typename T> struct Dft<T, 5> {
+  template <typename V> __device__ __forceinline__ static void run(V* v) {
+    const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
+    const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);
+    V a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+    V a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    V x0 = v[0];
+    V r1 = mk<V>(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
+    V r2 = mk<V>(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
+    V i1 = mk<V>(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+    V i2 = mk<V>(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+    v[0] = mk<V>(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
+    // y = r -/+ i*ii :  -i*(a+ib) = (b, -a)
+    v[1] = mk<V>(r1.x + i1.y, r1.y - i1.x);
+    v[4] = mk<V>(r1.x - i1.y, r1.y + i1.x);
+    v[2] = mk<V>(r2.x + i2.y, r2.y - i2.x);
+    v[3] = mk<V>(r2.x - i2.y, r2.y + i2.x);
+  }
+};
+
+// One Stockham stage of radix R on a length-M complex line, executed by one warp, from
+// `src` to `dst` (ping-pong buffers in shared memory).  Butterfly j reads src[j + r*M/R],
+// applies e^{-2 pi i r k/(Ns R)} (k = j mod Ns) and writes dst[(j-k)R + k + r Ns].
+template <typename T, int R>
+__device__ __forceinline__ void fft_stage(const c2_t<T>* __restrict__ src, c2_t<T>* __restrict__ dst, int M, int Ns,
+                                          const c2_t<T>* __restrict__ tw, int lane) {
+  using V = c2_t<T>;
+  const int nb = M / R;
+  const int tstride = M / (Ns * R);
+  for (int j = lane; j < nb; j += 32) {
+    const int k = j % Ns;
+    V v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * tstride]));
+    }
+    Dft<T, R>::run(v);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) dst[base + r * Ns] = v[r];
+  }
+  __syncwarp();
+}
+
+template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
+template <> __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
+
+// In-place DST-I (F convention, see file header) of s[1..n-1]; s and scratch must be 16-byte
+// aligned and hold n values each.  Executed by one full warp.
+template <typename T>
+__device__ __noinline__ void dst1_warp(T* s, T* scratch, const DstAxis<T>& ax, int lane) {
+  using V = c2_t<T>;
+  const int n = ax.n, M = ax.M, hn = n >> 1;
+  // 1. pre-processing
+  for (int j = 1 + lane; j < hn; j += 32) {
+    const T a = s[j], b = s[n - j];
+    const T sm = a + b, df = T(0.5) * (a - b);
+    const T sn = __ldg(&ax.sintab[j]);
+    s[j] = fmaT(sn, sm, df);
+    s[n - j] = fmaT(sn, sm, -df);
+  }
+  if (lane == 0) {
+    s[0] = T(0);
+    s[hn] = T(2) * s[hn];
+  }
+  __syncwarp();
+  // 2. complex FFT of length M, ping-pong between s and scratch
+  V* src = reinterpret_cast<V*>(s);
+  V* dst = reinterpret_cast<V*>(scratch);
+  int Ns = 1;
+  for (int st = 0; st < ax.nstages; ++st) {
+    const int R = ax.radix[st];
+    switch (R) {
+      case 8: fft_stage<T, 8>(src, dst, M, Ns, ax.tw, lane); break;
+      case 4: fft_stage<T, 4>(src, dst, M, Ns, ax.tw, lane); break;
+      case 2: fft_stage<T, 2>(src, dst, M, Ns, ax.tw, lane); break;
+      case 3: fft_stage<T, 3>(src, dst, M, Ns, ax.tw, lane); break;
+      default: fft_stage<T, 5>(src, dst, M, Ns, ax.tw, lane); break;
+    }
+    Ns *= R;
+    V* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  // 3. split the real DFT: pairs (k, M-k), read from the FFT result, written into s
+  const V* z = src;
+  V* c = reinterpret_cast<V*>(s);
+  const int hM = M >> 1;
+  for (int k = 1 + lane; k < hM; k += 32) {
+    const V zk = z[k], zm = z[M - k];
+    const T er = T(0.5) * (zk.x + zm.x), ei = T(0.5) * (zk.y - zm.y);
+    const T orr = T(0.5) * (zk.y + zm.y), oi = T(0.5) * (zm.x - zk.x);
+    const V w = __ldg(&ax.post[k]);
+    const T tr = w.x * orr - w.y * oi, ti = w.x * oi + w.y * orr;
+    c[k] = mk<V>(-(ei + ti), er + tr);
+    c[M - k] = mk<V>(ei - ti, er - tr);
+  }
+  if (lane == 0) {
+    const V z0 = z[0];
+    const V zh = z[hM];
+    c[0] = mk<V>(T(0), z0.x + z0.y);
+    c[hM] = mk<V>(zh.y, zh.x);
+  }
+  __syncwarp();
+  // 4. odd outputs: prefix sum of D over k (chunked per lane, then across lanes)
+  const int C = (M + 31) >> 5;
+  const int k0 = lane * C;
+  const int k1 = min(M, k0 + C);
+  T acc = T(0);
+  for (int k = k0; k < k1; ++k) {
+    T d = s[2 * k + 1];
+    if (k == 0) d *= T(0.5);
+    acc += d;
+    s[2 * k + 1] = acc;
+  }
+  T incl = acc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += v;
+  }
+  T excl = __shfl_up_sync(kFull, incl, 1);
+  if (lane == 0) excl = T(0);
+  for (int k = k0; k < k1; ++k) s[2 * k + 1] += excl;
+  __syncwarp();
+}
+
+// ------------------------------------------------------------------------------------------
+// x pass: one warp per row (contiguous), optional apply_bc prologue and subtract epilogue.
+// Shared memory per warp: the row (n values) and the FFT scratch (n values).
+// ------------------------------------------------------------------------------------------
+constexpr int kXWarps = 4;
+
+template <typename T, bool kBC, bool kSub>
+__global__ void __launch_bounds__(kXWarps * 32)
+k_xpass(Geometry g, DstAxis<T> ax, XPassArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = ax.n;
+  T* s = reinterpret_cast<T*>(smem_raw) + warp * 2 * n;
+  T* scratch = s + n;
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int total = a.batch * nrow;
+  for (int row = blockIdx.x * kXWarps + warp; row < total; row += gridDim.x * kXWarps) {
+    const int b = row / nrow, J = row - b * nrow;
+    const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
+    const T* src = a.in + off;
+    for (int I = lane; I < ncol; I += 32) s[I + 1] = src[I];
+    if (kBC) {
+      const T* bc = a.bc + (int64_t)b * g.nbc;
+      const T fac = a.bcfac;
+      __syncwarp();
+      if (J == 0)
+        for (int I = lane; I < ncol; I += 32) s[I + 1] += fac * bc[g.B + 1 + I];
+      if (J == nrow - 1)
+        for (int I = lane; I < ncol; I += 32) s[I + 1] += fac * bc[g.T + 1 + I];
+      __syncwarp();
+      if (lane == 0) {
+        s[1] += fac * bc[g.L + 1 + J];
+        s[ncol] += fac * bc[g.R + 1 + J];
+      }
+    }
+    __syncwarp();
+    dst1_warp<T>(s, scratch, ax, lane);
+    T* dst = a.out + off;
+    if (kSub) {
+      const T* sf = a.sub_from + off;
+      for (int I = lane; I < ncol; I += 32) dst[I] = sf[I] - s[I + 1];
+    } else {
+      for (int I = lane; I < ncol; I += 32) dst[I] = s[I + 1];
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// y pass: one CTA per strip of W columns, one warp per column; forward DST, spectral
+// multiply, second DST.  Multipliers are stored column-major in spectral space
+// (index I*(ny-1) + J) so a warp reads them contiguously.
+// Shared memory per warp: P, [Q,] scratch, each n values padded to keep 16-byte alignment.
+// ------------------------------------------------------------------------------------------
+template <typename T, SpecOp OP>
+__global__ void __launch_bounds__(256)
+k_ypass(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int W = blockDim.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = ax.n;
+  const int ps = n + 16 / (int)sizeof(T);
+  T* P = reinterpret_cast<T*>(smem_raw);
+  T* Q = P + W * ps;
+  T* S = (OP == SpecOp::kCn) ? Q + W * ps : Q;
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int nstrips = (ncol + W - 1) / W;
+  for (int blk = blockIdx.x; blk < a.batch * nstrips; blk += gridDim.x) {
+    const int b = blk / nstrips, I0 = (blk - b * nstrips) * W;
+    const int64_t off = (int64_t)b * a.stride;
+    for (int idx = threadIdx.x; idx < nrow * W; idx += blockDim.x) {
+      const int J = idx / W, w = idx - J * W, I = I0 + w;
+      const int64_t gi = off + (int64_t)J * ncol + I;
+      P[w * ps + J + 1] = (I < ncol) ? a.in1[gi] : T(0);
+      if (OP == SpecOp::kCn) Q[w * ps + J + 1] = (I < ncol) ? a.in2[gi] : T(0);
+    }
+    __syncthreads();
+    {
+      T* p = P + warp * ps;
+      T* sc = S + warp * ps;
+      const int I = I0 + warp;
+      dst1_warp<T>(p, sc, ax, lane);
+      const int64_t mo = (int64_t)b * a.mstride + (int64_t)min(I, ncol - 1) * nrow;
+      if (OP == SpecOp::kCn) {
+        T* q = Q + warp * ps;
+        dst1_warp<T>(q, sc, ax, lane);
+        for (int J = lane; J < nrow; J += 32) {
+          const T m1 = __ldg(&a.m1[mo + J]), m2 = __ldg(&a.m2[mo + J]);
+          p[J + 1] = m1 * fmaT(m2, p[J + 1], q[J + 1]);
+        }
+      } else if (OP == SpecOp::kFwd) {
+        for (int J = lane; J < nrow; J += 32) p[J + 1] *= a.scal;
+      } else {
+        for (int J = lane; J < nrow; J += 32) p[J + 1] *= __ldg(&a.m1[mo + J]);
+      }
+      __syncwarp();
+      if (OP != SpecOp::kFwd) dst1_warp<T>(p, sc, ax, lane);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nrow * W; idx += blockDim.x) {
+      const int J = idx / W, w = idx - J * W, I = I0 + w;
+      if (I < ncol) a.out[off + (int64_t)J * ncol + I] = P[w * ps + J + 1];
+    }
+    __syncthreads();
+  }
+}
+
+// Raise a kernel's dynamic shared-memory limit once per device (never inside stream capture:
+// the first launch of every variant happens while a handle is being created).
+cudaError_t ensure_smem(const void* fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_pair(fn, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done[key] = bytes;
+  return e;
+}
+
+int plan_radices(int M, int* radix) {
+  int m = M, ns = 0;
+  int p2 = 0;
+  while (m % 5 == 0) { radix[ns++] = 5; m /= 5; }
+  while (m % 3 == 0) { radix[ns++] = 3; m /= 3; }
+  while (m % 2 == 0) { ++p2; m /= 2; }
+  if (m != 1) return -1;
+  int a = p2 / 3, rem = p2 % 3;
+  if (rem == 1 && a >= 1) { a -= 1; radix[ns++] = 4; radix[ns++] = 4; }
+  else if (rem == 1) { radix[ns++] = 2; }
+  else if (rem == 2) { radix[ns++] = 4; }
+  for (int i = 0; i < a; ++i) radix[ns++] = 8;
+  if (ns > kMaxStages) return -1;
+  return ns;
+}
+
+template <typename T>
+cudaError_t launch_x(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s) {
+  ProfScope prof(kClassXPass, s);
+  const int total = a.batch * (g.ny - 1);
+  const int blocks = (total + kXWarps - 1) / kXWarps;
+  const size_t smem = (size_t)kXWarps * 2 * ax.n * sizeof(T);
+  if (a.bc && a.sub_from) return cudaErrorInvalidValue;
+  cudaError_t e;
+  if (a.bc) {
+    auto k = k_xpass<T, true, false>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
+  } else if (a.sub_from) {
+    auto k = k_xpass<T, false, true>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
+  } else {
+    auto k = k_xpass<T, false, false>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_y(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s) {
+  ProfScope prof(kClassYPass, s);
+  const int nbuf = (a.op == SpecOp::kCn) ? 3 : 2;
+  const int ps = ax.n + 16 / (int)sizeof(T);
+  int W = 8;
+  while (W > 1 && (size_t)nbuf * W * ps * sizeof(T) > 200 * 1024) W >>= 1;
+  const size_t smem = (size_t)nbuf * W * ps * sizeof(T);
+  const int nstrips = (g.nx - 1 + W - 1) / W;
+  const int blocks = a.batch * nstrips;
+  cudaError_t e;
+  if (a.op == SpecOp::kCn) {
+    auto k = k_ypass<T, SpecOp::kCn>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
+  } else if (a.op == SpecOp::kFwd) {
+    auto k = k_ypass<T, SpecOp::kFwd>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
+  } else {
+    auto k = k_ypass<T, SpecOp::kScale>;
+    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
+    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool dst_axis_supported(int n) {
+  if (n < 8 || n % 4 != 0 || n / 2 > 1024) return false;
+  int r[kMaxStages];
+  return plan_radices(n / 2, r) > 0;
+}
+
+template <typename T>
+cudaError_t AxisTables<T>::build(int n) {
+  release();
+  if (!dst_axis_supported(n)) return cudaErrorInvalidValue;
+  using V = c2_t<T>;
+  const int M = n / 2;
+  d.n = n;
+  d.M = M;
+  d.nstages = plan_radices(M, d.radix);
+  std::vector<V> tw(M), post(M / 2 + 1);
+  std::vector<T> sn(n / 2 + 1);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int p = 0; p < M; ++p) {
+    const long double ang = -2.0L * pi * (long double)p / (long double)M;
+    tw[p] = mk<V>((T)cosl(ang), (T)sinl(ang));
+  }
+  for (int k = 0; k <= M / 2; ++k) {
+    const long double ang = -2.0L * pi * (long double)k / (long double)n;
+    post[k] = mk<V>((T)cosl(ang), (T)sinl(ang));
+  }
+  for (int j = 0; j <= n / 2; ++j) sn[j] = (T)sinl(pi * (long double)j / (long double)n);
+  const size_t b_tw = tw.size() * sizeof(V), b_post = post.size() * sizeof(V), b_sn = sn.size() * sizeof(T);
+  const size_t o_post = (b_tw + 255) / 256 * 256;
+  const size_t o_sn = o_post + (b_post + 255) / 256 * 256;
+  cudaError_t e = cudaMalloc(&mem, o_sn + b_sn);
+  if (e != cudaSuccess) { mem = nullptr; return e; }
+  char* base = (char*)mem;
+  if ((e = cudaMemcpy(base, tw.data(), b_tw, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  if ((e = cudaMemcpy(base + o_post, post.data(), b_post, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  if ((e = cudaMemcpy(base + o_sn, sn.data(), b_sn, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  d.tw = (const V*)base;
+  d.post = (const V*)(base + o_post);
+  d.sintab = (const T*)(base + o_sn);
+  return cudaSuccess;
+}
+
+template <typename T>
+void AxisTables<T>::release() {
+  if (mem) cudaFree(mem);
+  mem = nullptr;
+}
+
+template <typename T>
+cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s) {
+  if (ax.n != g.nx) return cudaErrorInvalidValue;
+  if (a.batch <= 0) return cudaSuccess;
+  return launch_x<T>(g, ax, a, s);
+}
+
+template <typename T>
+cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s) {
+  if (ax.n != g.ny) return cudaErrorInvalidValue;
+  if (a.batch <= 0) return cudaSuccess;
+  return launch_y<T>(g, ax, a, s);
+}
+
+template <typename T>
+cudaError_t dst_rows(const Geometry& g, const DstAxis<T>& ax, const T* in, T* out, int batch,
+                     cudaStream_t s) {
+  XPassArgs<T> a{};
+  a.in = in;
+  a.out = out;
+  a.batch = batch;
+  a.stride = g.nG;
+  return xpass<T>(g, ax, a, s);
+}
+
+template struct AxisTables<double>;
+template struct AxisTables<float>;
+template cudaError_t xpass<double>(const Geometry&, const DstAxis<double>&, const XPassArgs<double>&, cudaStream_t);
+template cudaError_t xpass<float>(const Geometry&, const DstAxis<float>&, const XPassArgs<float>&, cudaStream_t);
+template cudaError_t ypass<double>(const Geometry&, const DstAxis<double>&, const YPassArgs<double>&, cudaStream_t);
+template cudaError_t ypass<float>(const Geometry&, const DstAxis<float>&, const YPassArgs<float>&, cudaStream_t);
+template cudaError_t dst_rows<double>(const Geometry&, const DstAxis<double>&, const double*, double*, int, cudaStream_t);
+template cudaError_t dst_rows<float>(const Geometry&, const DstAxis<float>&, const float*, float*, int, cudaStream_t);
+
+}  // namespace ib

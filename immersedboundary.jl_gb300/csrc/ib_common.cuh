@@ -1,0 +1,247 @@
+// Internal declarations shared by the translation units of libibgb300.
+//
+// Layout conventions (identical to the reference's column-major Julia arrays):
+//   circulation / streamfunction level: (nx-1)*(ny-1), index i + (nx-1)*j, i fastest
+//   flux level: [qx (nx+1)*ny ; qy nx*(ny+1)], each i fastest
+//   boundary ring: 2(nx+1)+2(ny+1) values with offsets L=0, R=ny+1, B=2(ny+1), T=B+nx+1
+//   body forces: [fx_1..fx_nb, fy_1..fy_nb]
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ib {
+
+// ----------------------------------------------------------------------------------------------
+// complex helpers (forward transforms use e^{-2 pi i / N})
+// ----------------------------------------------------------------------------------------------
+template <typename T> struct C2;
+template <> struct C2<double> { using type = double2; };
+template <> struct C2<float> { using type = float2; };
+template <typename T> using c2_t = typename C2<T>::type;
+
+template <typename V> __host__ __device__ __forceinline__ V mk(decltype(V::x) a, decltype(V::x) b) {
+  V v; v.x = a; v.y = b; return v;
+}
+template <typename V> __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
+template <typename V> __device__ __forceinline__ V csub(V a, V b) { return mk<V>(a.x - b.x, a.y - b.y); }
+template <typename V> __device__ __forceinline__ V cmul(V a, V b) {
+  return mk<V>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// multiply by -i
+template <typename V> __device__ __forceinline__ V cmul_mi(V a) { return mk<V>(a.y, -a.x); }
+
+// ----------------------------------------------------------------------------------------------
+// Transform tables for one axis: DST-I of the n-1 interior values of an n-cell axis,
+// computed as a half-length (M = n/2) complex FFT (Stockham, mixed radix 8/4/2/3/5).
+// ----------------------------------------------------------------------------------------------
+constexpr int kMaxStages = 10;
+
+template <typename T> struct DstAxis {
+  int n;                    // cells along the axis (array length n-1)
+  int M;                    // n/2, complex FFT length
+  int nstages;
+  int radix[kMaxStages];
+  const c2_t<T>* tw;        // [M]      e^{-2 pi i p / M}
+  const T* sintab;          // [n/2+1]  sin(pi j / n)
+  const c2_t<T>* post;      // [M/2+1]  e^{-2 pi i k / n}
+};
+
+struct Geometry {
+  int nx, ny, nlev;
+  int nG, nq, nu, nbc;
+  int L, R, B, T;           // ring offsets
+  double h, x0, y0;
+};
+
+inline Geometry make_geometry(int nx, int ny, int nlev, double h, double x0, double y0) {
+  Geometry g;
+  g.nx = nx; g.ny = ny; g.nlev = nlev;
+  g.nG = (nx - 1) * (ny - 1);
+  g.nu = (nx + 1) * ny;
+  g.nq = g.nu + nx * (ny + 1);
+  g.nbc = 2 * (nx + 1) + 2 * (ny + 1);
+  g.L = 0; g.R = ny + 1; g.B = 2 * (ny + 1); g.T = 2 * (ny + 1) + nx + 1;
+  g.h = h; g.x0 = x0; g.y0 = y0;
+  return g;
+}
+
+// Host-side owner of the device tables of one axis.
+template <typename T> struct AxisTables {
+  DstAxis<T> d{};
+  void* mem = nullptr;
+  cudaError_t build(int n);
+  void release();
+};
+
+bool dst_axis_supported(int n);
+
+// ----------------------------------------------------------------------------------------------
+// DST passes (dst.cu)
+// ----------------------------------------------------------------------------------------------
+// Every pass takes arrays of (nx-1)*(ny-1) values; `batch` arrays live at stride nG.
+// Spectral multipliers are stored per array slot with stride `mstride` (0 = shared).
+enum class SpecOp : int {
+  kScale = 0,      // Z = m1 * P
+  kCn = 1,         // Z = m1 * (m2 * P + Q)   (P from input 1, Q from input 2)
+  kFwd = 2,        // out = scal * P          (one transform only)
+};
+
+template <typename T>
+struct XPassArgs {
+  const T* in; T* out; int batch; int64_t stride;     // plain in -> out
+  // optional fused prologue: edge terms of apply_bc (added to rows J=0, ny-2 and columns 0, nx-2)
+  const T* bc;             // ring (nbc), one per batch slot at stride nbc; nullptr = none
+  T bcfac;
+  // optional fused epilogue: out = sub_from - value  (projection)  or plain store
+  const T* sub_from;
+};
+
+template <typename T>
+cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s);
+
+template <typename T>
+struct YPassArgs {
+  const T* in1; const T* in2; T* out; int batch; int64_t stride;
+  const T* m1; const T* m2; int64_t mstride;  // multipliers (per slot stride)
+  SpecOp op;
+  T scal;                                      // kFwd scale
+};
+
+template <typename T>
+cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s);
+
+// plain 1-D DST along x only (for tests of the transform itself)
+template <typename T>
+cudaError_t dst_rows(const Geometry& g, const DstAxis<T>& ax, const T* in, T* out, int batch,
+                     cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
+// stencils (stencil.cu)
+// ----------------------------------------------------------------------------------------------
+template <typename T>
+cudaError_t get_bc(const Geometry& g, const T* r, T* bc, int batch, T extra_scale, cudaStream_t s);
+template <typename T>
+cudaError_t apply_bc(const Geometry& g, T* r, const T* bc, T fac, int batch, cudaStream_t s);
+template <typename T>
+cudaError_t coarsify(const Geometry& g, T* gc, const T* gf, int batch, int64_t stride, cudaStream_t s);
+template <typename T>
+cudaError_t curl(const Geometry& g, const T* psi, const T* bc, T* q, int batch, cudaStream_t s);
+template <typename T>
+cudaError_t rot(const Geometry& g, const T* q, T* gam, int batch, cudaStream_t s);
+
+// Trial-state explicit part for all levels at once.  For each level (0-based l):
+//   nl_new[l] = rot(direct_product(avg_flux(q[l] + q0[l]), gamma[l], bcn[l])) / hc_l^2
+//   rhs[l]    = dt*beta0*nl_new[l] + dt*beta1*nl_old[l] + rhsbc edges of level l
+// bcn[l] is the nonlinear boundary ring (zero for the coarsest level); rhsbc edges are
+// given as 4 edge vectors per level (bottom/top: nx-1, left/right: ny-1).
+template <typename T>
+struct NonlinArgs {
+  const T* q; const T* gamma; const T* bcn; const T* nl_old; const T* edges;
+  T* nl_new; T* rhs;
+  const double* q0;        // [nlev][2] (u hc, v hc)
+  const double* inv_hc2;   // [nlev]
+  double dtb0, dtb1;
+};
+template <typename T>
+cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s);
+
+// Trial-step boundary rings: bcn[l] (nonlinear ring, already x0.25x0.25) for l < nlev-1 and
+// the accumulated rhsbc edge vectors of every level (reference quirk: never reset).
+template <typename T>
+cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac,
+                        cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
+// bodies (body.cu)
+// ----------------------------------------------------------------------------------------------
+constexpr int kSupp = 6;
+constexpr int kWin = 2 * kSupp + 1;   // 13
+constexpr int kWin2 = kWin * kWin;    // 169
+
+// weights [nb][2][13][13] (component, y offset b, x offset a); body_idx [nb][2]
+cudaError_t reg_update(const Geometry& g, const double* xb, int nb, int* body_idx, double* weight,
+                       int* status, cudaStream_t s);
+// E: fb[k + c*nb] = sum_w weight * q_c(window), with q = q1 + q0; q0 is a device pointer to the
+// uniform level-1 base flux (q0x, q0y) or nullptr
+template <typename T>
+cudaError_t reg_gather(const Geometry& g, const T* q, const double* q0, const int* body_idx,
+                       const double* weight, int nb, double* fb, int ncols, int64_t qstride,
+                       int64_t fstride, cudaStream_t s);
+// E^T followed by rot restricted to the body box: gamma_out = rot(E^T f) (whole array written)
+template <typename T>
+cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_idx,
+                            const double* weight, int nb, T* qtmp, T* gam, int ncols,
+                            int64_t fstride, int* status, cudaStream_t s);
+// E^T alone (operator test entry point)
+template <typename T>
+cudaError_t reg_scatter(const Geometry& g, const double* f, const int* body_idx, const double* weight,
+                        int nb, T* q, int* status, cudaStream_t s);
+// unit-vector columns: f[c][r] = (r == col0 + c)
+cudaError_t unit_columns(double* f, int nf, int col0, int ncols, cudaStream_t s);
+
+// unit-force columns for the Schur assembly: gam[c] = rot(E^T e_{col0+c}), c < ncols
+template <typename T>
+cudaError_t unit_scatter_rot(const Geometry& g, const int* body_idx, const double* weight, int nb, int col0,
+                             int ncols, T* gam, cudaStream_t s);
+
+// forces -> coefficients (update_stress!): out[2b] = C_D, out[2b+1] = C_L of body b;
+// stress (optional) = per-body column-major (n x 2) surface stress blocks
+cudaError_t update_stress_hd(const double* fb, int nb, int nbodies, const int* body_start, const double* ds,
+                             double h, double dt, double* cd_cl_out, double* stress_out, cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
+// dense linear algebra (linalg.cu)
+// ----------------------------------------------------------------------------------------------
+// y = A x for row-major A (n x n), one warp per row, fixed reduction order
+cudaError_t gemv_rowmajor(const double* A, const double* x, double* y, int n, cudaStream_t s);
+// in-place inverse of a column-major n x n matrix (blocked Gauss-Jordan); status!=0 on a
+// zero/non-finite pivot
+cudaError_t invert_inplace(double* A, int n, double* work, int* status, cudaStream_t s);
+size_t invert_workspace_bytes(int n);
+cudaError_t transpose(const double* in, double* out, int rows, int cols, cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
+// launch profiling: when a Prof is installed for the calling thread, launches of the selected
+// kernel class are bracketed by CUDA events on their stream (used by ib_profile_steps)
+// ----------------------------------------------------------------------------------------------
+enum KClass : int { kClassXPass = 0, kClassYPass = 1, kClassNonlin = 2, kClassCount = 3 };
+struct Prof {
+  int cls = -1;
+  std::vector<cudaEvent_t> ev;
+  size_t used = 0;
+};
+extern thread_local Prof* g_prof;
+struct ProfScope {
+  cudaEvent_t end = nullptr;
+  cudaStream_t s;
+  ProfScope(int cls, cudaStream_t st) : s(st) {
+    Prof* p = g_prof;
+    if (!p || p->cls != cls) return;
+    if (p->used + 2 > p->ev.size()) {
+      for (int i = 0; i < 64; ++i) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        p->ev.push_back(e);
+      }
+    }
+    cudaEventRecord(p->ev[p->used], s);
+    end = p->ev[p->used + 1];
+    p->used += 2;
+  }
+  ~ProfScope() {
+    if (end) cudaEventRecord(end, s);
+  }
+};
+
+// ----------------------------------------------------------------------------------------------
+// misc
+// ----------------------------------------------------------------------------------------------
+template <typename T>
+cudaError_t fill(T* p, T v, int64_t n, cudaStream_t s);
+template <typename T>
+cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s);  // y = a x + b y
+
+}  // namespace ib

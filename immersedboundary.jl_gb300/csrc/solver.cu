@@ -1,0 +1,965 @@
+// libibgb300: handle, setup (Solver), the CNAB advance! step as captured CUDA graphs, and the
+// C ABI of include/ibgb300.h and include/ibgb300_ops.h.
+//
+// Step sequence (reference: src/streamfcn/cnab/timestepping.jl:253-290), FP64:
+//   d  trial state   trial_rings -> nonlin_rhs (all levels) -> X(Gamma), X(rhs) -> Y(CN) -> X
+//                    -> trial Vort2Flux (coarse-to-fine chain, curl on level 1 only)
+//   e  forces        E(qs1 + q0) -> Binv gemv
+//   f  stress        C_D, C_L per body -> device history
+//   g  projection    rot(E^T Fb) -> Ainv_1 -> Gamma_1 = Gamma_s1 - (.)   (buffers swap)
+//   h  Vort2Flux     coarsify + chain of Poisson solves + curl on every level
+// The CN pair A / Ainv of a level shares its transforms: Gamma_s = S[(a S Gamma + S r) m]
+// (3 DSTs instead of the reference's 4, equal up to round-off).
+#include "ib_common.cuh"
+#include "ibgb300.h"
+#include "ibgb300_ops.h"
+#include "ibgb300_diag.h"
+
+#include <chrono>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+using namespace ib;
+
+namespace ib {
+thread_local Prof* g_prof = nullptr;
+}
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+constexpr int kQ0Slots = 1024;  // pinned staging slots of per-step base flux
+
+}  // namespace
+
+struct ib_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Geometry g{};
+  double dt = 0, re = 0, beta0 = 1.5, beta1 = -0.5;
+  int nbodies = 0, nb = 0, nf = 0;
+  int precision = IB_PREC_FP64;
+  AxisTables<double> axx, axy;
+  // state
+  double* G[2] = {nullptr, nullptr};
+  double* N[2] = {nullptr, nullptr};
+  double* psi = nullptr;
+  double* q = nullptr;
+  double* fb = nullptr;
+  double t = 0.0;
+  int parity = 0;
+  int64_t steps = 0;
+  // step scratch
+  double *rhs = nullptr, *w1 = nullptr, *w2 = nullptr, *qs1 = nullptr, *qtmp = nullptr, *gtmp = nullptr;
+  double *bcn = nullptr, *edges = nullptr, *rings = nullptr;
+  // spectral multipliers (column-major in spectral space, x16)
+  double *mLap = nullptr, *mCN1 = nullptr, *mCN2 = nullptr;
+  // per-level parameters
+  double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr;
+  double* h_q0 = nullptr;  // pinned [kQ0Slots][2L]
+  int q0_slot = 0;
+  // bodies
+  double *xb = nullptr, *ds = nullptr, *weight = nullptr;
+  int *body_start = nullptr, *body_idx = nullptr;
+  double *bmat = nullptr, *binv_cm = nullptr, *binv_rm = nullptr, *ftmp = nullptr;
+  double *cdcl = nullptr, *stress = nullptr, *hist = nullptr;
+  int hist_cap = 4096;
+  int* d_counter = nullptr;
+  int* status = nullptr;  // [0] out of grid, [1] non-finite flux, [2] singular Schur matrix
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  bool use_graph = true;
+  int kernels_per_step = 0;
+  int64_t device_bytes = 0;
+  double setup_ms = 0.0;
+  std::string err;
+  std::vector<void*> allocs;
+
+  template <typename T>
+  cudaError_t alloc(T** p, size_t count) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+    if (e != cudaSuccess) return e;
+    device_bytes += (int64_t)(count * sizeof(T));
+    allocs.push_back(v);
+    *p = (T*)v;
+    return cudaMemsetAsync(v, 0, count * sizeof(T) > 0 ? count * sizeof(T) : 16, stream);
+  }
+};
+
+namespace {
+
+int fail(ib_handle* h, int code, const char* what, cudaError_t e = cudaSuccess) {
+  std::string m = what;
+  if (e != cudaSuccess) {
+    m += ": ";
+    m += cudaGetErrorString(e);
+  }
+  if (h) h->err = m;
+  else {
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    g_create_err = m;
+  }
+  return code;
+}
+
+#define CK(x)                                                        \
+  do {                                                               \
+    cudaError_t e_ = (x);                                            \
+    if (e_ != cudaSuccess) return fail(h, IB_ERR_CUDA, #x, e_);      \
+  } while (0)
+
+// cudaError_t-returning variant for the enqueue helpers
+#define CE(x)                              \
+  do {                                     \
+    cudaError_t e_ = (x);                  \
+    if (e_ != cudaSuccess) return e_;      \
+  } while (0)
+
+// Poisson-type solve of `batch` arrays: out = S2D( m1 .* S2D(in [+ apply_bc(bc, 1)]) ), with an
+// optional subtract epilogue out = sub_from - (...).
+cudaError_t poisson(ib_handle* h, const double* in, double* out, int batch, const double* bc, const double* m1,
+                    int64_t mstride, const double* sub_from, double* w) {
+  XPassArgs<double> xa{};
+  xa.in = in;
+  xa.out = w;
+  xa.batch = batch;
+  xa.stride = h->g.nG;
+  xa.bc = bc;
+  xa.bcfac = 1.0;
+  CE(xpass<double>(h->g, h->axx.d, xa, h->stream));
+  YPassArgs<double> ya{};
+  ya.in1 = w;
+  ya.out = w;
+  ya.batch = batch;
+  ya.stride = h->g.nG;
+  ya.m1 = m1;
+  ya.mstride = mstride;
+  ya.op = SpecOp::kScale;
+  CE(ypass<double>(h->g, h->axy.d, ya, h->stream));
+  XPassArgs<double> xb{};
+  xb.in = w;
+  xb.out = out;
+  xb.batch = batch;
+  xb.stride = h->g.nG;
+  xb.sub_from = sub_from;
+  return xpass<double>(h->g, h->axx.d, xb, h->stream);
+}
+
+// Vort2Flux (src/streamfcn/fluid-ops.jl:438-472) on one L-level set.  If q is null only the
+// level-1 flux is formed, into q1.  gam is coarsened in place like the reference.
+cudaError_t vort2flux(ib_handle* h, double* gam, double* psi, double* q, double* q1, double* rings) {
+  const Geometry& g = h->g;
+  const int L = g.nlev;
+  const int64_t nG = g.nG;
+  for (int l = 1; l < L; ++l) CE(coarsify<double>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
+  CE(poisson(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, h->mLap, 0, nullptr, h->w1));
+  if (q) CE(curl<double>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
+  else if (L == 1) CE(curl<double>(g, psi, nullptr, q1, 1, h->stream));
+  for (int l = L - 2; l >= 0; --l) {
+    double* ring = rings + (int64_t)l * g.nbc;
+    CE(get_bc<double>(g, psi + (l + 1) * nG, ring, 1, 1.0, h->stream));
+    CE(poisson(h, gam + l * nG, psi + l * nG, 1, ring, h->mLap, 0, nullptr, h->w1));
+    if (q) CE(curl<double>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
+    else if (l == 0) CE(curl<double>(g, psi, ring, q1, 1, h->stream));
+  }
+  return cudaSuccess;
+}
+
+__global__ void k_hist_append(const double* __restrict__ cdcl, double* __restrict__ hist, int cap, int n,
+                              int* __restrict__ counter) {
+  const int idx = *counter % cap;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) hist[(int64_t)idx * n + i] = cdcl[i];
+  __syncthreads();
+  if (threadIdx.x == 0) *counter = *counter + 1;
+}
+
+// Enqueue one advance! for buffer parity p (see the file header).
+cudaError_t enqueue_step(ib_handle* h, int p) {
+  const Geometry& g = h->g;
+  const int L = g.nlev;
+  const int64_t nG = g.nG;
+  cudaStream_t s = h->stream;
+  double* gam = h->G[p];
+  double* gs = h->G[p ^ 1];
+  double* nl_new = h->N[p];
+  double* nl_old = h->N[p ^ 1];
+  // d. trial state (GetTrialState, timestepping.jl:28-79)
+  CE(trial_rings<double>(g, gam, h->bcn, h->edges, h->d_fac, s));
+  NonlinArgs<double> na{};
+  na.q = h->q;
+  na.gamma = gam;
+  na.bcn = h->bcn;
+  na.nl_old = nl_old;
+  na.edges = h->edges;
+  na.nl_new = nl_new;
+  na.rhs = h->rhs;
+  na.q0 = h->d_q0;
+  na.inv_hc2 = h->d_inv_hc2;
+  na.dtb0 = h->dt * h->beta0;
+  na.dtb1 = h->dt * h->beta1;
+  CE(nonlin_rhs<double>(g, na, s));
+  XPassArgs<double> xa{};
+  xa.in = gam;
+  xa.out = h->w1;
+  xa.batch = L;
+  xa.stride = nG;
+  CE(xpass<double>(g, h->axx.d, xa, s));
+  xa.in = h->rhs;
+  xa.out = h->w2;
+  CE(xpass<double>(g, h->axx.d, xa, s));
+  YPassArgs<double> ya{};
+  ya.in1 = h->w1;
+  ya.in2 = h->w2;
+  ya.out = h->w1;
+  ya.batch = L;
+  ya.stride = nG;
+  ya.m1 = h->mCN1;
+  ya.m2 = h->mCN2;
+  ya.mstride = nG;
+  ya.op = SpecOp::kCn;
+  CE(ypass<double>(g, h->axy.d, ya, s));
+  xa.in = h->w1;
+  xa.out = gs;
+  CE(xpass<double>(g, h->axx.d, xa, s));
+  // trial Vort2Flux: psi on every level, flux on level 1 only (the only one read)
+  CE(vort2flux(h, gs, h->psi, nullptr, h->qs1, h->rings));
+  if (h->nb > 0) {
+    // e. BoundaryForcer{RigidBody{GridFrame}} (timestepping.jl:106-120)
+    CE(reg_gather<double>(g, h->qs1, h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, g.nq, h->nf, s));
+    CE(gemv_rowmajor(h->binv_rm, h->ftmp, h->fb, h->nf, s));
+    // f. update_stress! (states.jl:53-84)
+    CE(update_stress_hd(h->fb, h->nb, h->nbodies, h->body_start, h->ds, g.h, h->dt, h->cdcl, h->stress, s));
+    k_hist_append<<<1, 64, 0, s>>>(h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies, h->d_counter);
+    CE(cudaGetLastError());
+    // g. CircProjecter (timestepping.jl:156-171): Gamma_1 = Gamma_s1 - Ainv_1 C^T E^T Fb
+    CE(reg_scatter_rot<double>(g, h->fb, h->body_idx, h->weight, h->nb, h->qtmp, h->gtmp, 1, h->nf, h->status + 1, s));
+    CE(poisson(h, h->gtmp, gs, 1, nullptr, h->mCN1, 0, gs, h->w1));
+  }
+  // h. Vort2Flux on the new state (timestepping.jl:285): gs is the new Gamma
+  CE(vort2flux(h, gs, h->psi, h->q, nullptr, h->rings));
+  return cudaSuccess;
+}
+
+int check_status(ib_handle* h) {
+  int st[3] = {0, 0, 0};
+  CK(cudaMemcpyAsync(st, h->status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (st[0]) return fail(h, IB_ERR_BODY_OUT_OF_GRID, "body point within 7 cells of the finest-grid edge");
+  if (st[1]) return fail(h, IB_ERR_NONFINITE, "infinite flux");
+  if (st[2]) return fail(h, IB_ERR_SINGULAR, "zero or non-finite pivot in the Schur matrix");
+  return IB_OK;
+}
+
+// host copy of the spectral multipliers, x16 for the F-convention transforms
+void build_multipliers(const ib_handle* h, std::vector<double>& lap, std::vector<double>& cn1,
+                       std::vector<double>& cn2) {
+  const Geometry& g = h->g;
+  const int nx = g.nx, ny = g.ny, ncol = nx - 1, nrow = ny - 1;
+  const double pi = 3.14159265358979323846;
+  const double scale = 1.0 / (4.0 * nx * ny);
+  std::vector<double> ci(ncol), cj(nrow);
+  for (int i = 0; i < ncol; ++i) ci[i] = std::cos(pi * (double)(i + 1) / nx);
+  for (int j = 0; j < nrow; ++j) cj[j] = std::cos(pi * (double)(j + 1) / ny);
+  lap.assign((size_t)ncol * nrow, 0.0);
+  cn1.assign((size_t)g.nlev * ncol * nrow, 0.0);
+  cn2.assign((size_t)g.nlev * ncol * nrow, 0.0);
+  for (int I = 0; I < ncol; ++I)
+    for (int J = 0; J < nrow; ++J) {
+      const double lam = -2.0 * (ci[I] + cj[J] - 2.0);  // lap_eigs, fluid-ops.jl:58-61
+      const size_t idx = (size_t)I * nrow + J;           // spectral column-major
+      lap[idx] = 16.0 * (scale / lam);
+      for (int l = 0; l < g.nlev; ++l) {
+        const double hc = g.h * std::ldexp(1.0, l);
+        const double expl = 1.0 / (1.0 - lam * h->dt / (2.0 * h->re * (hc * hc)));  // cnab/ops.jl:26
+        const double impl = 1.0 + lam * h->dt / (2.0 * h->re * (hc * hc));          // cnab/ops.jl:29
+        cn1[(size_t)l * ncol * nrow + idx] = 16.0 * (scale / impl);
+        cn2[(size_t)l * ncol * nrow + idx] = 1.0 / expl;
+      }
+    }
+}
+
+// Schur matrix assembly (cnab/ops.jl:79-94 with B_Times, ops.jl:125-143), `nc` columns per
+// batch of device solves; then inverse (ops.jl:96) and a row-major copy for the step's gemv.
+int assemble_schur(ib_handle* h) {
+  const Geometry& g = h->g;
+  const int L = g.nlev, nf = h->nf;
+  const int64_t nG = g.nG;
+  size_t freeb = 0, totb = 0;
+  CK(cudaMemGetInfo(&freeb, &totb));
+  const double per_col = 8.0 * ((2.0 * L + 2.0) * nG + g.nq + g.nbc);
+  double budget = 0.25 * (double)freeb;
+  if (budget > 16e9) budget = 16e9;
+  int nc = (int)(budget / per_col);
+  if (nc > 64) nc = 64;
+  if (nc > nf) nc = nf;
+  if (nc < 1) return fail(h, IB_ERR_CUDA, "not enough device memory for the Schur assembly");
+  double *Gb, *Pb, *Wa, *Wb, *Qb, *Rb;
+  CK(cudaMalloc(&Gb, sizeof(double) * L * nc * nG));
+  CK(cudaMalloc(&Pb, sizeof(double) * L * nc * nG));
+  CK(cudaMalloc(&Wa, sizeof(double) * nc * nG));
+  CK(cudaMalloc(&Wb, sizeof(double) * nc * nG));
+  CK(cudaMalloc(&Qb, sizeof(double) * nc * g.nq));
+  CK(cudaMalloc(&Rb, sizeof(double) * nc * g.nbc));
+  cudaStream_t s = h->stream;
+  int rc = IB_OK;
+  for (int c0 = 0; c0 < nf && rc == IB_OK; c0 += nc) {
+    const int n = (nf - c0 < nc) ? nf - c0 : nc;
+    auto run = [&]() -> cudaError_t {
+      CE(unit_scatter_rot<double>(g, h->body_idx, h->weight, h->nb, c0, n, Wa, s));
+      CE(poisson(h, Wa, Gb, n, nullptr, h->mCN1, 0, nullptr, Wb));
+      if (L > 1) CE(cudaMemsetAsync(Gb + (int64_t)n * nG, 0, sizeof(double) * (L - 1) * n * nG, s));
+      for (int l = 1; l < L; ++l)
+        CE(coarsify<double>(g, Gb + (int64_t)l * n * nG, Gb + (int64_t)(l - 1) * n * nG, n, nG, s));
+      CE(poisson(h, Gb + (int64_t)(L - 1) * n * nG, Pb + (int64_t)(L - 1) * n * nG, n, nullptr, h->mLap, 0, nullptr, Wb));
+      for (int l = L - 2; l >= 0; --l) {
+        CE(get_bc<double>(g, Pb + (int64_t)(l + 1) * n * nG, Rb, n, 1.0, s));
+        CE(poisson(h, Gb + (int64_t)l * n * nG, Pb + (int64_t)l * n * nG, n, Rb, h->mLap, 0, nullptr, Wb));
+      }
+      CE(curl<double>(g, Pb, L > 1 ? Rb : nullptr, Qb, n, s));
+      CE(reg_gather<double>(g, Qb, nullptr, h->body_idx, h->weight, h->nb, h->bmat + (int64_t)c0 * nf, n, g.nq, nf, s));
+      return cudaSuccess;
+    };
+    cudaError_t e = run();
+    if (e != cudaSuccess) rc = fail(h, IB_ERR_CUDA, "Schur assembly", e);
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(Gb); cudaFree(Pb); cudaFree(Wa); cudaFree(Wb); cudaFree(Qb); cudaFree(Rb);
+  if (rc != IB_OK) return rc;
+  // inverse (column-major), then the row-major copy
+  CK(cudaMemcpyAsync(h->binv_cm, h->bmat, sizeof(double) * (size_t)nf * nf, cudaMemcpyDeviceToDevice, s));
+  double* work = nullptr;
+  CK(cudaMalloc(&work, invert_workspace_bytes(nf)));
+  cudaError_t e = invert_inplace(h->binv_cm, nf, work, h->status + 2, s);
+  if (e != cudaSuccess) { cudaFree(work); return fail(h, IB_ERR_CUDA, "Schur inverse", e); }
+  // column-major (nf x nf) read as row-major is the transpose: transpose it back
+  CK(transpose(h->binv_cm, h->binv_rm, nf, nf, s));
+  CK(cudaStreamSynchronize(s));
+  cudaFree(work);
+  return IB_OK;
+}
+
+// Launch every kernel variant once outside of any capture (sets shared-memory attributes).
+int prime_kernels(ib_handle* h) {
+  const Geometry& g = h->g;
+  CK(poisson(h, h->w2, h->w2, 1, h->rings, h->mLap, 0, nullptr, h->w1));
+  CK(poisson(h, h->w2, h->w2, 1, nullptr, h->mLap, 0, h->w2, h->w1));
+  YPassArgs<double> ya{};
+  ya.in1 = h->w1;
+  ya.in2 = h->w2;
+  ya.out = h->w1;
+  ya.batch = 1;
+  ya.stride = g.nG;
+  ya.m1 = h->mCN1;
+  ya.m2 = h->mCN2;
+  ya.mstride = g.nG;
+  ya.op = SpecOp::kCn;
+  CK(ypass<double>(g, h->axy.d, ya, h->stream));
+  CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
+  CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return IB_OK;
+}
+
+int capture_graphs(ib_handle* h) {
+  for (int p = 0; p < 2; ++p) {
+    if (h->gexec[p]) { cudaGraphExecDestroy(h->gexec[p]); h->gexec[p] = nullptr; }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_step(h, p);
+    cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
+    if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return fail(h, IB_ERR_CUDA, "step capture", e); }
+    if (e2 != cudaSuccess) return fail(h, IB_ERR_CUDA, "step capture", e2);
+    size_t nn = 0;
+    if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+      std::vector<cudaGraphNode_t> nodes(nn);
+      cudaGraphGetNodes(graph, nodes.data(), &nn);
+      int k = 0;
+      for (auto nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++k;
+      }
+      h->kernels_per_step = k;
+    }
+    e = cudaGraphInstantiate(&h->gexec[p], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "graph instantiate", e);
+  }
+  return IB_OK;
+}
+
+void destroy_handle(ib_handle* h) {
+  if (!h) return;
+  if (h->device >= 0) cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& ge : h->gexec)
+    if (ge) cudaGraphExecDestroy(ge);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->h_q0) cudaFreeHost(h->h_q0);
+  h->axx.release();
+  h->axy.release();
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int stage_q0(ib_handle* h, double u, double v) {
+  const int L = h->g.nlev;
+  if (h->q0_slot >= kQ0Slots) {
+    CK(cudaStreamSynchronize(h->stream));
+    h->q0_slot = 0;
+  }
+  double* slot = h->h_q0 + (size_t)h->q0_slot * 2 * L;
+  h->q0_slot++;
+  for (int l = 0; l < L; ++l) {
+    const double hc = h->g.h * std::ldexp(1.0, l);  // gridstep(grid, lev), fluids.jl:102
+    slot[2 * l] = u * hc;                            // base_flux!, fluid-ops.jl:414-415
+    slot[2 * l + 1] = v * hc;
+  }
+  CK(cudaMemcpyAsync(h->d_q0, slot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, h->stream));
+  return IB_OK;
+}
+
+int one_step(ib_handle* h, double t, double u, double v) {
+  int rc = stage_q0(h, u, v);
+  if (rc != IB_OK) return rc;
+  if (h->use_graph) {
+    CK(cudaGraphLaunch(h->gexec[h->parity], h->stream));
+  } else {
+    CK(enqueue_step(h, h->parity));
+  }
+  h->parity ^= 1;
+  h->steps++;
+  h->t = t;
+  return IB_OK;
+}
+
+}  // namespace
+
+// ================================================================================================
+// C ABI
+// ================================================================================================
+extern "C" {
+
+const char* ib_status_string(int status) {
+  switch (status) {
+    case IB_OK: return "ok";
+    case IB_ERR_INVALID: return "invalid argument";
+    case IB_ERR_CUDA: return "CUDA error";
+    case IB_ERR_NONFINITE: return "infinite flux";
+    case IB_ERR_BODY_OUT_OF_GRID: return "body outside the finest grid";
+    case IB_ERR_SINGULAR: return "singular Schur matrix";
+    case IB_ERR_CG_MAXITER: return "Schur CG iteration cap reached";
+    case IB_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+const char* ib_last_error(const ib_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> lock(g_err_mu);
+  return g_create_err.c_str();
+}
+
+int ib_create(const ib_problem* p, ib_handle** out) {
+  const auto t_start = std::chrono::steady_clock::now();
+  ib_handle* h = nullptr;
+  if (!p || !out) return fail(nullptr, IB_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (p->nlevels < 1 || p->nx < 8 || p->ny < 8 || !(p->h > 0) || !(p->dt > 0) || !(p->re > 0))
+    return fail(nullptr, IB_ERR_INVALID, "invalid grid or scheme parameters");
+  if (!dst_axis_supported(p->nx) || !dst_axis_supported(p->ny))
+    return fail(nullptr, IB_ERR_INVALID,
+                "nx and ny must be multiples of 4, at most 2048, with n/2 a product of 2, 3 and 5");
+  if (p->precision != IB_PREC_FP64) return fail(nullptr, IB_ERR_UNSUPPORTED, "precision mode not available");
+  if (p->motion != IB_MOTION_STATIC) return fail(nullptr, IB_ERR_UNSUPPORTED, "moving bodies not available");
+  int nb = 0;
+  if (p->nbodies < 0) return fail(nullptr, IB_ERR_INVALID, "negative body count");
+  for (int b = 0; b < p->nbodies; ++b) {
+    if (!p->body_npoints || p->body_npoints[b] < 0) return fail(nullptr, IB_ERR_INVALID, "bad body point count");
+    nb += p->body_npoints[b];
+  }
+  if (nb > 0 && (!p->xb || !p->ds)) return fail(nullptr, IB_ERR_INVALID, "missing body points");
+  h = new ib_handle();
+  h->device = p->device;
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e != cudaSuccess) { int rc = fail(nullptr, IB_ERR_CUDA, "cudaSetDevice", e); delete h; return rc; }
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { int rc = fail(nullptr, IB_ERR_CUDA, "cudaStreamCreate", e); h->stream = nullptr; destroy_handle(h); return rc; }
+  auto bail = [&](int rc) {
+    {
+      std::lock_guard<std::mutex> lock(g_err_mu);
+      g_create_err = h->err;
+    }
+    destroy_handle(h);
+    return rc;
+  };
+  h->g = make_geometry(p->nx, p->ny, p->nlevels, p->h, p->x0, p->y0);
+  h->dt = p->dt;
+  h->re = p->re;
+  h->beta0 = p->beta0;
+  h->beta1 = p->beta1;
+  h->nbodies = p->nbodies;
+  h->nb = nb;
+  h->nf = 2 * nb;
+  h->precision = p->precision;
+  h->hist_cap = p->history_capacity > 0 ? p->history_capacity : 4096;
+  if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
+  const Geometry& g = h->g;
+  const int L = g.nlev;
+  const int64_t nG = g.nG;
+  if ((e = h->axx.build(g.nx)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "x transform tables", e));
+  if ((e = h->axy.build(g.ny)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "y transform tables", e));
+#define AL(ptr, n)                                                                       \
+  do {                                                                                   \
+    cudaError_t ea = h->alloc(&(ptr), (size_t)(n));                                      \
+    if (ea != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "device allocation", ea));   \
+  } while (0)
+  AL(h->G[0], L * nG); AL(h->G[1], L * nG);
+  AL(h->N[0], L * nG); AL(h->N[1], L * nG);
+  AL(h->psi, L * nG); AL(h->q, (int64_t)L * g.nq);
+  AL(h->fb, h->nf);
+  AL(h->rhs, L * nG); AL(h->w1, L * nG); AL(h->w2, L * nG);
+  AL(h->qs1, g.nq); AL(h->qtmp, g.nq); AL(h->gtmp, nG);
+  AL(h->bcn, (int64_t)L * g.nbc); AL(h->edges, (int64_t)L * (2 * (g.nx - 1) + 2 * (g.ny - 1)));
+  AL(h->rings, (int64_t)L * g.nbc);
+  AL(h->mLap, nG); AL(h->mCN1, L * nG); AL(h->mCN2, L * nG);
+  AL(h->d_fac, L); AL(h->d_q0, 2 * L); AL(h->d_inv_hc2, L);
+  AL(h->status, 4); AL(h->d_counter, 1);
+  AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
+  AL(h->hist, (int64_t)h->hist_cap * 2 * (h->nbodies > 0 ? h->nbodies : 1));
+  AL(h->stress, h->nf);
+  if ((e = cudaMallocHost(&h->h_q0, sizeof(double) * kQ0Slots * 2 * L)) != cudaSuccess) {
+    h->h_q0 = nullptr;
+    return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
+  }
+  {
+    std::vector<double> lap, cn1, cn2;
+    build_multipliers(h, lap, cn1, cn2);
+    std::vector<double> fac(L), ihc(L);
+    for (int l = 0; l < L; ++l) {
+      const double hc = g.h * std::ldexp(1.0, l);
+      fac[l] = 0.25 * h->dt / (h->re * (hc * hc));  // timestepping.jl:50
+      ihc[l] = 1.0 / (hc * hc);                     // cnab/ops.jl:162-163
+    }
+    if ((e = cudaMemcpy(h->mLap, lap.data(), sizeof(double) * lap.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->mCN1, cn1.data(), sizeof(double) * cn1.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->mCN2, cn2.data(), sizeof(double) * cn2.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_fac, fac.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_inv_hc2, ihc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+  }
+  if (nb > 0) {
+    AL(h->xb, 2 * nb); AL(h->ds, nb); AL(h->weight, (int64_t)nb * 2 * kWin2);
+    AL(h->body_idx, 2 * nb); AL(h->body_start, h->nbodies + 1);
+    AL(h->bmat, (int64_t)h->nf * h->nf); AL(h->binv_cm, (int64_t)h->nf * h->nf);
+    AL(h->binv_rm, (int64_t)h->nf * h->nf); AL(h->ftmp, h->nf);
+    std::vector<int> bs(h->nbodies + 1, 0);
+    for (int b = 0; b < h->nbodies; ++b) bs[b + 1] = bs[b] + p->body_npoints[b];
+    if ((e = cudaMemcpy(h->xb, p->xb, sizeof(double) * 2 * nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->ds, p->ds, sizeof(double) * nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->body_start, bs.data(), sizeof(int) * bs.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "body upload", e));
+    if ((e = reg_update(g, h->xb, nb, h->body_idx, h->weight, h->status, h->stream)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "delta weights", e));
+    int rc = check_status(h);
+    if (rc != IB_OK) return bail(rc);
+  }
+#undef AL
+  {
+    int rc = prime_kernels(h);
+    if (rc != IB_OK) return bail(rc);
+  }
+  if (nb > 0) {
+    int rc = assemble_schur(h);
+    if (rc != IB_OK) return bail(rc);
+    rc = check_status(h);
+    if (rc != IB_OK) return bail(rc);
+  }
+  if (h->use_graph) {
+    int rc = capture_graphs(h);
+    if (rc != IB_OK) return bail(rc);
+  }
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "setup", e));
+  h->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  *out = h;
+  return IB_OK;
+}
+
+int ib_destroy(ib_handle* h) {
+  destroy_handle(h);
+  return IB_OK;
+}
+
+int ib_set_state(ib_handle* h, const double* gamma, const double* q, const double* psi, const double* nonlin1,
+                 const double* nonlin2, const double* fb, double t) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  const Geometry& g = h->g;
+  const size_t nGL = sizeof(double) * g.nlev * g.nG, nqL = sizeof(double) * g.nlev * g.nq;
+  const int p = h->parity;
+  cudaStream_t s = h->stream;
+  CK(cudaStreamSynchronize(s));
+  if (gamma) CK(cudaMemcpyAsync(h->G[p], gamma, nGL, cudaMemcpyHostToDevice, s));
+  if (q) CK(cudaMemcpyAsync(h->q, q, nqL, cudaMemcpyHostToDevice, s));
+  if (psi) CK(cudaMemcpyAsync(h->psi, psi, nGL, cudaMemcpyHostToDevice, s));
+  if (nonlin1) CK(cudaMemcpyAsync(h->N[p], nonlin1, nGL, cudaMemcpyHostToDevice, s));
+  if (nonlin2) CK(cudaMemcpyAsync(h->N[p ^ 1], nonlin2, nGL, cudaMemcpyHostToDevice, s));
+  if (fb && h->nf) CK(cudaMemcpyAsync(h->fb, fb, sizeof(double) * h->nf, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  h->t = t;
+  return IB_OK;
+}
+
+int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* nonlin1, double* nonlin2, double* fb,
+                 double* t) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  const Geometry& g = h->g;
+  const size_t nGL = sizeof(double) * g.nlev * g.nG, nqL = sizeof(double) * g.nlev * g.nq;
+  const int p = h->parity;
+  cudaStream_t s = h->stream;
+  if (gamma) CK(cudaMemcpyAsync(gamma, h->G[p], nGL, cudaMemcpyDeviceToHost, s));
+  if (q) CK(cudaMemcpyAsync(q, h->q, nqL, cudaMemcpyDeviceToHost, s));
+  if (psi) CK(cudaMemcpyAsync(psi, h->psi, nGL, cudaMemcpyDeviceToHost, s));
+  if (nonlin1) CK(cudaMemcpyAsync(nonlin1, h->N[p], nGL, cudaMemcpyDeviceToHost, s));
+  if (nonlin2) CK(cudaMemcpyAsync(nonlin2, h->N[p ^ 1], nGL, cudaMemcpyDeviceToHost, s));
+  if (fb && h->nf) CK(cudaMemcpyAsync(fb, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (t) *t = h->t;
+  return check_status(h);
+}
+
+int ib_advance(ib_handle* h, double t, double u, double v) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  int rc = one_step(h, t, u, v);
+  if (rc != IB_OK) return rc;
+  return check_status(h);
+}
+
+int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv) {
+  if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  for (int i = 0; i < n; ++i) {
+    int rc = one_step(h, t[i], uv[2 * i], uv[2 * i + 1]);
+    if (rc != IB_OK) return rc;
+  }
+  return check_status(h);
+}
+
+int ib_vort2flux(ib_handle* h) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  CK(vort2flux(h, h->G[h->parity], h->psi, h->q, nullptr, h->rings));
+  CK(cudaStreamSynchronize(h->stream));
+  return IB_OK;
+}
+
+int ib_get_stress(ib_handle* h, double* cd, double* cl, double* fb_surface) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  const int nbd = h->nbodies;
+  if (nbd == 0) return IB_OK;
+  std::vector<double> v(2 * nbd);
+  CK(cudaMemcpyAsync(v.data(), h->cdcl, sizeof(double) * 2 * nbd, cudaMemcpyDeviceToHost, h->stream));
+  if (fb_surface && h->nf)
+    CK(cudaMemcpyAsync(fb_surface, h->stress, sizeof(double) * h->nf, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int b = 0; b < nbd; ++b) {
+    if (cd) cd[b] = v[2 * b];
+    if (cl) cl[b] = v[2 * b + 1];
+  }
+  return IB_OK;
+}
+
+int ib_get_force_history(ib_handle* h, int32_t count, double* cd, double* cl) {
+  if (!h || count < 0) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  const int nbd = h->nbodies;
+  if (nbd == 0 || count == 0) return IB_OK;
+  if (count > h->hist_cap || count > h->steps) return fail(h, IB_ERR_INVALID, "history count exceeds recorded steps");
+  std::vector<double> all((size_t)h->hist_cap * 2 * nbd);
+  CK(cudaMemcpyAsync(all.data(), h->hist, sizeof(double) * all.size(), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int i = 0; i < count; ++i) {
+    const int64_t step = h->steps - count + i;
+    const int64_t slot = step % h->hist_cap;
+    for (int b = 0; b < nbd; ++b) {
+      if (cd) cd[(int64_t)i * nbd + b] = all[(size_t)slot * 2 * nbd + 2 * b];
+      if (cl) cl[(int64_t)i * nbd + b] = all[(size_t)slot * 2 * nbd + 2 * b + 1];
+    }
+  }
+  return IB_OK;
+}
+
+int64_t ib_step_count(const ib_handle* h) { return h ? h->steps : 0; }
+
+int ib_synchronize(ib_handle* h) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  return check_status(h);
+}
+
+// ------------------------------------------------------------------------------------------------
+// diagnostics (include/ibgb300_diag.h)
+// ------------------------------------------------------------------------------------------------
+int ib_get_info(ib_handle* h, ib_info* info) {
+  if (!h || !info) return IB_ERR_INVALID;
+  info->kernels_per_step = h->kernels_per_step;
+  info->nx = h->g.nx;
+  info->ny = h->g.ny;
+  info->nlevels = h->g.nlev;
+  info->nbodies = h->nbodies;
+  info->npoints = h->nb;
+  info->device_bytes = h->device_bytes;
+  info->setup_ms = h->setup_ms;
+  return IB_OK;
+}
+
+int ib_advance_n_timed(ib_handle* h, int32_t n, const double* t, const double* uv, double* device_ms) {
+  if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  int rc = IB_OK;
+  for (int i = 0; i < n && rc == IB_OK; ++i) rc = one_step(h, t[i], uv[2 * i], uv[2 * i + 1]);
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (device_ms) *device_ms = ms;
+  if (rc != IB_OK) return rc;
+  return check_status(h);
+}
+
+int ib_profile_steps(ib_handle* h, int32_t n, const double* t, const double* uv, int32_t kernel_class,
+                     double* total_ms, int64_t* launches) {
+  if (!h || n < 0 || (n > 0 && (!t || !uv)) || kernel_class < 0 || kernel_class >= kClassCount)
+    return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  Prof prof;
+  prof.cls = kernel_class;
+  g_prof = &prof;
+  const bool graph = h->use_graph;
+  h->use_graph = false;
+  int rc = IB_OK;
+  for (int i = 0; i < n && rc == IB_OK; ++i) rc = one_step(h, t[i], uv[2 * i], uv[2 * i + 1]);
+  h->use_graph = graph;
+  g_prof = nullptr;
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  double sum = 0.0;
+  for (size_t i = 0; i + 1 < prof.used; i += 2) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, prof.ev[i], prof.ev[i + 1]) == cudaSuccess) sum += ms;
+  }
+  for (auto ev : prof.ev) cudaEventDestroy(ev);
+  if (total_ms) *total_ms = sum;
+  if (launches) *launches = (int64_t)(prof.used / 2);
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "profiled steps", e);
+  if (rc != IB_OK) return rc;
+  return check_status(h);
+}
+
+// ------------------------------------------------------------------------------------------------
+// operator entry points (device pointers)
+// ------------------------------------------------------------------------------------------------
+#define OP_BEGIN()                         \
+  if (!h) return IB_ERR_INVALID;           \
+  CK(cudaSetDevice(h->device));            \
+  const Geometry& g = h->g;                \
+  cudaStream_t s = h->stream;              \
+  (void)g;                                 \
+  (void)s;
+#define OP_END()                      \
+  CK(cudaGetLastError());             \
+  CK(cudaStreamSynchronize(s));       \
+  return IB_OK;
+
+int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out) {
+  OP_BEGIN();
+  if (batch < 1) return IB_ERR_INVALID;
+  double* w;
+  CK(cudaMalloc(&w, sizeof(double) * batch * g.nG));
+  // RODFT00 in both dimensions = 4 F_y F_x (F: the half-scaled transform of dst.cu)
+  XPassArgs<double> xa{};
+  xa.in = in; xa.out = w; xa.batch = batch; xa.stride = g.nG;
+  cudaError_t e = xpass<double>(g, h->axx.d, xa, s);
+  YPassArgs<double> ya{};
+  ya.in1 = w; ya.out = out; ya.batch = batch; ya.stride = g.nG; ya.op = SpecOp::kFwd; ya.scal = 4.0;
+  if (e == cudaSuccess) e = ypass<double>(g, h->axy.d, ya, s);
+  cudaStreamSynchronize(s);
+  cudaFree(w);
+  CK(e);
+  OP_END();
+}
+
+int ib_op_laplacian_inv(ib_handle* h, int32_t batch, const double* b, double* x) {
+  OP_BEGIN();
+  if (batch < 1) return IB_ERR_INVALID;
+  double* w;
+  CK(cudaMalloc(&w, sizeof(double) * batch * g.nG));
+  cudaError_t e = poisson(h, b, x, batch, nullptr, h->mLap, 0, nullptr, w);
+  cudaStreamSynchronize(s);
+  cudaFree(w);
+  CK(e);
+  OP_END();
+}
+
+static int cn_op(ib_handle* h, int32_t lev, const double* b, double* x, bool inverse) {
+  OP_BEGIN();
+  if (lev < 1 || lev > g.nlev) return IB_ERR_INVALID;
+  double *w, *m;
+  CK(cudaMalloc(&w, sizeof(double) * g.nG));
+  CK(cudaMalloc(&m, sizeof(double) * g.nG));
+  cudaError_t e;
+  const int64_t off = (int64_t)(lev - 1) * g.nG;
+  if (inverse) {
+    e = poisson(h, b, x, 1, nullptr, h->mCN1 + off, 0, nullptr, w);
+  } else {
+    // A multiplier = 16 * scale / Lambda_expl = 16 * scale * cn2 ; build it on the device
+    e = cudaMemcpyAsync(m, h->mCN2 + off, sizeof(double) * g.nG, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = axpby<double>(m, m, 16.0 / (4.0 * g.nx * g.ny), 0.0, g.nG, s);
+    if (e == cudaSuccess) e = poisson(h, b, x, 1, nullptr, m, 0, nullptr, w);
+  }
+  cudaStreamSynchronize(s);
+  cudaFree(w);
+  cudaFree(m);
+  CK(e);
+  OP_END();
+}
+
+int ib_op_cn_a(ib_handle* h, int32_t lev, const double* b, double* x) { return cn_op(h, lev, b, x, false); }
+int ib_op_cn_ainv(ib_handle* h, int32_t lev, const double* b, double* x) { return cn_op(h, lev, b, x, true); }
+
+int ib_op_curl(ib_handle* h, const double* psi, const double* bc, double* q) {
+  OP_BEGIN();
+  CK(curl<double>(g, psi, bc, q, 1, s));
+  OP_END();
+}
+
+int ib_op_rot(ib_handle* h, const double* q, double* gamma) {
+  OP_BEGIN();
+  CK(rot<double>(g, q, gamma, 1, s));
+  OP_END();
+}
+
+int ib_op_coarsify(ib_handle* h, double* gc, const double* gf) {
+  OP_BEGIN();
+  CK(coarsify<double>(g, gc, gf, 1, g.nG, s));
+  OP_END();
+}
+
+int ib_op_get_bc(ib_handle* h, const double* r, double* bc) {
+  OP_BEGIN();
+  CK(get_bc<double>(g, r, bc, 1, 1.0, s));
+  OP_END();
+}
+
+int ib_op_apply_bc(ib_handle* h, double* r, const double* bc, double fac) {
+  OP_BEGIN();
+  CK(apply_bc<double>(g, r, bc, fac, 1, s));
+  OP_END();
+}
+
+int ib_op_nonlinear(ib_handle* h, int32_t lev, const double* q, double u, double v, const double* gamma,
+                    const double* bc, double* nonlin) {
+  OP_BEGIN();
+  if (lev < 1 || lev > g.nlev) return IB_ERR_INVALID;
+  Geometry g1 = g;
+  g1.nlev = 1;
+  const double hc = g.h * std::ldexp(1.0, lev - 1);
+  double par[3] = {u * hc, v * hc, 1.0 / (hc * hc)};
+  double *dpar, *zero_ring, *zero_g, *scratch, *edges;
+  const int ne = 2 * (g.nx - 1) + 2 * (g.ny - 1);
+  CK(cudaMalloc(&dpar, sizeof(par)));
+  CK(cudaMalloc(&zero_ring, sizeof(double) * g.nbc));
+  CK(cudaMalloc(&zero_g, sizeof(double) * g.nG));
+  CK(cudaMalloc(&scratch, sizeof(double) * g.nG));
+  CK(cudaMalloc(&edges, sizeof(double) * ne));
+  CK(cudaMemcpyAsync(dpar, par, sizeof(par), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(zero_ring, 0, sizeof(double) * g.nbc, s));
+  CK(cudaMemsetAsync(zero_g, 0, sizeof(double) * g.nG, s));
+  CK(cudaMemsetAsync(edges, 0, sizeof(double) * ne, s));
+  NonlinArgs<double> na{};
+  na.q = q;
+  na.gamma = gamma;
+  na.bcn = bc ? bc : zero_ring;
+  na.nl_old = zero_g;
+  na.edges = edges;
+  na.nl_new = nonlin;
+  na.rhs = scratch;
+  na.q0 = dpar;
+  na.inv_hc2 = dpar + 2;
+  na.dtb0 = 0.0;
+  na.dtb1 = 0.0;
+  cudaError_t e = nonlin_rhs<double>(g1, na, s);
+  cudaStreamSynchronize(s);
+  cudaFree(dpar); cudaFree(zero_ring); cudaFree(zero_g); cudaFree(scratch); cudaFree(edges);
+  CK(e);
+  OP_END();
+}
+
+int ib_op_vort2flux(ib_handle* h, double* gamma, double* psi, double* q) {
+  OP_BEGIN();
+  double* rings;
+  CK(cudaMalloc(&rings, sizeof(double) * g.nlev * g.nbc));
+  cudaError_t e = vort2flux(h, gamma, psi, q, nullptr, rings);
+  cudaStreamSynchronize(s);
+  cudaFree(rings);
+  CK(e);
+  OP_END();
+}
+
+int ib_op_reg_gather(ib_handle* h, const double* q, double u, double v, double* fb) {
+  OP_BEGIN();
+  if (h->nb == 0) return IB_OK;
+  double par[2] = {u * g.h, v * g.h};
+  double* dpar;
+  CK(cudaMalloc(&dpar, sizeof(par)));
+  CK(cudaMemcpyAsync(dpar, par, sizeof(par), cudaMemcpyHostToDevice, s));
+  cudaError_t e = reg_gather<double>(g, q, dpar, h->body_idx, h->weight, h->nb, fb, 1, g.nq, h->nf, s);
+  cudaStreamSynchronize(s);
+  cudaFree(dpar);
+  CK(e);
+  OP_END();
+}
+
+int ib_op_reg_scatter(ib_handle* h, const double* fb, double* q) {
+  OP_BEGIN();
+  CK(cudaMemsetAsync(q, 0, sizeof(double) * g.nq, s));
+  if (h->nb == 0) { OP_END(); }
+  CK(reg_scatter<double>(g, fb, h->body_idx, h->weight, h->nb, q, h->status + 1, s));
+  CK(cudaStreamSynchronize(s));
+  return check_status(h);
+}
+
+int ib_get_schur(ib_handle* h, double* bmat, double* binv) {
+  OP_BEGIN();
+  const size_t bytes = sizeof(double) * (size_t)h->nf * h->nf;
+  if (h->nf == 0) return IB_OK;
+  if (bmat) CK(cudaMemcpyAsync(bmat, h->bmat, bytes, cudaMemcpyDeviceToHost, s));
+  if (binv) CK(cudaMemcpyAsync(binv, h->binv_cm, bytes, cudaMemcpyDeviceToHost, s));
+  OP_END();
+}
+
+int ib_get_reg(ib_handle* h, int32_t* body_idx, double* weight) {
+  OP_BEGIN();
+  if (h->nb == 0) return IB_OK;
+  if (body_idx) CK(cudaMemcpyAsync(body_idx, h->body_idx, sizeof(int) * 2 * h->nb, cudaMemcpyDeviceToHost, s));
+  if (weight) CK(cudaMemcpyAsync(weight, h->weight, sizeof(double) * h->nb * 2 * kWin2, cudaMemcpyDeviceToHost, s));
+  OP_END();
+}
+
+}  // extern "C"

@@ -1,0 +1,330 @@
+// Stencil kernels of the stream-function discretisation.
+//
+// Each kernel restates one operator of src/streamfcn/fluid-ops.jl (cited per kernel) on the
+// reference's own column-major layouts.  Grid-stride loops, one thread per output value.
+#include "ib_common.cuh"
+
+namespace ib {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int blocks_for(int64_t n) {
+  int64_t b = (n + kThreads - 1) / kThreads;
+  if (b > 65535LL * 8) b = 65535LL * 8;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// get_bc! value at ring index idx (fluid-ops.jl:210-239), including the final *0.25.
+template <typename T>
+__device__ __forceinline__ T ring_value(const Geometry& g, const T* __restrict__ r, int idx) {
+  const int nx = g.nx, ny = g.ny, ncol = nx - 1;
+  const int nx4 = nx / 4, ny4 = ny / 4;
+  T v;
+  if (idx < g.B) {  // left (idx < R) or right block, node along y
+    const bool right = idx >= g.R;
+    const int jb = idx - (right ? g.R : g.L);
+    const int col = right ? 3 * nx4 - 1 : nx4 - 1;
+    if ((jb & 1) == 0) {
+      const int t = jb >> 1;
+      v = r[(ny4 - 1 + t) * ncol + col];
+    } else {
+      const int t = (jb + 1) >> 1;
+      v = T(0.5) * (r[(ny4 - 1 + t) * ncol + col] + r[(ny4 - 2 + t) * ncol + col]);
+    }
+  } else {  // bottom (idx < T) or top block, node along x
+    const bool top = idx >= g.T;
+    const int ib = idx - (top ? g.T : g.B);
+    const int row = top ? 3 * ny4 - 1 : ny4 - 1;
+    if ((ib & 1) == 0) {
+      const int t = ib >> 1;
+      v = r[row * ncol + nx4 - 1 + t];
+    } else {
+      const int t = (ib + 1) >> 1;
+      v = T(0.5) * (r[row * ncol + nx4 - 1 + t] + r[row * ncol + nx4 - 2 + t]);
+    }
+  }
+  return v * T(0.25);
+}
+
+template <typename T>
+__global__ void k_get_bc(Geometry g, const T* __restrict__ r, T* __restrict__ bc, int batch, T extra) {
+  const int64_t total = (int64_t)batch * g.nbc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / g.nbc), idx = (int)(t - (int64_t)b * g.nbc);
+    T v = ring_value(g, r + (int64_t)b * g.nG, idx);
+    if (extra != T(1)) v *= extra;
+    bc[t] = v;
+  }
+}
+
+// apply_bc! (fluid-ops.jl:249-275): rows first, then columns (same order as the reference).
+template <typename T>
+__global__ void k_apply_bc_rows(Geometry g, T* __restrict__ r, const T* __restrict__ bc, T fac, int batch) {
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int64_t total = (int64_t)batch * ncol;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / ncol), I = (int)(t - (int64_t)b * ncol);
+    T* rr = r + (int64_t)b * g.nG;
+    const T* bb = bc + (int64_t)b * g.nbc;
+    rr[I] += fac * bb[g.B + 1 + I];
+    rr[(nrow - 1) * ncol + I] += fac * bb[g.T + 1 + I];
+  }
+}
+template <typename T>
+__global__ void k_apply_bc_cols(Geometry g, T* __restrict__ r, const T* __restrict__ bc, T fac, int batch) {
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int64_t total = (int64_t)batch * nrow;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / nrow), J = (int)(t - (int64_t)b * nrow);
+    T* rr = r + (int64_t)b * g.nG;
+    const T* bb = bc + (int64_t)b * g.nbc;
+    rr[J * ncol] += fac * bb[g.L + 1 + J];
+    rr[J * ncol + ncol - 1] += fac * bb[g.R + 1 + J];
+  }
+}
+
+// coarsify! (fluid-ops.jl:184-202)
+template <typename T>
+__global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__ gf, int batch, int64_t stride) {
+  const int ncol = g.nx - 1;
+  const int ct = g.nx / 2 - 1, cs = g.ny / 2 - 1;  // coarse centre extent
+  const int64_t per = (int64_t)ct * cs;
+  const int64_t total = (int64_t)batch * per;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / per);
+    const int rem = (int)(t - (int64_t)b * per);
+    const int s = rem / ct, tt = rem - s * ct;
+    const T* f = gf + (int64_t)b * stride;
+    const int J = 2 * s + 1, I = 2 * tt + 1;
+    const int c = J * ncol + I;
+    const T v = f[c]
+                + T(0.5) * (f[c + 1] + f[c + ncol] + f[c - 1] + f[c - ncol])
+                + T(0.25) * (f[c + ncol + 1] + f[c - ncol + 1] + f[c - ncol - 1] + f[c + ncol - 1]);
+    gc[(int64_t)b * stride + (int64_t)(g.ny / 4 + s) * ncol + g.nx / 4 + tt] = v;
+  }
+}
+
+// Multilevel curl! (fluid-ops.jl:138-182); bc == nullptr means a zero ring.
+template <typename T>
+__global__ void k_curl(Geometry g, const T* __restrict__ psi, const T* __restrict__ bc, T* __restrict__ q, int batch) {
+  const int nx = g.nx, ny = g.ny, ncol = nx - 1;
+  const int64_t total = (int64_t)batch * g.nq;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / g.nq), e = (int)(t - (int64_t)b * g.nq);
+    const T* p = psi + (int64_t)b * g.nG;
+    const T* c = bc ? bc + (int64_t)b * g.nbc : nullptr;
+#define BC(i) (c ? c[(i)] : T(0))
+    T v;
+    if (e < g.nu) {
+      const int J = e / (nx + 1), I = e - J * (nx + 1);
+      if (I == 0) v = BC(g.L + J + 1) - BC(g.L + J);
+      else if (I == nx) v = BC(g.R + J + 1) - BC(g.R + J);
+      else if (J == 0) v = p[I - 1] - BC(g.B + I);
+      else if (J == ny - 1) v = BC(g.T + I) - p[(ny - 2) * ncol + I - 1];
+      else v = p[J * ncol + I - 1] - p[(J - 1) * ncol + I - 1];
+    } else {
+      const int e2 = e - g.nu;
+      const int J = e2 / nx, I = e2 - J * nx;
+      if (J == 0) v = BC(g.B + I) - BC(g.B + I + 1);
+      else if (J == ny) v = BC(g.T + I) - BC(g.T + I + 1);
+      else if (I == 0) v = BC(g.L + J) - p[(J - 1) * ncol];
+      else if (I == nx - 1) v = p[(J - 1) * ncol + nx - 2] - BC(g.R + J);
+      else v = p[(J - 1) * ncol + I - 1] - p[(J - 1) * ncol + I];
+    }
+#undef BC
+    q[t] = v;
+  }
+}
+
+// rot! = C^T (fluid-ops.jl:117-129)
+template <typename T>
+__global__ void k_rot(Geometry g, const T* __restrict__ q, T* __restrict__ gam, int batch) {
+  const int nx = g.nx, ncol = nx - 1;
+  const int64_t total = (int64_t)batch * g.nG;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / g.nG), e = (int)(t - (int64_t)b * g.nG);
+    const int J = e / ncol, I = e - J * ncol;
+    const T* qx = q + (int64_t)b * g.nq;
+    const T* qy = qx + g.nu;
+    gam[t] = (qx[J * (nx + 1) + I + 1] - qx[(J + 1) * (nx + 1) + I + 1])
+             + (qy[(J + 1) * nx + I + 1] - qy[(J + 1) * nx + I]);
+  }
+}
+
+// ---- nonlinear term + explicit right-hand side (cnab/ops.jl:151-167, fluid-ops.jl:277-401,
+//      cnab/timestepping.jl:54-67) ----------------------------------------------------------
+template <typename T>
+struct LevelView {
+  const T* qx; const T* qy; const T* G; const T* bc;
+  T q0x, q0y;
+  int nx, ny, ncol;
+  // avg_flux!: Qx at (Jq in 1..ny-1, Iq in 0..nx), Qy at (Jq in 0..ny, Iq in 1..nx-1)
+  __device__ __forceinline__ T Qx(int Jq, int Iq) const {
+    return (((qx[Jq * (nx + 1) + Iq] + qx[(Jq - 1) * (nx + 1) + Iq]) + q0x) + q0x) / T(2);
+  }
+  __device__ __forceinline__ T Qy(int Jq, int Iq) const {
+    return (((qy[Jq * nx + Iq] + qy[Jq * nx + Iq - 1]) + q0y) + q0y) / T(2);
+  }
+  __device__ __forceinline__ T Gm(int J, int I) const { return G[J * ncol + I]; }
+};
+
+// fqx at (Jf, If), If in 1..nx-1 (direct_product_loops!, fluid-ops.jl:329-362)
+template <typename T>
+__device__ __forceinline__ T fqx_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qyHi, T qyLo) {
+  if (Jf == 0) return (qyHi * v.Gm(0, If - 1) + qyLo * v.bc[g.B + If]) / T(2);
+  if (Jf == v.ny - 1) return (qyLo * v.Gm(v.ny - 2, If - 1) + qyHi * v.bc[g.T + If]) / T(2);
+  return (qyHi * v.Gm(Jf, If - 1) + qyLo * v.Gm(Jf - 1, If - 1)) / T(2);
+}
+// fqy at (Jf, If), Jf in 1..ny-1 (fluid-ops.jl:365-398); qxHi = Qx(Jf, If+1), qxLo = Qx(Jf, If)
+template <typename T>
+__device__ __forceinline__ T fqy_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qxHi, T qxLo) {
+  if (If == 0) return -(qxHi * v.Gm(Jf - 1, 0) + qxLo * v.bc[g.L + Jf]) / T(2);
+  if (If == v.nx - 1) return -(qxLo * v.Gm(Jf - 1, v.nx - 2) + qxHi * v.bc[g.R + Jf]) / T(2);
+  return -(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1)) / T(2);
+}
+
+template <typename T>
+__global__ void k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
+  const int nx = g.nx, ny = g.ny, ncol = nx - 1, nrow = ny - 1;
+  const int ne = 2 * ncol + 2 * nrow;
+  const int64_t total = (int64_t)g.nlev * g.nG;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(t / g.nG), e = (int)(t - (int64_t)l * g.nG);
+    const int J = e / ncol, I = e - J * ncol;
+    LevelView<T> v;
+    v.qx = a.q + (int64_t)l * g.nq;
+    v.qy = v.qx + g.nu;
+    v.G = a.gamma + (int64_t)l * g.nG;
+    v.bc = a.bcn + (int64_t)l * g.nbc;
+    v.q0x = (T)a.q0[2 * l];
+    v.q0y = (T)a.q0[2 * l + 1];
+    v.nx = nx; v.ny = ny; v.ncol = ncol;
+    // the six averaged fluxes this node touches
+    const T qy0 = v.Qy(J, I + 1), qy1 = v.Qy(J + 1, I + 1), qy2 = v.Qy(J + 2, I + 1);
+    const T qx0 = v.Qx(J + 1, I), qx1 = v.Qx(J + 1, I + 1), qx2 = v.Qx(J + 1, I + 2);
+    const T fx_lo = fqx_at(g, v, J, I + 1, qy1, qy0);       // fqx[J,   I+1]
+    const T fx_hi = fqx_at(g, v, J + 1, I + 1, qy2, qy1);   // fqx[J+1, I+1]
+    const T fy_r = fqy_at(g, v, J + 1, I + 1, qx2, qx1);    // fqy[J+1, I+1]
+    const T fy_l = fqy_at(g, v, J + 1, I, qx1, qx0);        // fqy[J+1, I]
+    const T nl = ((fx_lo - fx_hi) + (fy_r - fy_l)) * (T)a.inv_hc2[l];
+    a.nl_new[t] = nl;
+    T r = (T)a.dtb0 * nl;
+    r = r + (T)a.dtb1 * a.nl_old[t];
+    const T* ed = a.edges + (int64_t)l * ne;
+    T edge = T(0);
+    if (J == 0) edge += ed[I];
+    if (J == nrow - 1) edge += ed[ncol + I];
+    if (I == 0) edge += ed[2 * ncol + J];
+    if (I == ncol - 1) edge += ed[2 * ncol + nrow + J];
+    a.rhs[t] = r + edge;
+  }
+}
+
+// Rings of the trial step (cnab/timestepping.jl:42-57): bcn[l] = 0.25 * get_bc(gamma[l+1]) for
+// l < nlev-1 (zero on the coarsest level) and the accumulated rhsbc edge vectors
+// edges[l] = sum_{l' = l}^{nlev-2} fac[l'] * get_bc(gamma[l'+1]) on the four edges.
+template <typename T>
+__global__ void k_trial_rings(Geometry g, const T* __restrict__ gamma, T* __restrict__ bcn, T* __restrict__ edges,
+                              const double* __restrict__ fac) {
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int ne = 2 * ncol + 2 * nrow;
+  const int nl = g.nlev;
+  const int64_t nb_total = (int64_t)nl * g.nbc;
+  const int64_t total = nb_total + (int64_t)nl * ne;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < nb_total) {
+      const int l = (int)(t / g.nbc), idx = (int)(t - (int64_t)l * g.nbc);
+      bcn[t] = (l < nl - 1) ? ring_value(g, gamma + (int64_t)(l + 1) * g.nG, idx) * T(0.25) : T(0);
+    } else {
+      const int64_t u = t - nb_total;
+      const int l = (int)(u / ne), e = (int)(u - (int64_t)l * ne);
+      int ridx;
+      if (e < ncol) ridx = g.B + 1 + e;
+      else if (e < 2 * ncol) ridx = g.T + 1 + (e - ncol);
+      else if (e < 2 * ncol + nrow) ridx = g.L + 1 + (e - 2 * ncol);
+      else ridx = g.R + 1 + (e - 2 * ncol - nrow);
+      T acc = T(0);
+      for (int lp = nl - 2; lp >= l; --lp) acc += (T)fac[lp] * ring_value(g, gamma + (int64_t)(lp + 1) * g.nG, ridx);
+      edges[u] = acc;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_fill(T* p, T v, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) p[t] = v;
+}
+template <typename T>
+__global__ void k_axpby(T* y, const T* x, T a, T b, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    y[t] = a * x[t] + b * y[t];
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t get_bc(const Geometry& g, const T* r, T* bc, int batch, T extra, cudaStream_t s) {
+  k_get_bc<T><<<blocks_for((int64_t)batch * g.nbc), kThreads, 0, s>>>(g, r, bc, batch, extra);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t apply_bc(const Geometry& g, T* r, const T* bc, T fac, int batch, cudaStream_t s) {
+  k_apply_bc_rows<T><<<blocks_for((int64_t)batch * (g.nx - 1)), kThreads, 0, s>>>(g, r, bc, fac, batch);
+  k_apply_bc_cols<T><<<blocks_for((int64_t)batch * (g.ny - 1)), kThreads, 0, s>>>(g, r, bc, fac, batch);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t coarsify(const Geometry& g, T* gc, const T* gf, int batch, int64_t stride, cudaStream_t s) {
+  k_coarsify<T><<<blocks_for((int64_t)batch * (g.nx / 2 - 1) * (g.ny / 2 - 1)), kThreads, 0, s>>>(g, gc, gf, batch, stride);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t curl(const Geometry& g, const T* psi, const T* bc, T* q, int batch, cudaStream_t s) {
+  k_curl<T><<<blocks_for((int64_t)batch * g.nq), kThreads, 0, s>>>(g, psi, bc, q, batch);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t rot(const Geometry& g, const T* q, T* gam, int batch, cudaStream_t s) {
+  k_rot<T><<<blocks_for((int64_t)batch * g.nG), kThreads, 0, s>>>(g, q, gam, batch);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s) {
+  ProfScope prof(kClassNonlin, s);
+  k_nonlin_rhs<T><<<blocks_for((int64_t)g.nlev * g.nG), kThreads, 0, s>>>(g, a);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac, cudaStream_t s) {
+  const int64_t n = (int64_t)g.nlev * g.nbc + (int64_t)g.nlev * (2 * (g.nx - 1) + 2 * (g.ny - 1));
+  k_trial_rings<T><<<blocks_for(n), kThreads, 0, s>>>(g, gamma, bcn, edges, fac);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t fill(T* p, T v, int64_t n, cudaStream_t s) {
+  k_fill<T><<<blocks_for(n), kThreads, 0, s>>>(p, v, n);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s) {
+  k_axpby<T><<<blocks_for(n), kThreads, 0, s>>>(y, x, a, b, n);
+  return cudaGetLastError();
+}
+
+#define IB_INST(T)                                                                                   \
+  template cudaError_t get_bc<T>(const Geometry&, const T*, T*, int, T, cudaStream_t);               \
+  template cudaError_t apply_bc<T>(const Geometry&, T*, const T*, T, int, cudaStream_t);             \
+  template cudaError_t coarsify<T>(const Geometry&, T*, const T*, int, int64_t, cudaStream_t);       \
+  template cudaError_t curl<T>(const Geometry&, const T*, const T*, T*, int, cudaStream_t);          \
+  template cudaError_t rot<T>(const Geometry&, const T*, T*, int, cudaStream_t);                     \
+  template cudaError_t nonlin_rhs<T>(const Geometry&, const NonlinArgs<T>&, cudaStream_t);           \
+  template cudaError_t trial_rings<T>(const Geometry&, const T*, T*, T*, const double*, cudaStream_t); \
+  template cudaError_t fill<T>(T*, T, int64_t, cudaStream_t);                                        \
+  template cudaError_t axpby<T>(T*, const T*, T, T, int64_t, cudaStream_t);
+IB_INST(double)
+IB_INST(float)
+#undef IB_INST
+
+}  // namespace ib

@@ -1,0 +1,129 @@
+/*
+ * libibgb300 -- C ABI of the GB300-native immersed-boundary projection (IBPM / CNAB) step.
+ *
+ * Drop-in boundary for the stream-function / CNAB path of ImmersedBoundary.jl.  In the
+ * reference the "plugin" is Julia dispatch: statetype(prob) / solvertype(prob) choose
+ * CNAB.State / CNAB.Solver and solve! calls advance!(state, solver, t) once per step.  Each
+ * entry point below names the reference function (file:line, relative to the
+ * ImmersedBoundary.jl project root) that it replaces; INTEGRATION.md shows the Julia ccall
+ * binding.
+ *
+ * Conventions
+ *   - every call returns an int status (IB_OK == 0); ib_last_error() gives the message;
+ *   - host arrays are caller-owned FP64 in the reference's column-major layouts:
+ *       gamma, psi, nonlin : (nx-1)*(ny-1) x nlevels  (Matrix nGamma x nlevel)
+ *       q                  : nq x nlevels, each level [qx (nx+1)*ny ; qy nx*(ny+1)]
+ *       fb                 : 2*nb, [fx_1..fx_nb, fy_1..fy_nb]
+ *       xb                 : nb x 2 column-major, i.e. [x_1..x_nb, y_1..y_nb]
+ *   - the library owns all device memory; nothing crosses the boundary per step except t,
+ *     the freestream (u, v) at t and a status;
+ *   - one handle owns one CUDA stream and its captured step graphs; a handle is not
+ *     thread-safe, separate handles are independent.
+ */
+#ifndef IBGB300_H
+#define IBGB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define IB_OK 0
+#define IB_ERR_INVALID 1            /* bad argument / unsupported grid size */
+#define IB_ERR_CUDA 2               /* CUDA runtime failure (message in ib_last_error) */
+#define IB_ERR_NONFINITE 3          /* error("infinite flux"), src/streamfcn/structure-ops.jl:79-82 */
+#define IB_ERR_BODY_OUT_OF_GRID 4   /* body point within 7 cells of the finest-grid edge */
+#define IB_ERR_SINGULAR 5           /* zero / non-finite pivot while inverting the Schur matrix */
+#define IB_ERR_CG_MAXITER 6         /* Schur CG hit its iteration cap */
+#define IB_ERR_UNSUPPORTED 7        /* feature not available in this build */
+
+/* arithmetic of the fluid solve (the Schur solve and forces are FP64 in every mode) */
+#define IB_PREC_FP64 0
+
+/* body motion */
+#define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */
+
+typedef struct ib_problem {
+  /* MultiLevel(UniformGrid(h, (x0, x1), (y0, y1)), nlevels), src/fluids/fluids.jl:53-95 */
+  int32_t nx, ny, nlevels;
+  double x0, y0, h;
+  /* SchemeCNAB(dt), src/schemes.jl:19-26; beta = (1.5, -0.5) */
+  double dt;
+  double beta0, beta1;
+  /* StreamFcnFluid(domain, freestream, Re), src/streamfcn/fluids.jl:49-58 */
+  double re;
+  /* BodyGroup(RigidBody(frame, xb, ds)...), src/bodies/bodies.jl:11-21, rigid-bodies.jl:4-10 */
+  int32_t nbodies;
+  const int32_t* body_npoints;  /* [nbodies] */
+  const double* xb;             /* [2*nb] stacked points, column-major nb x 2 */
+  const double* ds;             /* [nb] segment lengths */
+  int32_t motion;               /* IB_MOTION_* */
+  int32_t precision;            /* IB_PREC_* */
+  int32_t device;               /* CUDA device ordinal */
+  int32_t history_capacity;     /* steps of C_D / C_L kept on the device (0 -> 4096) */
+} ib_problem;
+
+typedef struct ib_handle ib_handle;
+
+/* initsolver(prob, state) -> CNAB.Solver(prob, state): src/streamfcn/cnab/timestepping.jl:193-249,
+ * plus the zeroed CNAB.State buffers of initstate, src/streamfcn/cnab/states.jl:8-16.
+ * Builds the transform tables, the delta weights (structure-ops.jl:24-61), assembles
+ * Bmat column by column and inverts it (cnab/ops.jl:79-97), all on the device. */
+int ib_create(const ib_problem* prob, ib_handle** out);
+
+/* releases every device resource of the handle */
+int ib_destroy(ib_handle* h);
+
+/* copy!(state, src) of CNAB.State / StreamFcnQuantities (src/streamfcn/states.jl:90-100,
+ * cnab/states.jl:1-16): upload Gamma, q, psi, the two nonlinear-history matrices
+ * (nonlin1 = state.nonlin[1], nonlin2 = state.nonlin[2]), Fb and t.  NULL leaves a field. */
+int ib_set_state(ib_handle* h, const double* gamma, const double* q, const double* psi,
+                 const double* nonlin1, const double* nonlin2, const double* fb, double t);
+
+/* read back state.qty.Γ, q, ψ, state.nonlin[1], state.nonlin[2], Fb and state.t; NULL skips */
+int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* nonlin1,
+                 double* nonlin2, double* fb, double* t);
+
+/* advance!(state, solver, t): src/streamfcn/cnab/timestepping.jl:253-290.  (u_inf, v_inf) is
+ * fluid.freestream(t) (src/streamfcn/fluids.jl:82), evaluated by the caller; base_flux!
+ * (src/streamfcn/fluid-ops.jl:403-417) runs on the device.  Synchronous: returns the step's
+ * status (e.g. IB_ERR_NONFINITE for the reference's "infinite flux" error). */
+int ib_advance(ib_handle* h, double t, double u_inf, double v_inf);
+
+/* solver.vort2flux!(state.qty) (Vort2Flux, src/streamfcn/fluid-ops.jl:438-472) on the handle's
+ * current state: coarsens Γ in place and recomputes ψ and q on every level. */
+int ib_vort2flux(ib_handle* h);
+
+/* The solve! time loop (src/solve.jl:198-212) for n steps without host callbacks:
+ * advance! at t[i] with freestream (uv[2i], uv[2i+1]).  Replays the captured step graph;
+ * synchronises once at the end and returns the first error. */
+int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv);
+
+/* state.qty.stress of the last step (BodyStress, src/streamfcn/states.jl:3-7,53-84):
+ * cd[b], cl[b] per body and, if fb_surface != NULL, the surface stress of every body as
+ * consecutive column-major (n_b x 2) blocks. */
+int ib_get_stress(ib_handle* h, double* cd, double* cl, double* fb_surface);
+
+/* C_D / C_L of the last `count` steps (oldest first), per body: cd[s*nbodies + b].  This is
+ * what a solve(...; save=(each_timestep(s -> s.qty.stress[b].CD),)) callback collects. */
+int ib_get_force_history(ib_handle* h, int32_t count, double* cd, double* cl);
+
+/* number of steps taken by this handle */
+int64_t ib_step_count(const ib_handle* h);
+
+/* block until every queued step of the handle has finished */
+int ib_synchronize(ib_handle* h);
+
+/* message of the last failed call on this handle (or of the last failed ib_create) */
+const char* ib_last_error(const ib_handle* h);
+
+/* static name of a status code */
+const char* ib_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IBGB300_H */

@@ -1,0 +1,148 @@
+"""Step-level parity of the CUDA advance! against the FP64 oracle, through the C ABI.
+
+Tolerances (the spec bar for the FP64 path): per-step vorticity relative L2 <= 1e-10 and
+C_L / C_D <= 1e-8 (relative to max(1, |C|)), over the whole run; bitwise run-to-run.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from _util import rel, start_pair
+
+pytestmark = pytest.mark.gpu
+
+G_TOL = 1e-10
+C_TOL = 1e-8
+
+
+def cerr(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.maximum(1.0, np.abs(b))))
+
+
+def run_parity(ib, O, wl, nsteps, check_every=1):
+    prob, st, solver, op, ost, osol = start_pair(ib, O, wl)
+    g = op.grid
+    worst_g = worst_c = 0.0
+    for i in range(nsteps):
+        t = i * wl.dt
+        ib.advance_(st, solver, t)
+        osol.advance(ost, t)
+        stress = st.qty.stress
+        cd = [s.CD for s in stress]
+        cl = [s.CL for s in stress]
+        worst_c = max(worst_c, cerr(cd, ost.cd), cerr(cl, ost.cl))
+        if (i + 1) % check_every == 0 or i == nsteps - 1:
+            worst_g = max(worst_g, rel(st.qty.gamma, ost.gamma.reshape(g.nlevels, -1)))
+    # full state at the end
+    assert rel(st.qty.psi, ost.psi.reshape(g.nlevels, -1)) < G_TOL
+    assert rel(st.qty.q, ost.q) < G_TOL
+    assert rel(st.qty.Fb, ost.fb) < 1e-8
+    assert rel(st.nonlin[1], ost.nonlin[1].reshape(g.nlevels, -1)) < G_TOL
+    for k, s in enumerate(st.qty.stress):
+        assert rel(s.fb, ost.stress[k]) < 1e-8
+    solver.close()
+    return worst_g, worst_c
+
+
+def test_step_parity_small_cylinder(ib, O):
+    wl = ib.workloads.scaled(ib.workloads.cylinder_small(), 64, 48, nlevels=3)
+    wg, wc = run_parity(ib, O, wl, 30)
+    assert wg < G_TOL and wc < C_TOL, (wg, wc)
+
+
+def test_step_parity_two_bodies(ib, O):
+    wl = ib.workloads.scaled(ib.workloads.two_body_large(), 128, 128, nlevels=2)
+    wg, wc = run_parity(ib, O, wl, 15)
+    assert wg < G_TOL and wc < C_TOL, (wg, wc)
+
+
+def test_step_parity_cylinder_small_full_size(ib, O):
+    """The 200x200, 5-level, 157-point cylinder at Re=100 (first 100 of its 500 steps)."""
+    wl = ib.workloads.cylinder_small(nsteps=100)
+    wg, wc = run_parity(ib, O, wl, 100, check_every=10)
+    assert wg < G_TOL and wc < C_TOL, (wg, wc)
+
+
+def test_no_body_freestream_stays_zero(ib):
+    grid = ib.MultiLevel(ib.UniformGrid(0.05, (-1.0, 2.2), (-1.6, 1.6)), 2)
+    prob = ib.Problem(ib.StreamFcnFluid(grid, (1.0, 0.0), 100.0), ib.BodyGroup(), ib.SchemeCNAB(0.01))
+    st = ib.initstate(prob)
+    solver = ib.initsolver(prob, st)
+    for i in range(3):
+        ib.advance_(st, solver, i * 0.01)
+    assert np.all(st.qty.gamma == 0.0) and np.all(st.qty.q == 0.0)
+    solver.close()
+
+
+def test_bitwise_deterministic_and_graph_equals_eager(ib):
+    wl = ib.workloads.scaled(ib.workloads.two_body_large(), 96, 96, nlevels=3)
+    outs = []
+    for no_graph in ("0", "0", "1"):
+        os.environ["IBGB300_NO_GRAPH"] = no_graph
+        try:
+            prob = wl.problem()
+            st = ib.initstate(prob)
+            st._gamma[:] = wl.initial_gamma()
+            s = ib.initsolver(prob, st)
+            s.vort2flux(st)
+            for i in range(8):
+                ib.advance_(st, s, i * wl.dt)
+            outs.append((st.qty.gamma.copy(), st.qty.Fb.copy()))
+            s.close()
+        finally:
+            os.environ.pop("IBGB300_NO_GRAPH", None)
+    for a, b in outs[1:]:
+        np.testing.assert_array_equal(a, outs[0][0])
+        np.testing.assert_array_equal(b, outs[0][1])
+
+
+def test_advance_n_and_solve_callbacks_match_single_steps(ib):
+    wl = ib.workloads.scaled(ib.workloads.cylinder_small(), 64, 64, nlevels=2)
+    prob = wl.problem()
+    # single steps with a per-step callback
+    cds = ib.solve(prob, (0.0, 9 * wl.dt), save=(ib.each_timestep(lambda s: s.qty.stress[0].CD),))[0]
+    assert len(cds) == 10 and cds.t[0] == 0.0
+    # batched graph replays, then the device force history
+    st = ib.initstate(prob)
+    s = ib.initsolver(prob, st)
+    ib.solve_(st, prob, (0.0, 9 * wl.dt), solver=s)
+    cd_hist, _ = s.force_history(10)
+    np.testing.assert_array_equal(cd_hist[:, 0], np.array(cds))
+    assert st.t == pytest.approx(9 * wl.dt)
+    s.close()
+
+
+def test_stop_iteration_and_at_indices(ib):
+    wl = ib.workloads.scaled(ib.workloads.cylinder_small(), 64, 64, nlevels=2)
+    prob = wl.problem()
+    seen = []
+
+    def stopper(s):
+        seen.append(s.t)
+        return ib.StopIteration() if len(seen) == 4 else None
+    res = ib.solve(prob, (0.0, 20 * wl.dt), save=(ib.at_indices(lambda s: s.t, [2, 3]),),
+                   call=(ib.each_timestep(stopper),))
+    assert len(seen) == 4
+    assert list(res[0]) == pytest.approx([wl.dt, 2 * wl.dt])
+
+
+def test_errors_are_reported_not_faulted(ib):
+    """A body too close to the edge and a non-finite state come back as status codes."""
+    grid = ib.MultiLevel(ib.UniformGrid(0.05, (-1.0, 2.2), (-1.6, 1.6)), 2)
+    fluid = ib.StreamFcnFluid(grid, (1.0, 0.0), 100.0)
+    edge = ib.RigidBody(ib.GridFrame(), np.array([[-0.98, 0.0], [-0.9, 0.0]]), np.array([0.05, 0.05]))
+    prob = ib.Problem(fluid, ib.BodyGroup(edge), ib.SchemeCNAB(0.01))
+    with pytest.raises(ib.IBError) as e:
+        ib.initsolver(prob, ib.initstate(prob))
+    assert e.value.status == 4
+    body = ib.circle((0.5, 0.0), 0.4, 0.05)
+    prob = ib.Problem(fluid, ib.BodyGroup(body), ib.SchemeCNAB(0.01))
+    st = ib.initstate(prob)
+    st._q[0, 10] = np.nan
+    s = ib.initsolver(prob, st)
+    with pytest.raises(ib.IBError) as e:
+        ib.advance_(st, s, 0.0)
+    assert e.value.status == 3
+    s.close()

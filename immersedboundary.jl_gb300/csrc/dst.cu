@@ -271,7 +271,8 @@ k_xpass(Geometry g, DstAxis<T> ax, XPassArgs<T> a) {
 // y pass: one CTA per strip of W columns, one warp per column; forward DST, spectral
 // multiply, second DST.  Multipliers are stored column-major in spectral space
 // (index I*(ny-1) + J) so a warp reads them contiguously.
-// Shared memory per warp: P, [Q,] scratch, each n values padded to keep 16-byte alignment.
+// Shared memory per warp: the column and the FFT scratch, n values each, padded to keep
+// 16-byte alignment.
 // ------------------------------------------------------------------------------------------
 template <typename T, SpecOp OP>
 __global__ void __launch_bounds__(256)
@@ -282,8 +283,7 @@ k_ypass(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
   const int n = ax.n;
   const int ps = n + 16 / (int)sizeof(T);
   T* P = reinterpret_cast<T*>(smem_raw);
-  T* Q = P + W * ps;
-  T* S = (OP == SpecOp::kCn) ? Q + W * ps : Q;
+  T* S = P + W * ps;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int nstrips = (ncol + W - 1) / W;
   for (int blk = blockIdx.x; blk < a.batch * nstrips; blk += gridDim.x) {
@@ -293,7 +293,6 @@ k_ypass(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
       const int J = idx / W, w = idx - J * W, I = I0 + w;
       const int64_t gi = off + (int64_t)J * ncol + I;
       P[w * ps + J + 1] = (I < ncol) ? a.in1[gi] : T(0);
-      if (OP == SpecOp::kCn) Q[w * ps + J + 1] = (I < ncol) ? a.in2[gi] : T(0);
     }
     __syncthreads();
     {
@@ -302,17 +301,10 @@ k_ypass(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
       const int I = I0 + warp;
       dst1_warp<T>(p, sc, ax, lane);
       const int64_t mo = (int64_t)b * a.mstride + (int64_t)min(I, ncol - 1) * nrow;
-      if (OP == SpecOp::kCn) {
-        T* q = Q + warp * ps;
-        dst1_warp<T>(q, sc, ax, lane);
-        for (int J = lane; J < nrow; J += 32) {
-          const T m1 = __ldg(&a.m1[mo + J]), m2 = __ldg(&a.m2[mo + J]);
-          p[J + 1] = m1 * fmaT(m2, p[J + 1], q[J + 1]);
-        }
-      } else if (OP == SpecOp::kFwd) {
-        for (int J = lane; J < nrow; J += 32) p[J + 1] *= a.scal;
-      } else {
+      if (OP == SpecOp::kScale) {
         for (int J = lane; J < nrow; J += 32) p[J + 1] *= __ldg(&a.m1[mo + J]);
+      } else {
+        for (int J = lane; J < nrow; J += 32) p[J + 1] *= a.scal;
       }
       __syncwarp();
       if (OP != SpecOp::kFwd) dst1_warp<T>(p, sc, ax, lane);
@@ -385,7 +377,7 @@ cudaError_t launch_x(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>
 template <typename T>
 cudaError_t launch_y(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s) {
   ProfScope prof(kClassYPass, s);
-  const int nbuf = (a.op == SpecOp::kCn) ? 3 : 2;
+  const int nbuf = 2;
   const int ps = ax.n + 16 / (int)sizeof(T);
   int W = 8;
   while (W > 1 && (size_t)nbuf * W * ps * sizeof(T) > 200 * 1024) W >>= 1;
@@ -393,11 +385,7 @@ cudaError_t launch_y(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>
   const int nstrips = (g.nx - 1 + W - 1) / W;
   const int blocks = a.batch * nstrips;
   cudaError_t e;
-  if (a.op == SpecOp::kCn) {
-    auto k = k_ypass<T, SpecOp::kCn>;
-    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
-  } else if (a.op == SpecOp::kFwd) {
+  if (a.op == SpecOp::kFwd) {
     auto k = k_ypass<T, SpecOp::kFwd>;
     if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
     k<<<blocks, W * 32, smem, s>>>(g, ax, a);

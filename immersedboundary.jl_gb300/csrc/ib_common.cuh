@@ -84,9 +84,8 @@ bool dst_axis_supported(int n);
 // Every pass takes arrays of (nx-1)*(ny-1) values; `batch` arrays live at stride nG.
 // Spectral multipliers are stored per array slot with stride `mstride` (0 = shared).
 enum class SpecOp : int {
-  kScale = 0,      // Z = m1 * P
-  kCn = 1,         // Z = m1 * (m2 * P + Q)   (P from input 1, Q from input 2)
-  kFwd = 2,        // out = scal * P          (one transform only)
+  kScale = 0,      // out = S_y(m1 * S_y(in1))
+  kFwd = 2,        // out = scal * S_y(in1)   (one transform only)
 };
 
 template <typename T>
@@ -104,8 +103,8 @@ cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a
 
 template <typename T>
 struct YPassArgs {
-  const T* in1; const T* in2; T* out; int batch; int64_t stride;
-  const T* m1; const T* m2; int64_t mstride;  // multipliers (per slot stride)
+  const T* in1; T* out; int batch; int64_t stride;
+  const T* m1; int64_t mstride;                // multipliers (per slot stride)
   SpecOp op;
   T scal;                                      // kFwd scale
 };
@@ -134,7 +133,10 @@ cudaError_t rot(const Geometry& g, const T* q, T* gam, int batch, cudaStream_t s
 
 // Trial-state explicit part for all levels at once.  For each level (0-based l):
 //   nl_new[l] = rot(direct_product(avg_flux(q[l] + q0[l]), gamma[l], bcn[l])) / hc_l^2
-//   rhs[l]    = dt*beta0*nl_new[l] + dt*beta1*nl_old[l] + rhsbc edges of level l
+//   rhs[l]    = A_l gamma[l] + dt*beta0*nl_new[l] + dt*beta1*nl_old[l] + rhsbc edges of level l
+// where A_l = I - alpha_l * rot(curl(.)) (the 5-point Laplacian with zero boundary values,
+// alpha_l = dt / (2 Re hc_l^2)) is the explicit Crank-Nicolson operator that the reference
+// applies through its sine transform (its eigenvalues are 1 - alpha_l * lap_eigs).
 // bcn[l] is the nonlinear boundary ring (zero for the coarsest level); rhsbc edges are
 // given as 4 edge vectors per level (bottom/top: nx-1, left/right: ny-1).
 template <typename T>
@@ -143,6 +145,7 @@ struct NonlinArgs {
   T* nl_new; T* rhs;
   const double* q0;        // [nlev][2] (u hc, v hc)
   const double* inv_hc2;   // [nlev]
+  const double* alpha;     // [nlev] dt/(2 Re hc^2); nullptr: rhs without the A_l gamma term
   double dtb0, dtb1;
 };
 template <typename T>

@@ -8,8 +8,9 @@
 //   f  stress        C_D, C_L per body -> device history
 //   g  projection    rot(E^T Fb) -> Ainv_1 -> Gamma_1 = Gamma_s1 - (.)   (buffers swap)
 //   h  Vort2Flux     coarsify + chain of Poisson solves + curl on every level
-// The CN pair A / Ainv of a level shares its transforms: Gamma_s = S[(a S Gamma + S r) m]
-// (3 DSTs instead of the reference's 4, equal up to round-off).
+// The explicit CN operator A_l, which the reference applies with two sine transforms, is the
+// 5-point stencil it diagonalises (I - alpha_l rot curl); it is fused into the nonlinear-term
+// kernel, so each level's trial solve is one Poisson-type solve (equal up to round-off).
 #include "ib_common.cuh"
 #include "ibgb300.h"
 #include "ibgb300_ops.h"
@@ -63,7 +64,7 @@ struct ib_handle {
   // spectral multipliers (column-major in spectral space, x16)
   double *mLap = nullptr, *mCN1 = nullptr, *mCN2 = nullptr;
   // per-level parameters
-  double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr;
+  double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr, *d_alpha = nullptr;
   double* h_q0 = nullptr;  // pinned [kQ0Slots][2L]
   int q0_slot = 0;
   // bodies
@@ -203,32 +204,12 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
   na.rhs = h->rhs;
   na.q0 = h->d_q0;
   na.inv_hc2 = h->d_inv_hc2;
+  na.alpha = h->d_alpha;
   na.dtb0 = h->dt * h->beta0;
   na.dtb1 = h->dt * h->beta1;
   CE(nonlin_rhs<double>(g, na, s));
-  XPassArgs<double> xa{};
-  xa.in = gam;
-  xa.out = h->w1;
-  xa.batch = L;
-  xa.stride = nG;
-  CE(xpass<double>(g, h->axx.d, xa, s));
-  xa.in = h->rhs;
-  xa.out = h->w2;
-  CE(xpass<double>(g, h->axx.d, xa, s));
-  YPassArgs<double> ya{};
-  ya.in1 = h->w1;
-  ya.in2 = h->w2;
-  ya.out = h->w1;
-  ya.batch = L;
-  ya.stride = nG;
-  ya.m1 = h->mCN1;
-  ya.m2 = h->mCN2;
-  ya.mstride = nG;
-  ya.op = SpecOp::kCn;
-  CE(ypass<double>(g, h->axy.d, ya, s));
-  xa.in = h->w1;
-  xa.out = gs;
-  CE(xpass<double>(g, h->axx.d, xa, s));
+  // Gamma_s[l] = Ainv_l rhs[l] for every level in one batched solve
+  CE(poisson(h, h->rhs, gs, L, nullptr, h->mCN1, nG, nullptr, h->w1));
   // trial Vort2Flux: psi on every level, flux on level 1 only (the only one read)
   CE(vort2flux(h, gs, h->psi, nullptr, h->qs1, h->rings));
   if (h->nb > 0) {
@@ -351,17 +332,6 @@ int prime_kernels(ib_handle* h) {
   const Geometry& g = h->g;
   CK(poisson(h, h->w2, h->w2, 1, h->rings, h->mLap, 0, nullptr, h->w1));
   CK(poisson(h, h->w2, h->w2, 1, nullptr, h->mLap, 0, h->w2, h->w1));
-  YPassArgs<double> ya{};
-  ya.in1 = h->w1;
-  ya.in2 = h->w2;
-  ya.out = h->w1;
-  ya.batch = 1;
-  ya.stride = g.nG;
-  ya.m1 = h->mCN1;
-  ya.m2 = h->mCN2;
-  ya.mstride = g.nG;
-  ya.op = SpecOp::kCn;
-  CK(ypass<double>(g, h->axy.d, ya, h->stream));
   CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -530,7 +500,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   AL(h->bcn, (int64_t)L * g.nbc); AL(h->edges, (int64_t)L * (2 * (g.nx - 1) + 2 * (g.ny - 1)));
   AL(h->rings, (int64_t)L * g.nbc);
   AL(h->mLap, nG); AL(h->mCN1, L * nG); AL(h->mCN2, L * nG);
-  AL(h->d_fac, L); AL(h->d_q0, 2 * L); AL(h->d_inv_hc2, L);
+  AL(h->d_fac, L); AL(h->d_q0, 2 * L); AL(h->d_inv_hc2, L); AL(h->d_alpha, L);
   AL(h->status, 4); AL(h->d_counter, 1);
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->hist, (int64_t)h->hist_cap * 2 * (h->nbodies > 0 ? h->nbodies : 1));
@@ -542,17 +512,19 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   {
     std::vector<double> lap, cn1, cn2;
     build_multipliers(h, lap, cn1, cn2);
-    std::vector<double> fac(L), ihc(L);
+    std::vector<double> fac(L), ihc(L), alpha(L);
     for (int l = 0; l < L; ++l) {
       const double hc = g.h * std::ldexp(1.0, l);
-      fac[l] = 0.25 * h->dt / (h->re * (hc * hc));  // timestepping.jl:50
-      ihc[l] = 1.0 / (hc * hc);                     // cnab/ops.jl:162-163
+      fac[l] = 0.25 * h->dt / (h->re * (hc * hc));    // timestepping.jl:50
+      ihc[l] = 1.0 / (hc * hc);                       // cnab/ops.jl:162-163
+      alpha[l] = h->dt / (2.0 * h->re * (hc * hc));   // cnab/ops.jl:26
     }
     if ((e = cudaMemcpy(h->mLap, lap.data(), sizeof(double) * lap.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->mCN1, cn1.data(), sizeof(double) * cn1.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->mCN2, cn2.data(), sizeof(double) * cn2.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->d_fac, fac.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(h->d_inv_hc2, ihc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
+        (e = cudaMemcpy(h->d_inv_hc2, ihc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_alpha, alpha.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
   }
   if (nb > 0) {

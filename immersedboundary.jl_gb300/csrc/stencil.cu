@@ -212,6 +212,16 @@ __global__ void k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
     a.nl_new[t] = nl;
     T r = (T)a.dtb0 * nl;
     r = r + (T)a.dtb1 * a.nl_old[t];
+    if (a.alpha) {
+      // A_l gamma = gamma - alpha_l (4 gamma - neighbours), zero outside the array
+      const T gc = v.Gm(J, I);
+      T lap = T(4) * gc;
+      if (I > 0) lap -= v.Gm(J, I - 1);
+      if (I < ncol - 1) lap -= v.Gm(J, I + 1);
+      if (J > 0) lap -= v.Gm(J - 1, I);
+      if (J < nrow - 1) lap -= v.Gm(J + 1, I);
+      r = (gc - (T)a.alpha[l] * lap) + r;
+    }
     const T* ed = a.edges + (int64_t)l * ne;
     T edge = T(0);
     if (J == 0) edge += ed[I];

@@ -170,24 +170,73 @@ def cpu_reference(ib, wl, nsteps: int, warmup: int):
 # ----------------------------------------------------------------------------------------------
 # algorithmic bytes / flops of the sine-transform passes (per step), see the design doc
 # ----------------------------------------------------------------------------------------------
-def pass_model(wl):
+def pass_model(wl, precision: str):
+    """Algorithmic DRAM bytes, launches and flops of the x and y passes of one step.
+
+    Solves per step: the trial solve (one launch over all L levels), 2L Vort2Flux solves and
+    the projection solve (which also reads the trial Gamma it subtracts from).
+    FP64: x fwd (8+8 B/elem), y (8 in + 8 multiplier + 8 out), x inv (8+8).
+    mixed: x fwd from FP64 (8+4), y (4+4+4), x inv (4+4), x residual fwd (8 b + 4 x0 + 4),
+           y (12), x inv into FP64 (4 + 4 x0 + 8).
+    A length-n sine line costs ~2.5 n log2 n flops (a real FFT of length n).
+    """
     nG = (wl.nx - 1) * (wl.ny - 1)
     L = wl.nlevels
-    w = 8
-    # y passes: one CN pass over L levels (reads Gamma and rhs transforms + 2 multipliers,
-    # writes 1) and 2L+1 Poisson passes (reads 1 + multiplier, writes 1)
-    y_bytes = w * nG * (5 * L + 3 * (2 * L + 1))
-    y_launches = 1 + 2 * L + 1
-    # x passes: 3 launches of L arrays in the trial solve, 2 per level in each of the two
-    # Vort2Flux chains, 2 in the projection (the second also reads the trial Gamma)
-    x_bytes = w * nG * (2 * 3 * L + 2 * 4 * L + 2 * 2 + 1)
-    x_launches = 3 + 4 * L + 2
-    # flops: a length-n sine line costs ~2.5 n log2 n (real FFT of length n)
+    arrays = 3 * L + 1                      # arrays solved per step
     fx = 2.5 * wl.nx * np.log2(wl.nx) * (wl.ny - 1)
     fy = 2.5 * wl.ny * np.log2(wl.ny) * (wl.nx - 1)
-    y_flops = fy * (3 * L + 2 * (2 * L + 1))  # CN: 3 transforms per level; Poisson: 2
-    x_flops = fx * (3 * L + 4 * L + 2)
+    if precision == "fp64":
+        x_bytes = nG * (32 * arrays + 8)
+        x_launches = 2 * (2 + 2 * L)
+        y_bytes = nG * 24 * arrays
+        y_launches = 2 + 2 * L
+        x_flops = fx * 2 * arrays
+        y_flops = fy * 2 * arrays
+    else:
+        x_bytes = nG * (52 * arrays + 8)
+        x_launches = 4 * (2 + 2 * L)
+        y_bytes = nG * 24 * arrays
+        y_launches = 2 * (2 + 2 * L)
+        x_flops = fx * 4 * arrays
+        y_flops = fy * 4 * arrays
     return {"x": (x_bytes, x_launches, x_flops), "y": (y_bytes, y_launches, y_flops)}
+
+
+def run_arm(ib, lib, L, wl, precision, K, W, local, dist, profile_range=False):
+    """Set up one solver and time K steps (after W warm-up steps) with CUDA events."""
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = wl.initial_gamma()
+    solver = ib.initsolver(prob, st, device=local, precision=precision)
+    solver.vort2flux(st)
+    info = L.IbInfo()
+    lib.ib_get_info(solver.handle, C.byref(info))
+    n = W + K + 64
+    ts = np.ascontiguousarray(np.arange(n, dtype=np.float64) * wl.dt)
+    uv = np.ascontiguousarray(np.tile(np.array(wl.freestream, dtype=np.float64), n))
+
+    def tp(a, off):
+        return a[off:].ctypes.data_as(C.POINTER(C.c_double))
+
+    solver._check(lib.ib_advance_n(solver.handle, W, tp(ts, 0), tp(uv, 0)))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    dist.barrier()
+    lib.ib_synchronize(solver.handle)
+    if profile_range:
+        lib.ib_profiler_start()
+    dev_ms = C.c_double()
+    h0 = time.perf_counter()
+    solver._check(lib.ib_advance_n_timed(solver.handle, K, tp(ts, W), tp(uv, 2 * W), C.byref(dev_ms)))
+    host_s = time.perf_counter() - h0
+    if profile_range:
+        lib.ib_profiler_stop()
+    dist.barrier()
+    ck = clocks.stop()
+    cd, cl = solver.force_history(K)
+    return dict(solver=solver, state=st, prob=prob, info=info, ts=ts, uv=uv, tp=tp, dev_s=dev_ms.value / 1e3,
+                host_s=host_s, clocks=ck, cd=cd, cl=cl)
 
 
 def run_ours(args, rank, world, local):
@@ -198,64 +247,41 @@ def run_ours(args, rank, world, local):
     from ibgb300 import _lib as L
     dist = Dist(world, local, "nccl")
     wl = make_workload(ib, args.workload)
-    prob = wl.problem()
-    st = ib.initstate(prob)
-    st._gamma[:] = wl.initial_gamma()
-    solver = ib.initsolver(prob, st, device=local)
-    solver.vort2flux(st)
-    info = L.IbInfo()
-    lib.ib_get_info(solver.handle, C.byref(info))
     K, W = args.steps, args.warmup
-    ts = np.ascontiguousarray(np.arange(W + K + 64, dtype=np.float64) * wl.dt)
-    uv = np.ascontiguousarray(np.tile(np.array(wl.freestream, dtype=np.float64), W + K + 64))
-
-    def tptr(a, off):
-        return a[off:].ctypes.data_as(C.POINTER(C.c_double))
-
-    # warm-up
-    solver._check(lib.ib_advance_n(solver.handle, W, tptr(ts, 0), tptr(uv, 0)))
-    # timed region (device time with CUDA events on the library's stream)
-    clocks = ClockSampler(local)
-    clocks.start()
-    time.sleep(0.3)
-    dist.barrier()
-    lib.ib_synchronize(solver.handle)
-    if args.profile_range:
-        lib.ib_profiler_start()
-    dev_ms = C.c_double()
-    h0 = time.perf_counter()
-    solver._check(lib.ib_advance_n_timed(solver.handle, K, tptr(ts, W), tptr(uv, 2 * W), C.byref(dev_ms)))
-    host_s = time.perf_counter() - h0
-    if args.profile_range:
-        lib.ib_profiler_stop()
-    dist.barrier()
-    ck = clocks.stop()
-    t_max = dist.max(dev_ms.value / 1e3)
+    prec = args.precision
+    arm = run_arm(ib, lib, L, wl, prec, K, W, local, dist, args.profile_range)
+    t_max = dist.max(arm["dev_s"])
+    info = arm["info"]
     value = wl.cells_per_step * K * world / t_max
     ms_per_step = t_max / K * 1e3
     out = {
         "metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
-        "config": {"workload": describe(wl), "cells_per_step": wl.cells_per_step, "parallelism": "replicas",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + f64 residual/state",
+        "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
+        "config": {"workload": describe(wl), "precision": prec, "cells_per_step": wl.cells_per_step,
+                   "parallelism": "replicas",
                    "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),
-                   "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": host_s / K * 1e3},
+                   "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": arm["host_s"] / K * 1e3},
         "gpu_launches": int(info.kernels_per_step) * K,
     }
+    ck = arm["clocks"]
     if ck:
         out["clocks"] = {"sm_mhz": ck["sm_mhz"], "sm_max_mhz": ck["sm_max_mhz"], "reasons": ck["reasons"],
                          "samples": ck["samples"], "power_w_max": ck["power_w_max"]}
     if args.profile_range:
+        arm["solver"].close()
         print(json.dumps(out), flush=True)
         return
-    # dominant kernel class: event-timed launches over a second run of K steps
-    model = pass_model(wl)
+    solver, st, prob, ts, uv, tp = arm["solver"], arm["state"], arm["prob"], arm["ts"], arm["uv"], arm["tp"]
+    # dominant kernel class: event-timed launches over further steps
+    model = pass_model(wl, prec)
     prof = {}
     npf = min(K, 20)
     base = W + K
     for cls, key in ((0, "x"), (1, "y")):
         tot, nl = C.c_double(), C.c_int64()
-        solver._check(lib.ib_profile_steps(solver.handle, npf, tptr(ts, base), tptr(uv, 2 * base), cls,
+        solver._check(lib.ib_profile_steps(solver.handle, npf, tp(ts, base), tp(uv, 2 * base), cls,
                                            C.byref(tot), C.byref(nl)))
         base += npf
         prof[key] = (tot.value, nl.value)
@@ -274,21 +300,34 @@ def run_ours(args, rank, world, local):
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(args.workload, {}).get(dom)
+            traffic = json.loads(tf.read_text()).get(f"{args.workload}/{prec}", {}).get(dom)
         except Exception:
             traffic = None
+    pipe_peak = fp64.value if prec == "fp64" else fp32.value
     out["roofline"] = {
         "kernel": {"x": "k_xpass (x-direction sine pass)", "y": "k_ypass (y-direction sine pass + spectral op)"}[dom],
         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
         "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
         "avg_launch_ms": per_launch_s * 1e3, "launches_profiled": nlaunch,
         "share_of_step": tot_ms / npf / ms_per_step,
-        "fp64": {"achieved_tflops": flops_per_launch / per_launch_s / 1e12, "peak_tflops": fp64.value,
-                 "frac": flops_per_launch / per_launch_s / 1e12 / fp64.value if fp64.value > 0 else None,
-                 "peak_source": "measured FMA-chain probe on this GPU"},
-        "other_pass": {k: {"total_ms": prof[k][0], "launches": prof[k][1]} for k in prof},
+        "fp_pipe": {"pipe": "fp64" if prec == "fp64" else "fp32",
+                    "achieved_tflops": flops_per_launch / per_launch_s / 1e12, "peak_tflops": pipe_peak,
+                    "frac": flops_per_launch / per_launch_s / 1e12 / pipe_peak if pipe_peak > 0 else None,
+                    "peak_source": "measured FMA-chain probe on this GPU"},
+        "passes": {k: {"total_ms": prof[k][0], "launches": prof[k][1]} for k in prof},
     }
+    # the plain FP64 GPU path on the same workload, and the mixed path's C_L/C_D error against it
+    if prec != "fp64" and not args.no_fp64_arm:
+        ref = run_arm(ib, lib, L, wl, "fp64", K, W, local, dist)
+        t64 = dist.max(ref["dev_s"])
+        err = max(float(np.max(np.abs(arm["cd"] - ref["cd"]) / np.maximum(1.0, np.abs(ref["cd"])))),
+                  float(np.max(np.abs(arm["cl"] - ref["cl"]) / np.maximum(1.0, np.abs(ref["cl"])))))
+        out["fp64_gpu"] = {"value": wl.cells_per_step * K * world / t64, "ms_per_step": t64 / K * 1e3,
+                           "speedup_of_headline": t64 / t_max,
+                           "max_cl_cd_err_vs_fp64": err,
+                           "err_note": f"max over the {K} timed steps and all bodies of |C - C_fp64| / max(1, |C_fp64|)"}
+        ref["solver"].close()
     # end to end through the public API: solve_ with a per-step callback reading C_D / C_L
     nb = solver.nb
     t0 = float(ts[base])
@@ -345,6 +384,9 @@ def main():
     ap.add_argument("--workload", default="two_body_large")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+                    help="arithmetic of the timed arm (mixed: FP32 transforms + FP64 residual refinement)")
+    ap.add_argument("--no-fp64-arm", action="store_true", help="skip timing the FP64 GPU path beside it")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()

@@ -24,6 +24,8 @@ IB_ERR_CG_MAXITER = 6
 IB_ERR_UNSUPPORTED = 7
 
 IB_PREC_FP64 = 0
+IB_PREC_MIXED = 1
+PRECISIONS = {"fp64": IB_PREC_FP64, "mixed": IB_PREC_MIXED}
 IB_MOTION_STATIC = 0
 
 _dp = C.POINTER(C.c_double)

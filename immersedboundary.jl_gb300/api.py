@@ -378,9 +378,15 @@ def initstate(prob: Problem, t: float = 0.0) -> State:
 # solver (the GPU handle)
 # ---------------------------------------------------------------------------------------------
 class Solver:
-    """``CNAB.Solver`` (cnab/timestepping.jl:173-249) backed by a libibgb300 handle."""
+    """``CNAB.Solver`` (cnab/timestepping.jl:173-249) backed by a libibgb300 handle.
 
-    def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096):
+    ``precision``: ``"fp64"`` (every sine transform in FP64, the reference's arithmetic) or
+    ``"mixed"`` (FP32 sine transforms with one FP64-residual refinement per Poisson solve;
+    state, nonlinear term, Schur solve and forces stay FP64).
+    """
+
+    def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096,
+                 precision: str = "fp64"):
         if not isinstance(prob.scheme, SchemeCNAB):
             raise NotImplementedError(f"no solver for scheme {type(prob.scheme).__name__}")
         for b in prob.bodies:
@@ -414,7 +420,10 @@ class Solver:
         p.xb = _lib.dptr(self._xb) if self.nb else None
         p.ds = _lib.dptr(self._ds) if self.nb else None
         p.motion = _lib.IB_MOTION_STATIC
-        p.precision = _lib.IB_PREC_FP64
+        if precision not in _lib.PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(_lib.PRECISIONS)}")
+        self.precision = precision
+        p.precision = _lib.PRECISIONS[precision]
         p.device = device
         p.history_capacity = history_capacity
         h = C.c_void_p()

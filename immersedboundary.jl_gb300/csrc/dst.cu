@@ -220,14 +220,14 @@ __device__ __noinline__ void dst1_warp(T* s, T* scratch, const DstAxis<T>& ax, i
 }
 
 // ------------------------------------------------------------------------------------------
-// x pass: one warp per row (contiguous), optional apply_bc prologue and subtract epilogue.
+// x pass: one warp per row (contiguous); see XArgs for the prologue / epilogue variants.
 // Shared memory per warp: the row (n values) and the FFT scratch (n values).
 // ------------------------------------------------------------------------------------------
 constexpr int kXWarps = 4;
 
-template <typename T, bool kBC, bool kSub>
+template <typename T, typename Tin, typename Tout, int PRO, int EPI, bool kBC>
 __global__ void __launch_bounds__(kXWarps * 32)
-k_xpass(Geometry g, DstAxis<T> ax, XPassArgs<T> a) {
+k_xpass(Geometry g, DstAxis<T> ax, XArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = ax.n;
@@ -235,33 +235,57 @@ k_xpass(Geometry g, DstAxis<T> ax, XPassArgs<T> a) {
   T* scratch = s + n;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int total = a.batch * nrow;
+  const Tin* in = static_cast<const Tin*>(a.in);
+  Tout* out = static_cast<Tout*>(a.out);
   for (int row = blockIdx.x * kXWarps + warp; row < total; row += gridDim.x * kXWarps) {
     const int b = row / nrow, J = row - b * nrow;
     const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
-    const T* src = a.in + off;
-    for (int I = lane; I < ncol; I += 32) s[I + 1] = src[I];
-    if (kBC) {
-      const T* bc = a.bc + (int64_t)b * g.nbc;
-      const T fac = a.bcfac;
-      __syncwarp();
-      if (J == 0)
-        for (int I = lane; I < ncol; I += 32) s[I + 1] += fac * bc[g.B + 1 + I];
-      if (J == nrow - 1)
-        for (int I = lane; I < ncol; I += 32) s[I + 1] += fac * bc[g.T + 1 + I];
-      __syncwarp();
-      if (lane == 0) {
-        s[1] += fac * bc[g.L + 1 + J];
-        s[ncol] += fac * bc[g.R + 1 + J];
+    const Tin* src = in + off;
+    const double* bc = kBC ? a.bc + (int64_t)b * g.nbc : nullptr;
+    const double fac = a.bcfac;
+    if (PRO == kProLoad && !kBC && sizeof(Tin) == sizeof(T)) {
+      for (int I = lane; I < ncol; I += 32) s[I + 1] = (T)src[I];
+    } else {
+      // formed in FP64: input, apply_bc edges (rows first, then columns, as the reference),
+      // and for the refinement the residual of the first solution
+      const float* x0 = (PRO == kProResid) ? a.base + off : nullptr;
+      const double mc = (PRO == kProResid) ? a.mc[b * a.mstep] : 0.0;
+      const double ma = (PRO == kProResid) ? a.ma[b * a.mstep] : 0.0;
+      for (int I = lane; I < ncol; I += 32) {
+        double v = (double)src[I];
+        if (kBC) {
+          if (J == 0) v += fac * bc[g.B + 1 + I];
+          if (J == nrow - 1) v += fac * bc[g.T + 1 + I];
+          if (I == 0) v += fac * bc[g.L + 1 + J];
+          if (I == ncol - 1) v += fac * bc[g.R + 1 + J];
+        }
+        if (PRO == kProResid) {
+          const double xc = (double)x0[I];
+          double lap = 4.0 * xc;
+          if (I > 0) lap -= (double)x0[I - 1];
+          if (I < ncol - 1) lap -= (double)x0[I + 1];
+          if (J > 0) lap -= (double)x0[I - ncol];
+          if (J < nrow - 1) lap -= (double)x0[I + ncol];
+          v = v - (mc * xc + ma * lap);
+        }
+        s[I + 1] = (T)v;
       }
     }
     __syncwarp();
     dst1_warp<T>(s, scratch, ax, lane);
-    T* dst = a.out + off;
-    if (kSub) {
-      const T* sf = a.sub_from + off;
-      for (int I = lane; I < ncol; I += 32) dst[I] = sf[I] - s[I + 1];
+    Tout* dst = out + off;
+    if (EPI == kEpiStore) {
+      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)s[I + 1];
+    } else if (EPI == kEpiSub) {
+      const double* sf = a.sub_from + off;
+      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - (double)s[I + 1]);
+    } else if (EPI == kEpiAddBase) {
+      const float* bs = a.base + off;
+      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)((double)bs[I] + (double)s[I + 1]);
     } else {
-      for (int I = lane; I < ncol; I += 32) dst[I] = s[I + 1];
+      const double* sf = a.sub_from + off;
+      const float* bs = a.base + off;
+      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - ((double)bs[I] + (double)s[I + 1]));
     }
     __syncwarp();
   }
@@ -350,28 +374,37 @@ int plan_radices(int M, int* radix) {
   return ns;
 }
 
-template <typename T>
-cudaError_t launch_x(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s) {
-  ProfScope prof(kClassXPass, s);
+template <typename T, typename Tin, typename Tout, int PRO, int EPI, bool kBC>
+cudaError_t launch_x1(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
   const int total = a.batch * (g.ny - 1);
   const int blocks = (total + kXWarps - 1) / kXWarps;
   const size_t smem = (size_t)kXWarps * 2 * ax.n * sizeof(T);
-  if (a.bc && a.sub_from) return cudaErrorInvalidValue;
-  cudaError_t e;
-  if (a.bc) {
-    auto k = k_xpass<T, true, false>;
-    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
-  } else if (a.sub_from) {
-    auto k = k_xpass<T, false, true>;
-    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
-  } else {
-    auto k = k_xpass<T, false, false>;
-    if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
-  }
+  auto k = k_xpass<T, Tin, Tout, PRO, EPI, kBC>;
+  cudaError_t e = ensure_smem((const void*)k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
   return cudaGetLastError();
+}
+
+template <typename T, typename Tin, typename Tout, int PRO>
+cudaError_t launch_x_epi(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  const bool bc = a.bc != nullptr;
+  switch (a.epi) {
+    case kEpiStore:
+      return bc ? launch_x1<T, Tin, Tout, PRO, kEpiStore, true>(g, ax, a, s)
+                : launch_x1<T, Tin, Tout, PRO, kEpiStore, false>(g, ax, a, s);
+    case kEpiSub:
+      if (bc) return cudaErrorInvalidValue;
+      return launch_x1<T, Tin, Tout, PRO, kEpiSub, false>(g, ax, a, s);
+    case kEpiAddBase:
+      if (bc) return cudaErrorInvalidValue;
+      return launch_x1<T, Tin, Tout, PRO, kEpiAddBase, false>(g, ax, a, s);
+    case kEpiSubAddBase:
+      if (bc) return cudaErrorInvalidValue;
+      return launch_x1<T, Tin, Tout, PRO, kEpiSubAddBase, false>(g, ax, a, s);
+    default:
+      return cudaErrorInvalidValue;
+  }
 }
 
 template <typename T>
@@ -447,11 +480,16 @@ void AxisTables<T>::release() {
   mem = nullptr;
 }
 
-template <typename T>
-cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s) {
+template <typename T, typename Tin, typename Tout>
+cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
   if (ax.n != g.nx) return cudaErrorInvalidValue;
   if (a.batch <= 0) return cudaSuccess;
-  return launch_x<T>(g, ax, a, s);
+  ProfScope prof(kClassXPass, s);
+  if (a.pro == kProResid) {
+    if (!a.base || !a.mc || !a.ma || a.epi != kEpiStore) return cudaErrorInvalidValue;
+    return launch_x_epi<T, Tin, Tout, kProResid>(g, ax, a, s);
+  }
+  return launch_x_epi<T, Tin, Tout, kProLoad>(g, ax, a, s);
 }
 
 template <typename T>
@@ -461,24 +499,16 @@ cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a
   return launch_y<T>(g, ax, a, s);
 }
 
-template <typename T>
-cudaError_t dst_rows(const Geometry& g, const DstAxis<T>& ax, const T* in, T* out, int batch,
-                     cudaStream_t s) {
-  XPassArgs<T> a{};
-  a.in = in;
-  a.out = out;
-  a.batch = batch;
-  a.stride = g.nG;
-  return xpass<T>(g, ax, a, s);
-}
-
 template struct AxisTables<double>;
 template struct AxisTables<float>;
-template cudaError_t xpass<double>(const Geometry&, const DstAxis<double>&, const XPassArgs<double>&, cudaStream_t);
-template cudaError_t xpass<float>(const Geometry&, const DstAxis<float>&, const XPassArgs<float>&, cudaStream_t);
+// FP64 path: double in, double out.  Mixed path: FP32 transforms fed from FP64 inputs,
+// FP32 intermediates, FP64 results.
+template cudaError_t xpass<double, double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
+template cudaError_t xpass<float, double, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t xpass<float, float, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t xpass<float, float, double>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
 template cudaError_t ypass<double>(const Geometry&, const DstAxis<double>&, const YPassArgs<double>&, cudaStream_t);
 template cudaError_t ypass<float>(const Geometry&, const DstAxis<float>&, const YPassArgs<float>&, cudaStream_t);
-template cudaError_t dst_rows<double>(const Geometry&, const DstAxis<double>&, const double*, double*, int, cudaStream_t);
-template cudaError_t dst_rows<float>(const Geometry&, const DstAxis<float>&, const float*, float*, int, cudaStream_t);
+
 
 }  // namespace ib

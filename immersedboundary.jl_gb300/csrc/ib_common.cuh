@@ -88,18 +88,36 @@ enum class SpecOp : int {
   kFwd = 2,        // out = scal * S_y(in1)   (one transform only)
 };
 
-template <typename T>
-struct XPassArgs {
-  const T* in; T* out; int batch; int64_t stride;     // plain in -> out
-  // optional fused prologue: edge terms of apply_bc (added to rows J=0, ny-2 and columns 0, nx-2)
-  const T* bc;             // ring (nbc), one per batch slot at stride nbc; nullptr = none
-  T bcfac;
-  // optional fused epilogue: out = sub_from - value  (projection)  or plain store
-  const T* sub_from;
+// x pass: a 1-D sine transform along x of every row of `batch` arrays (compute type T).
+// prologue (how a row is formed before the transform):
+//   kProLoad   row = in                                  (in: Tin)
+//   kProResid  row = in - M x0, M x = mc*x + ma*rot(curl(x)), formed in FP64   (x0 = base)
+// either optionally plus fac * apply_bc(bc) on the edges (bc != nullptr)
+// epilogue (what is stored):
+//   kEpiStore       out = row                              (out: Tout)
+//   kEpiSub         out = sub_from - row
+//   kEpiAddBase     out = base + row                       (FP64 sum)
+//   kEpiSubAddBase  out = sub_from - (base + row)
+enum XPro : int { kProLoad = 0, kProResid = 1 };
+enum XEpi : int { kEpiStore = 0, kEpiSub = 1, kEpiAddBase = 2, kEpiSubAddBase = 3 };
+
+struct XArgs {
+  const void* in;           // Tin
+  void* out;                // Tout
+  int batch;
+  int64_t stride;           // elements between batch slots (in, out, base, sub_from)
+  const double* bc;         // apply_bc ring per slot (stride nbc) or nullptr
+  double bcfac;
+  const double* sub_from;   // kEpiSub / kEpiSubAddBase
+  const float* base;        // x0 of the refinement (kProResid, kEpiAddBase)
+  const double* mc;         // residual operator per slot (stride mstep)
+  const double* ma;
+  int mstep;
+  int pro, epi;
 };
 
-template <typename T>
-cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XPassArgs<T>& a, cudaStream_t s);
+template <typename T, typename Tin, typename Tout>
+cudaError_t xpass(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s);
 
 template <typename T>
 struct YPassArgs {
@@ -112,10 +130,6 @@ struct YPassArgs {
 template <typename T>
 cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s);
 
-// plain 1-D DST along x only (for tests of the transform itself)
-template <typename T>
-cudaError_t dst_rows(const Geometry& g, const DstAxis<T>& ax, const T* in, T* out, int batch,
-                     cudaStream_t s);
 
 // ----------------------------------------------------------------------------------------------
 // stencils (stencil.cu)

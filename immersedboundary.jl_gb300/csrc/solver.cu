@@ -49,6 +49,7 @@ struct ib_handle {
   int nbodies = 0, nb = 0, nf = 0;
   int precision = IB_PREC_FP64;
   AxisTables<double> axx, axy;
+  AxisTables<float> axx32, axy32;  // mixed precision: FP32 transform tables
   // state
   double* G[2] = {nullptr, nullptr};
   double* N[2] = {nullptr, nullptr};
@@ -63,6 +64,9 @@ struct ib_handle {
   double *bcn = nullptr, *edges = nullptr, *rings = nullptr;
   // spectral multipliers (column-major in spectral space, x16)
   double *mLap = nullptr, *mCN1 = nullptr, *mCN2 = nullptr;
+  float *mLap32 = nullptr, *mCN1_32 = nullptr;  // FP32 copies (mixed precision)
+  float *w32 = nullptr, *x032 = nullptr;        // mixed-precision work: transforms and x0
+  double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
   double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr, *d_alpha = nullptr;
   double* h_q0 = nullptr;  // pinned [kQ0Slots][2L]
@@ -124,34 +128,97 @@ int fail(ib_handle* h, int code, const char* what, cudaError_t e = cudaSuccess) 
     if (e_ != cudaSuccess) return e_;      \
   } while (0)
 
-// Poisson-type solve of `batch` arrays: out = S2D( m1 .* S2D(in [+ apply_bc(bc, 1)]) ), with an
-// optional subtract epilogue out = sub_from - (...).
-cudaError_t poisson(ib_handle* h, const double* in, double* out, int batch, const double* bc, const double* m1,
-                    int64_t mstride, const double* sub_from, double* w) {
-  XPassArgs<double> xa{};
+// A Poisson-type operator M: the Laplacian (vort2flux) or I + alpha_l L (CN implicit part).
+// m64/m32: spectral multipliers (x16, FP64 / FP32) with their per-slot stride; mc, ma: the
+// same operator as a stencil, M x = mc x + ma rot(curl(x)), per slot (stride mstep), used by
+// the refinement residual of the mixed-precision solve.
+struct SolveOp {
+  const double* m64;
+  const float* m32;
+  int64_t mstride;
+  const double* mc;
+  const double* ma;
+  int mstep;
+};
+
+SolveOp op_lap(const ib_handle* h) { return {h->mLap, h->mLap32, 0, h->d_zero, h->d_one, 0}; }
+SolveOp op_cn_all(const ib_handle* h) { return {h->mCN1, h->mCN1_32, h->g.nG, h->d_one, h->d_alpha, 1}; }
+SolveOp op_cn1(const ib_handle* h) { return {h->mCN1, h->mCN1_32, 0, h->d_one, h->d_alpha, 0}; }
+
+// FP64 solve of `batch` arrays: out = F2D(m .* F2D(in [+ apply_bc(bc, 1)])), optional
+// subtract epilogue out = sub_from - (...).  w: FP64 work of batch arrays.
+cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
+                      const double* sub_from, double* w) {
+  XArgs xa{};
   xa.in = in;
   xa.out = w;
   xa.batch = batch;
   xa.stride = h->g.nG;
   xa.bc = bc;
   xa.bcfac = 1.0;
-  CE(xpass<double>(h->g, h->axx.d, xa, h->stream));
+  xa.pro = kProLoad;
+  xa.epi = kEpiStore;
+  CE((xpass<double, double, double>(h->g, h->axx.d, xa, h->stream)));
   YPassArgs<double> ya{};
   ya.in1 = w;
   ya.out = w;
   ya.batch = batch;
   ya.stride = h->g.nG;
-  ya.m1 = m1;
-  ya.mstride = mstride;
+  ya.m1 = op.m64;
+  ya.mstride = op.mstride;
   ya.op = SpecOp::kScale;
   CE(ypass<double>(h->g, h->axy.d, ya, h->stream));
-  XPassArgs<double> xb{};
+  XArgs xb{};
   xb.in = w;
   xb.out = out;
   xb.batch = batch;
   xb.stride = h->g.nG;
   xb.sub_from = sub_from;
-  return xpass<double>(h->g, h->axx.d, xb, h->stream);
+  xb.pro = kProLoad;
+  xb.epi = sub_from ? kEpiSub : kEpiStore;
+  return xpass<double, double, double>(h->g, h->axx.d, xb, h->stream);
+}
+
+// Mixed-precision solve: FP32 sine transforms, one refinement with an FP64 residual.
+//   x0 = F32 solve(b);  r = b - M x0 (FP64, fused into the next x pass);  x = x0 + F32 solve(r)
+// b, the result and the residual arithmetic are FP64; w32 / x032: FP32 work of batch arrays.
+cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
+                          const double* sub_from, float* w32, float* x032) {
+  const Geometry& g = h->g;
+  cudaStream_t s = h->stream;
+  YPassArgs<float> ya{};
+  ya.in1 = w32;
+  ya.out = w32;
+  ya.batch = batch;
+  ya.stride = g.nG;
+  ya.m1 = op.m32;
+  ya.mstride = op.mstride;
+  ya.op = SpecOp::kScale;
+  XArgs a{};
+  a.batch = batch;
+  a.stride = g.nG;
+  a.bcfac = 1.0;
+  // first solve
+  a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
+  CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+  CE(ypass<float>(g, h->axy32.d, ya, s));
+  a.in = w32; a.out = x032; a.bc = nullptr;
+  CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
+  // residual (FP64) fused with the forward transform of the correction
+  a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+  CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+  CE(ypass<float>(g, h->axy32.d, ya, s));
+  // x = x0 + correction, in FP64 (optionally subtracted from sub_from)
+  a.in = w32; a.out = out; a.bc = nullptr; a.pro = kProLoad; a.sub_from = sub_from;
+  a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
+  return xpass<float, float, double>(g, h->axx32.d, a, s);
+}
+
+// Solve with the handle's precision mode (batch <= nlevels: uses the step's work buffers).
+cudaError_t solve(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
+                  const double* sub_from) {
+  if (h->precision == IB_PREC_MIXED) return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032);
+  return poisson64(h, in, out, batch, bc, op, sub_from, h->w1);
 }
 
 // Vort2Flux (src/streamfcn/fluid-ops.jl:438-472) on one L-level set.  If q is null only the
@@ -161,13 +228,13 @@ cudaError_t vort2flux(ib_handle* h, double* gam, double* psi, double* q, double*
   const int L = g.nlev;
   const int64_t nG = g.nG;
   for (int l = 1; l < L; ++l) CE(coarsify<double>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
-  CE(poisson(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, h->mLap, 0, nullptr, h->w1));
+  CE(solve(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, op_lap(h), nullptr));
   if (q) CE(curl<double>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
   else if (L == 1) CE(curl<double>(g, psi, nullptr, q1, 1, h->stream));
   for (int l = L - 2; l >= 0; --l) {
     double* ring = rings + (int64_t)l * g.nbc;
     CE(get_bc<double>(g, psi + (l + 1) * nG, ring, 1, 1.0, h->stream));
-    CE(poisson(h, gam + l * nG, psi + l * nG, 1, ring, h->mLap, 0, nullptr, h->w1));
+    CE(solve(h, gam + l * nG, psi + l * nG, 1, ring, op_lap(h), nullptr));
     if (q) CE(curl<double>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
     else if (l == 0) CE(curl<double>(g, psi, ring, q1, 1, h->stream));
   }
@@ -209,7 +276,7 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
   na.dtb1 = h->dt * h->beta1;
   CE(nonlin_rhs<double>(g, na, s));
   // Gamma_s[l] = Ainv_l rhs[l] for every level in one batched solve
-  CE(poisson(h, h->rhs, gs, L, nullptr, h->mCN1, nG, nullptr, h->w1));
+  CE(solve(h, h->rhs, gs, L, nullptr, op_cn_all(h), nullptr));
   // trial Vort2Flux: psi on every level, flux on level 1 only (the only one read)
   CE(vort2flux(h, gs, h->psi, nullptr, h->qs1, h->rings));
   if (h->nb > 0) {
@@ -222,7 +289,7 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
     CE(cudaGetLastError());
     // g. CircProjecter (timestepping.jl:156-171): Gamma_1 = Gamma_s1 - Ainv_1 C^T E^T Fb
     CE(reg_scatter_rot<double>(g, h->fb, h->body_idx, h->weight, h->nb, h->qtmp, h->gtmp, 1, h->nf, h->status + 1, s));
-    CE(poisson(h, h->gtmp, gs, 1, nullptr, h->mCN1, 0, gs, h->w1));
+    CE(solve(h, h->gtmp, gs, 1, nullptr, op_cn1(h), gs));
   }
   // h. Vort2Flux on the new state (timestepping.jl:285): gs is the new Gamma
   CE(vort2flux(h, gs, h->psi, h->q, nullptr, h->rings));
@@ -295,14 +362,14 @@ int assemble_schur(ib_handle* h) {
     const int n = (nf - c0 < nc) ? nf - c0 : nc;
     auto run = [&]() -> cudaError_t {
       CE(unit_scatter_rot<double>(g, h->body_idx, h->weight, h->nb, c0, n, Wa, s));
-      CE(poisson(h, Wa, Gb, n, nullptr, h->mCN1, 0, nullptr, Wb));
+      CE(poisson64(h, Wa, Gb, n, nullptr, op_cn1(h), nullptr, Wb));
       if (L > 1) CE(cudaMemsetAsync(Gb + (int64_t)n * nG, 0, sizeof(double) * (L - 1) * n * nG, s));
       for (int l = 1; l < L; ++l)
         CE(coarsify<double>(g, Gb + (int64_t)l * n * nG, Gb + (int64_t)(l - 1) * n * nG, n, nG, s));
-      CE(poisson(h, Gb + (int64_t)(L - 1) * n * nG, Pb + (int64_t)(L - 1) * n * nG, n, nullptr, h->mLap, 0, nullptr, Wb));
+      CE(poisson64(h, Gb + (int64_t)(L - 1) * n * nG, Pb + (int64_t)(L - 1) * n * nG, n, nullptr, op_lap(h), nullptr, Wb));
       for (int l = L - 2; l >= 0; --l) {
         CE(get_bc<double>(g, Pb + (int64_t)(l + 1) * n * nG, Rb, n, 1.0, s));
-        CE(poisson(h, Gb + (int64_t)l * n * nG, Pb + (int64_t)l * n * nG, n, Rb, h->mLap, 0, nullptr, Wb));
+        CE(poisson64(h, Gb + (int64_t)l * n * nG, Pb + (int64_t)l * n * nG, n, Rb, op_lap(h), nullptr, Wb));
       }
       CE(curl<double>(g, Pb, L > 1 ? Rb : nullptr, Qb, n, s));
       CE(reg_gather<double>(g, Qb, nullptr, h->body_idx, h->weight, h->nb, h->bmat + (int64_t)c0 * nf, n, g.nq, nf, s));
@@ -330,8 +397,12 @@ int assemble_schur(ib_handle* h) {
 // Launch every kernel variant once outside of any capture (sets shared-memory attributes).
 int prime_kernels(ib_handle* h) {
   const Geometry& g = h->g;
-  CK(poisson(h, h->w2, h->w2, 1, h->rings, h->mLap, 0, nullptr, h->w1));
-  CK(poisson(h, h->w2, h->w2, 1, nullptr, h->mLap, 0, h->w2, h->w1));
+  CK(poisson64(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w1));
+  CK(poisson64(h, h->w2, h->w2, 1, nullptr, op_lap(h), h->w2, h->w1));
+  if (h->precision == IB_PREC_MIXED) {
+    CK(poisson_mixed(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w32, h->x032));
+    CK(poisson_mixed(h, h->w2, h->w2, 1, nullptr, op_cn1(h), h->w2, h->w32, h->x032));
+  }
   CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -375,6 +446,8 @@ void destroy_handle(ib_handle* h) {
   if (h->h_q0) cudaFreeHost(h->h_q0);
   h->axx.release();
   h->axy.release();
+  h->axx32.release();
+  h->axy32.release();
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -447,7 +520,8 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (!dst_axis_supported(p->nx) || !dst_axis_supported(p->ny))
     return fail(nullptr, IB_ERR_INVALID,
                 "nx and ny must be multiples of 4, at most 2048, with n/2 a product of 2, 3 and 5");
-  if (p->precision != IB_PREC_FP64) return fail(nullptr, IB_ERR_UNSUPPORTED, "precision mode not available");
+  if (p->precision != IB_PREC_FP64 && p->precision != IB_PREC_MIXED)
+    return fail(nullptr, IB_ERR_UNSUPPORTED, "precision mode not available");
   if (p->motion != IB_MOTION_STATIC) return fail(nullptr, IB_ERR_UNSUPPORTED, "moving bodies not available");
   int nb = 0;
   if (p->nbodies < 0) return fail(nullptr, IB_ERR_INVALID, "negative body count");
@@ -486,6 +560,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   const int64_t nG = g.nG;
   if ((e = h->axx.build(g.nx)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "x transform tables", e));
   if ((e = h->axy.build(g.ny)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "y transform tables", e));
+  if (h->precision == IB_PREC_MIXED) {
+    if ((e = h->axx32.build(g.nx)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "x transform tables", e));
+    if ((e = h->axy32.build(g.ny)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "y transform tables", e));
+  }
 #define AL(ptr, n)                                                                       \
   do {                                                                                   \
     cudaError_t ea = h->alloc(&(ptr), (size_t)(n));                                      \
@@ -501,6 +579,11 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   AL(h->rings, (int64_t)L * g.nbc);
   AL(h->mLap, nG); AL(h->mCN1, L * nG); AL(h->mCN2, L * nG);
   AL(h->d_fac, L); AL(h->d_q0, 2 * L); AL(h->d_inv_hc2, L); AL(h->d_alpha, L);
+  AL(h->d_one, L); AL(h->d_zero, 1);
+  if (h->precision == IB_PREC_MIXED) {
+    AL(h->mLap32, nG); AL(h->mCN1_32, L * nG);
+    AL(h->w32, L * nG); AL(h->x032, L * nG);
+  }
   AL(h->status, 4); AL(h->d_counter, 1);
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->hist, (int64_t)h->hist_cap * 2 * (h->nbodies > 0 ? h->nbodies : 1));
@@ -526,6 +609,15 @@ int ib_create(const ib_problem* p, ib_handle** out) {
         (e = cudaMemcpy(h->d_inv_hc2, ihc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->d_alpha, alpha.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    std::vector<double> ones(L, 1.0);
+    if ((e = cudaMemcpy(h->d_one, ones.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    if (h->precision == IB_PREC_MIXED) {
+      std::vector<float> l32(lap.begin(), lap.end()), c32(cn1.begin(), cn1.end());
+      if ((e = cudaMemcpy(h->mLap32, l32.data(), sizeof(float) * l32.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaMemcpy(h->mCN1_32, c32.data(), sizeof(float) * c32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    }
   }
   if (nb > 0) {
     AL(h->xb, 2 * nb); AL(h->ds, nb); AL(h->weight, (int64_t)nb * 2 * kWin2);
@@ -765,9 +857,9 @@ int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out) {
   double* w;
   CK(cudaMalloc(&w, sizeof(double) * batch * g.nG));
   // RODFT00 in both dimensions = 4 F_y F_x (F: the half-scaled transform of dst.cu)
-  XPassArgs<double> xa{};
-  xa.in = in; xa.out = w; xa.batch = batch; xa.stride = g.nG;
-  cudaError_t e = xpass<double>(g, h->axx.d, xa, s);
+  XArgs xa{};
+  xa.in = in; xa.out = w; xa.batch = batch; xa.stride = g.nG; xa.pro = kProLoad; xa.epi = kEpiStore;
+  cudaError_t e = xpass<double, double, double>(g, h->axx.d, xa, s);
   YPassArgs<double> ya{};
   ya.in1 = w; ya.out = out; ya.batch = batch; ya.stride = g.nG; ya.op = SpecOp::kFwd; ya.scal = 4.0;
   if (e == cudaSuccess) e = ypass<double>(g, h->axy.d, ya, s);
@@ -782,7 +874,7 @@ int ib_op_laplacian_inv(ib_handle* h, int32_t batch, const double* b, double* x)
   if (batch < 1) return IB_ERR_INVALID;
   double* w;
   CK(cudaMalloc(&w, sizeof(double) * batch * g.nG));
-  cudaError_t e = poisson(h, b, x, batch, nullptr, h->mLap, 0, nullptr, w);
+  cudaError_t e = poisson64(h, b, x, batch, nullptr, op_lap(h), nullptr, w);
   cudaStreamSynchronize(s);
   cudaFree(w);
   CK(e);
@@ -798,12 +890,16 @@ static int cn_op(ib_handle* h, int32_t lev, const double* b, double* x, bool inv
   cudaError_t e;
   const int64_t off = (int64_t)(lev - 1) * g.nG;
   if (inverse) {
-    e = poisson(h, b, x, 1, nullptr, h->mCN1 + off, 0, nullptr, w);
+    SolveOp op = op_cn1(h);
+    op.m64 = h->mCN1 + off;
+    e = poisson64(h, b, x, 1, nullptr, op, nullptr, w);
   } else {
     // A multiplier = 16 * scale / Lambda_expl = 16 * scale * cn2 ; build it on the device
     e = cudaMemcpyAsync(m, h->mCN2 + off, sizeof(double) * g.nG, cudaMemcpyDeviceToDevice, s);
     if (e == cudaSuccess) e = axpby<double>(m, m, 16.0 / (4.0 * g.nx * g.ny), 0.0, g.nG, s);
-    if (e == cudaSuccess) e = poisson(h, b, x, 1, nullptr, m, 0, nullptr, w);
+    SolveOp op = op_lap(h);
+    op.m64 = m;
+    if (e == cudaSuccess) e = poisson64(h, b, x, 1, nullptr, op, nullptr, w);
   }
   cudaStreamSynchronize(s);
   cudaFree(w);

@@ -39,8 +39,10 @@ extern "C" {
 #define IB_ERR_CG_MAXITER 6         /* Schur CG hit its iteration cap */
 #define IB_ERR_UNSUPPORTED 7        /* feature not available in this build */
 
-/* arithmetic of the fluid solve (the Schur solve and forces are FP64 in every mode) */
-#define IB_PREC_FP64 0
+/* arithmetic of the fluid solve (state, nonlinear term, Schur solve and forces are FP64 in
+ * every mode) */
+#define IB_PREC_FP64 0   /* every sine transform in FP64 (the reference's arithmetic) */
+#define IB_PREC_MIXED 1  /* sine transforms in FP32 with one FP64-residual refinement per solve */
 
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */

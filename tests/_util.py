@@ -12,12 +12,12 @@ def oracle_problem(O, wl, prob):
     return O.Problem(g, wl.dt, wl.Re, xb, ds, [b.npoints() for b in bodies], freestream=wl.freestream)
 
 
-def start_pair(ib, O, wl):
+def start_pair(ib, O, wl, precision="fp64"):
     """GPU state/solver and oracle state/solver from the same seeded initial condition."""
     prob = wl.problem()
     st = ib.initstate(prob)
     st._gamma[:] = wl.initial_gamma()
-    solver = ib.initsolver(prob, st)
+    solver = ib.initsolver(prob, st, precision=precision)
     solver.vort2flux(st)
     op = oracle_problem(O, wl, prob)
     g = op.grid

@@ -73,6 +73,7 @@ SIGNATURES = {
     # operators (device pointers passed as integers)
     "ib_op_dst2": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_laplacian_inv": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
+    "ib_op_laplacian_inv_noalloc": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_cn_a": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_cn_ainv": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_curl": (C.c_int, [_vp, _vp, _vp, _vp]),

@@ -254,6 +254,18 @@ struct ProfScope {
 };
 
 // ----------------------------------------------------------------------------------------------
+// read-only view of a handle's Laplacian-inverse operator (geometry, FP64 tables, multipliers,
+// stream) for entry points implemented outside solver.cu
+// ----------------------------------------------------------------------------------------------
+struct LapView {
+  Geometry g;
+  DstAxis<double> ax, ay;
+  const double* mlap;
+  cudaStream_t stream;
+  int device;
+};
+
+// ----------------------------------------------------------------------------------------------
 // misc
 // ----------------------------------------------------------------------------------------------
 template <typename T>
@@ -262,3 +274,9 @@ template <typename T>
 cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s);  // y = a x + b y
 
 }  // namespace ib
+
+struct ib_handle;
+// fills `v` from the handle; returns false for a null handle
+bool ib_handle_lap_view(const ib_handle* h, ib::LapView* v);
+// records `msg` as the handle's last error and returns `code`
+int ib_handle_fail(ib_handle* h, int code, const char* msg);

@@ -485,6 +485,19 @@ int one_step(ib_handle* h, double t, double u, double v) {
 
 }  // namespace
 
+bool ib_handle_lap_view(const ib_handle* h, ib::LapView* v) {
+  if (!h || !v) return false;
+  v->g = h->g;
+  v->ax = h->axx.d;
+  v->ay = h->axy.d;
+  v->mlap = h->mLap;
+  v->stream = h->stream;
+  v->device = h->device;
+  return true;
+}
+
+int ib_handle_fail(ib_handle* h, int code, const char* msg) { return fail(h, code, msg); }
+
 // ================================================================================================
 // C ABI
 // ================================================================================================

@@ -24,6 +24,15 @@ int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out);
 /* LaplacianInv with lap_eigs (fluid-ops.jl:42-61): x = DST(DST(b) * scale / Λ) */
 int ib_op_laplacian_inv(ib_handle* h, int32_t batch, const double* b, double* x);
 
+/* Same result as ib_op_laplacian_inv, for callers that cannot allocate device memory while they
+ * solve (their device memory belongs to another allocator or pool, or their loop cannot afford
+ * an allocation's device-wide synchronisation).  No counterpart in the reference.  The work
+ * buffer is a fixed 4,194,304-value FP64 array inside the library (32 MiB held on every device
+ * that loads it), so batch * (nx-1)*(ny-1) must not exceed 4,194,304 (IB_ERR_INVALID
+ * otherwise).  The first call on a device looks up the array's device address and should come
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU race. */
+int ib_op_laplacian_inv_noalloc(ib_handle* h, int32_t batch, const double* b, double* x);
+
 /* A[lev] and Ainv[lev] of A_Ainv_linearmaps (src/streamfcn/cnab/ops.jl:14-42); lev 1-based */
 int ib_op_cn_a(ib_handle* h, int32_t lev, const double* b, double* x);
 int ib_op_cn_ainv(ib_handle* h, int32_t lev, const double* b, double* x);

@@ -202,12 +202,12 @@ def pass_model(wl, precision: str):
     return {"x": (x_bytes, x_launches, x_flops), "y": (y_bytes, y_launches, y_flops)}
 
 
-def run_arm(ib, lib, L, wl, precision, K, W, local, dist, profile_range=False):
+def run_arm(ib, lib, L, wl, precision, K, W, local, dist, profile_range=False, refine=0):
     """Set up one solver and time K steps (after W warm-up steps) with CUDA events."""
     prob = wl.problem()
     st = ib.initstate(prob)
     st._gamma[:] = wl.initial_gamma()
-    solver = ib.initsolver(prob, st, device=local, precision=precision)
+    solver = ib.initsolver(prob, st, device=local, precision=precision, refine_sweeps=refine)
     solver.vort2flux(st)
     info = L.IbInfo()
     lib.ib_get_info(solver.handle, C.byref(info))
@@ -249,7 +249,7 @@ def run_ours(args, rank, world, local):
     wl = make_workload(ib, args.workload)
     K, W = args.steps, args.warmup
     prec = args.precision
-    arm = run_arm(ib, lib, L, wl, prec, K, W, local, dist, args.profile_range)
+    arm = run_arm(ib, lib, L, wl, prec, K, W, local, dist, args.profile_range, args.refine_sweeps)
     t_max = dist.max(arm["dev_s"])
     info = arm["info"]
     value = wl.cells_per_step * K * world / t_max
@@ -259,7 +259,9 @@ def run_ours(args, rank, world, local):
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + f64 residual/state",
         "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
-        "config": {"workload": describe(wl), "precision": prec, "cells_per_step": wl.cells_per_step,
+        "config": {"workload": describe(wl), "precision": prec,
+                   "refine_sweeps": (args.refine_sweeps or 2) if prec == "mixed" else 0,
+                   "cells_per_step": wl.cells_per_step,
                    "parallelism": "replicas",
                    "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),
                    "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": arm["host_s"] / K * 1e3},
@@ -387,6 +389,7 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="arithmetic of the timed arm (mixed: FP32 transforms + FP64 residual refinement)")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip timing the FP64 GPU path beside it")
+    ap.add_argument("--refine-sweeps", type=int, default=0, help="mixed precision: FP64-residual sweeps (0: default)")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()

@@ -51,7 +51,7 @@ class IbProblem(C.Structure):
         ("re", C.c_double),
         ("nbodies", C.c_int32), ("body_npoints", _ip), ("xb", _dp), ("ds", _dp),
         ("motion", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32),
-        ("history_capacity", C.c_int32),
+        ("history_capacity", C.c_int32), ("refine_sweeps", C.c_int32),
     ]
 
 

@@ -381,12 +381,13 @@ class Solver:
     """``CNAB.Solver`` (cnab/timestepping.jl:173-249) backed by a libibgb300 handle.
 
     ``precision``: ``"fp64"`` (every sine transform in FP64, the reference's arithmetic) or
-    ``"mixed"`` (FP32 sine transforms with one FP64-residual refinement per Poisson solve;
-    state, nonlinear term, Schur solve and forces stay FP64).
+    ``"mixed"`` (FP32 sine transforms refined with FP64 residuals, ``refine_sweeps`` sweeps per
+    Poisson solve, 0 = the library default of 2; state, nonlinear term, Schur solve and forces
+    stay FP64).
     """
 
     def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096,
-                 precision: str = "fp64"):
+                 precision: str = "fp64", refine_sweeps: int = 0):
         if not isinstance(prob.scheme, SchemeCNAB):
             raise NotImplementedError(f"no solver for scheme {type(prob.scheme).__name__}")
         for b in prob.bodies:
@@ -426,6 +427,7 @@ class Solver:
         p.precision = _lib.PRECISIONS[precision]
         p.device = device
         p.history_capacity = history_capacity
+        p.refine_sweeps = refine_sweeps
         h = C.c_void_p()
         _lib.check(self.lib, None, self.lib.ib_create(C.byref(p), C.byref(h)))
         self.handle = h

@@ -4,15 +4,17 @@
 // (src/streamfcn/fluid-ops.jl:19-56) and the CN multipliers of `A_Ainv_linearmaps`
 // (src/streamfcn/cnab/ops.jl:14-42).
 //
-// One warp transforms one line (a row for the x pass, a column for the y pass) held in
-// shared memory.  The DST-I of the n-1 interior values of an n-cell axis,
+// A group of kGroup = 64 threads transforms one line (a row for the x pass, a column for the
+// y pass) held in shared memory.  The DST-I of the n-1 interior values of an n-cell axis,
 //     F_k = sum_{j=1}^{n-1} y_j sin(pi j k / n),
 // is computed without the 2x padding of an odd extension:
 //   1. u_j = sin(pi j/n)(y_j + y_{n-j}) + (y_j - y_{n-j})/2         (in place, pairs j, n-j)
 //   2. U = real DFT_n(u) through a complex Stockham FFT of length M = n/2
-//      (mixed radix 8/4/2/3/5, register-staged stages, twiddles from a table)
+//      (mixed radix 8/4/2/3/5, ping-pong buffers padded one slot in nine against bank
+//      conflicts, twiddles from a table)
 //   3. split: F_{2k} = -Im U_k,  D_k = Re U_k                         (pairs k, M-k)
-//   4. F_{2k+1} = D_0/2 + D_1 + ... + D_k                             (warp prefix sum)
+//   4. F_{2k+1} = D_0/2 + D_1 + ... + D_k                             (prefix sum: per-thread
+//      Kahan-compensated chunks, then a scan of the chunk totals across the group)
 // (the half-length sine transform of Numerical Recipes "sinft", restated for a warp).
 // F is half of FFTW's RODFT00 output; the factor 2 per axis is folded into the
 // spectral multipliers, which are multiplied by 16 (exact in binary floating point).
@@ -109,20 +111,29 @@ template <typename T> struct Dft<T, 5> {
   }
 };
 
-// One Stockham stage of radix R on a length-M complex line, executed by one warp, from
-// `src` to `dst` (ping-pong buffers in shared memory).  Butterfly j reads src[j + r*M/R],
-// applies e^{-2 pi i r k/(Ns R)} (k = j mod Ns) and writes dst[(j-k)R + k + r Ns].
+constexpr int kGroup = 64;  // threads per line
+
+// padded complex index: one spare slot after every 8 complex values
+__device__ __forceinline__ int cpad(int i) { return i + (i >> 3); }
+// padded index of the prefix-sum workspace: one spare slot after every 32 values
+__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
+
+// One Stockham stage of radix R on a length-M complex line, executed by the kGroup threads of a
+// line, from `src` to `dst`.  Butterfly j reads src[j + r*M/R], applies e^{-2 pi i r k/(Ns R)}
+// (k = j mod Ns) and writes dst[(j-k)R + k + r Ns].  Buffers use the padded layout, except a
+// first stage, which reads the pre-processed line in its natural layout.
 template <typename T, int R>
 __device__ __forceinline__ void fft_stage(const c2_t<T>* __restrict__ src, c2_t<T>* __restrict__ dst, int M, int Ns,
-                                          const c2_t<T>* __restrict__ tw, int lane) {
+                                          const c2_t<T>* __restrict__ tw, int t, bool first) {
   using V = c2_t<T>;
   const int nb = M / R;
   const int tstride = M / (Ns * R);
-  for (int j = lane; j < nb; j += 32) {
-    const int k = j % Ns;
+  const bool pow2 = (Ns & (Ns - 1)) == 0;
+  for (int j = t; j < nb; j += kGroup) {
+    const int k = pow2 ? (j & (Ns - 1)) : (j % Ns);
     V v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
+    for (int r = 0; r < R; ++r) v[r] = first ? src[j + r * nb] : src[cpad(j + r * nb)];
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * tstride]));
@@ -130,83 +141,99 @@ __device__ __forceinline__ void fft_stage(const c2_t<T>* __restrict__ src, c2_t<
     Dft<T, R>::run(v);
     const int base = (j - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) dst[base + r * Ns] = v[r];
+    for (int r = 0; r < R; ++r) dst[cpad(base + r * Ns)] = v[r];
   }
-  __syncwarp();
 }
 
 template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
 template <> __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 
-// In-place DST-I (F convention, see file header) of s[1..n-1]; s and scratch must be 16-byte
-// aligned and hold n values each.  Executed by one full warp.
+// Shared-memory values per line buffer: the padded complex FFT layout of n reals, rounded to a
+// multiple of 4 values so consecutive buffers stay 16-byte aligned.
+__host__ __device__ inline int line_buffer_values(int n) { return (n + n / 8 + 8 + 3) & ~3; }
+// Prefix-sum workspace: M = n/2 values padded one in 32, plus two exchange slots.
+__host__ __device__ inline int scan_buffer_values(int n) { return ((n / 2 + n / 64 + 4) + 3) & ~3; }
+// All shared memory of one line.
+__host__ __device__ inline int line_values(int n) { return 2 * line_buffer_values(n) + scan_buffer_values(n); }
+
+// In-place DST-I (F convention, see file header) of s[1..n-1] by the kGroup threads of a line
+// (t = thread index in the group).  s and scratch hold line_buffer_values(n) values each, D
+// holds scan_buffer_values(n); all 16-byte aligned.  Every thread of the block must call it
+// (it contains __syncthreads).
 template <typename T>
-__device__ __noinline__ void dst1_warp(T* s, T* scratch, const DstAxis<T>& ax, int lane) {
+__device__ void dst1_line(T* s, T* scratch, T* D, const DstAxis<T>& ax, int t) {
   using V = c2_t<T>;
-  const int n = ax.n, M = ax.M, hn = n >> 1;
-  // 1. pre-processing
-  for (int j = 1 + lane; j < hn; j += 32) {
+  const int n = ax.n, M = ax.M, hn = n >> 1, hM = M >> 1;
+  // 1. pre-processing, natural layout
+  for (int j = 1 + t; j < hn; j += kGroup) {
     const T a = s[j], b = s[n - j];
     const T sm = a + b, df = T(0.5) * (a - b);
     const T sn = __ldg(&ax.sintab[j]);
     s[j] = fmaT(sn, sm, df);
     s[n - j] = fmaT(sn, sm, -df);
   }
-  if (lane == 0) {
+  if (t == 0) {
     s[0] = T(0);
     s[hn] = T(2) * s[hn];
   }
-  __syncwarp();
+  __syncthreads();
   // 2. complex FFT of length M, ping-pong between s and scratch
   V* src = reinterpret_cast<V*>(s);
   V* dst = reinterpret_cast<V*>(scratch);
   int Ns = 1;
   for (int st = 0; st < ax.nstages; ++st) {
     const int R = ax.radix[st];
+    const bool first = st == 0;
     switch (R) {
-      case 8: fft_stage<T, 8>(src, dst, M, Ns, ax.tw, lane); break;
-      case 4: fft_stage<T, 4>(src, dst, M, Ns, ax.tw, lane); break;
-      case 2: fft_stage<T, 2>(src, dst, M, Ns, ax.tw, lane); break;
-      case 3: fft_stage<T, 3>(src, dst, M, Ns, ax.tw, lane); break;
-      default: fft_stage<T, 5>(src, dst, M, Ns, ax.tw, lane); break;
+      case 8: fft_stage<T, 8>(src, dst, M, Ns, ax.tw, t, first); break;
+      case 4: fft_stage<T, 4>(src, dst, M, Ns, ax.tw, t, first); break;
+      case 2: fft_stage<T, 2>(src, dst, M, Ns, ax.tw, t, first); break;
+      case 3: fft_stage<T, 3>(src, dst, M, Ns, ax.tw, t, first); break;
+      default: fft_stage<T, 5>(src, dst, M, Ns, ax.tw, t, first); break;
     }
+    __syncthreads();
     Ns *= R;
     V* tmp = src;
     src = dst;
     dst = tmp;
   }
-  // 3. split the real DFT: pairs (k, M-k), read from the FFT result, written into s
+  // 3. split the real DFT: pairs (k, M-k) read from the FFT result (padded); F_{2k} goes to
+  //    whichever line buffer does not hold the result (natural layout), D_k to the prefix-sum
+  //    workspace D
   const V* z = src;
-  V* c = reinterpret_cast<V*>(s);
-  const int hM = M >> 1;
-  for (int k = 1 + lane; k < hM; k += 32) {
-    const V zk = z[k], zm = z[M - k];
+  T* fb = (reinterpret_cast<const T*>(z) == s) ? scratch : s;
+  for (int k = 1 + t; k < hM; k += kGroup) {
+    const V zk = z[cpad(k)], zm = z[cpad(M - k)];
     const T er = T(0.5) * (zk.x + zm.x), ei = T(0.5) * (zk.y - zm.y);
     const T orr = T(0.5) * (zk.y + zm.y), oi = T(0.5) * (zm.x - zk.x);
     const V w = __ldg(&ax.post[k]);
     const T tr = w.x * orr - w.y * oi, ti = w.x * oi + w.y * orr;
-    c[k] = mk<V>(-(ei + ti), er + tr);
-    c[M - k] = mk<V>(ei - ti, er - tr);
+    fb[2 * k] = -(ei + ti);
+    D[spad(k)] = er + tr;
+    fb[2 * (M - k)] = ei - ti;
+    D[spad(M - k)] = er - tr;
   }
-  if (lane == 0) {
-    const V z0 = z[0];
-    const V zh = z[hM];
-    c[0] = mk<V>(T(0), z0.x + z0.y);
-    c[hM] = mk<V>(zh.y, zh.x);
+  if (t == 0) {
+    const V z0 = z[cpad(0)], zh = z[cpad(hM)];
+    D[spad(0)] = T(0.5) * (z0.x + z0.y);  // D_0 / 2
+    fb[2 * hM] = zh.y;                    // F_M
+    D[spad(hM)] = zh.x;
   }
-  __syncwarp();
-  // 4. odd outputs: prefix sum of D over k (chunked per lane, then across lanes)
-  const int C = (M + 31) >> 5;
-  const int k0 = lane * C;
-  const int k1 = min(M, k0 + C);
-  T acc = T(0);
+  __syncthreads();
+  // 4. F_{2k+1} = sum_{k' <= k} D_k': compensated chunk sums, scan of chunk totals
+  const int C = (M + kGroup - 1) / kGroup;
+  const int k0 = t * C, k1 = min(M, k0 + C);
+  T acc = T(0), comp = T(0);
   for (int k = k0; k < k1; ++k) {
-    T d = s[2 * k + 1];
-    if (k == 0) d *= T(0.5);
-    acc += d;
-    s[2 * k + 1] = acc;
+    const T y = D[spad(k)] - comp;
+    const T tmp = acc + y;
+    comp = (tmp - acc) - y;
+    acc = tmp;
+    D[spad(k)] = acc;
   }
+  // inclusive scan of the chunk totals over the group (two warps)
+  const int lane = t & 31, wg = t >> 5;
   T incl = acc;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -215,128 +242,150 @@ __device__ __noinline__ void dst1_warp(T* s, T* scratch, const DstAxis<T>& ax, i
   }
   T excl = __shfl_up_sync(kFull, incl, 1);
   if (lane == 0) excl = T(0);
-  for (int k = k0; k < k1; ++k) s[2 * k + 1] += excl;
-  __syncwarp();
+  // warp 1 of the group adds warp 0's total (exchanged through the padding slot after the
+  // workspace, which no index above touches)
+  T* wtot = D + spad(M) + 1;
+  if (wg == 0 && lane == 31) wtot[0] = incl;
+  __syncthreads();
+  if (wg == 1) excl += wtot[0];
+  for (int k = k0; k < k1; ++k) D[spad(k)] += excl;
+  __syncthreads();
+  if (fb != s) {
+    for (int k = t; k < M; k += kGroup) {
+      s[2 * k] = fb[2 * k];
+      s[2 * k + 1] = D[spad(k)];
+    }
+  } else {
+    for (int k = t; k < M; k += kGroup) s[2 * k + 1] = D[spad(k)];
+  }
+  if (t == 0) s[0] = T(0);
+  __syncthreads();
 }
 
 // ------------------------------------------------------------------------------------------
-// x pass: one warp per row (contiguous); see XArgs for the prologue / epilogue variants.
-// Shared memory per warp: the row (n values) and the FFT scratch (n values).
+// x pass: kXLines rows per block, kGroup threads per row; see XArgs for the prologue /
+// epilogue variants.  Shared memory per row: the line and the FFT scratch.
 // ------------------------------------------------------------------------------------------
-constexpr int kXWarps = 4;
+constexpr int kXLines = 4;
 
 template <typename T, typename Tin, typename Tout, int PRO, int EPI, bool kBC>
-__global__ void __launch_bounds__(kXWarps * 32)
+__global__ void __launch_bounds__(kXLines * kGroup)
 k_xpass(Geometry g, DstAxis<T> ax, XArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n = ax.n;
-  T* s = reinterpret_cast<T*>(smem_raw) + warp * 2 * n;
-  T* scratch = s + n;
+  const int grp = threadIdx.x / kGroup, t = threadIdx.x % kGroup;
+  const int lb = line_buffer_values(ax.n);
+  T* s = reinterpret_cast<T*>(smem_raw) + grp * line_values(ax.n);
+  T* scratch = s + lb;
+  T* D = scratch + lb;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int total = a.batch * nrow;
   const Tin* in = static_cast<const Tin*>(a.in);
   Tout* out = static_cast<Tout*>(a.out);
-  for (int row = blockIdx.x * kXWarps + warp; row < total; row += gridDim.x * kXWarps) {
-    const int b = row / nrow, J = row - b * nrow;
+  for (int base = blockIdx.x * kXLines; base < total; base += gridDim.x * kXLines) {
+    const int row = base + grp;
+    const bool active = row < total;
+    const int b = active ? row / nrow : 0, J = active ? row - b * nrow : 0;
     const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
-    const Tin* src = in + off;
-    const double* bc = kBC ? a.bc + (int64_t)b * g.nbc : nullptr;
-    const double fac = a.bcfac;
-    if (PRO == kProLoad && !kBC && sizeof(Tin) == sizeof(T)) {
-      for (int I = lane; I < ncol; I += 32) s[I + 1] = (T)src[I];
-    } else {
-      // formed in FP64: input, apply_bc edges (rows first, then columns, as the reference),
-      // and for the refinement the residual of the first solution
-      const float* x0 = (PRO == kProResid) ? a.base + off : nullptr;
-      const double mc = (PRO == kProResid) ? a.mc[b * a.mstep] : 0.0;
-      const double ma = (PRO == kProResid) ? a.ma[b * a.mstep] : 0.0;
-      for (int I = lane; I < ncol; I += 32) {
-        double v = (double)src[I];
-        if (kBC) {
-          if (J == 0) v += fac * bc[g.B + 1 + I];
-          if (J == nrow - 1) v += fac * bc[g.T + 1 + I];
-          if (I == 0) v += fac * bc[g.L + 1 + J];
-          if (I == ncol - 1) v += fac * bc[g.R + 1 + J];
+    if (active) {
+      const Tin* src = in + off;
+      if (PRO == kProLoad && !kBC && sizeof(Tin) == sizeof(T)) {
+        for (int I = t; I < ncol; I += kGroup) s[I + 1] = (T)src[I];
+      } else {
+        // formed in FP64: input, apply_bc edges (rows then columns, as the reference) and, for
+        // the refinement, the residual of the first solution
+        const double* bc = kBC ? a.bc + (int64_t)b * g.nbc : nullptr;
+        const double fac = a.bcfac;
+        const float* x0 = (PRO == kProResid) ? a.base + off : nullptr;
+        const float* x1 = (PRO == kProResid && a.base2) ? a.base2 + off : nullptr;
+        const double mc = (PRO == kProResid) ? a.mc[b * a.mstep] : 0.0;
+        const double ma = (PRO == kProResid) ? a.ma[b * a.mstep] : 0.0;
+        for (int I = t; I < ncol; I += kGroup) {
+          double v = (double)src[I];
+          if (kBC) {
+            if (J == 0) v += fac * bc[g.B + 1 + I];
+            if (J == nrow - 1) v += fac * bc[g.T + 1 + I];
+            if (I == 0) v += fac * bc[g.L + 1 + J];
+            if (I == ncol - 1) v += fac * bc[g.R + 1 + J];
+          }
+          if (PRO == kProResid) {
+            auto X = [&](int i) { return x1 ? (double)x0[i] + (double)x1[i] : (double)x0[i]; };
+            const double xc = X(I);
+            double lap = 4.0 * xc;
+            if (I > 0) lap -= X(I - 1);
+            if (I < ncol - 1) lap -= X(I + 1);
+            if (J > 0) lap -= X(I - ncol);
+            if (J < nrow - 1) lap -= X(I + ncol);
+            v = v - (mc * xc + ma * lap);
+          }
+          s[I + 1] = (T)v;
         }
-        if (PRO == kProResid) {
-          const double xc = (double)x0[I];
-          double lap = 4.0 * xc;
-          if (I > 0) lap -= (double)x0[I - 1];
-          if (I < ncol - 1) lap -= (double)x0[I + 1];
-          if (J > 0) lap -= (double)x0[I - ncol];
-          if (J < nrow - 1) lap -= (double)x0[I + ncol];
-          v = v - (mc * xc + ma * lap);
-        }
-        s[I + 1] = (T)v;
       }
     }
-    __syncwarp();
-    dst1_warp<T>(s, scratch, ax, lane);
-    Tout* dst = out + off;
-    if (EPI == kEpiStore) {
-      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)s[I + 1];
-    } else if (EPI == kEpiSub) {
-      const double* sf = a.sub_from + off;
-      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - (double)s[I + 1]);
-    } else if (EPI == kEpiAddBase) {
-      const float* bs = a.base + off;
-      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)((double)bs[I] + (double)s[I + 1]);
-    } else {
-      const double* sf = a.sub_from + off;
-      const float* bs = a.base + off;
-      for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - ((double)bs[I] + (double)s[I + 1]));
+    __syncthreads();
+    dst1_line<T>(s, scratch, D, ax, t);
+    if (active) {
+      Tout* dst = out + off;
+      if (EPI == kEpiStore) {
+        for (int I = t; I < ncol; I += kGroup) dst[I] = (Tout)s[I + 1];
+      } else if (EPI == kEpiSub) {
+        const double* sf = a.sub_from + off;
+        for (int I = t; I < ncol; I += kGroup) dst[I] = (Tout)(sf[I] - (double)s[I + 1]);
+      } else {
+        const float* bs = a.base + off;
+        const float* bs2 = a.base2 ? a.base2 + off : nullptr;
+        const double* sf = (EPI == kEpiSubAddBase) ? a.sub_from + off : nullptr;
+        for (int I = t; I < ncol; I += kGroup) {
+          double xv = (double)bs[I];
+          if (bs2) xv += (double)bs2[I];
+          xv += (double)s[I + 1];
+          dst[I] = (Tout)((EPI == kEpiSubAddBase) ? sf[I] - xv : xv);
+        }
+      }
     }
-    __syncwarp();
+    __syncthreads();
   }
 }
 
 // ------------------------------------------------------------------------------------------
-// y pass: one CTA per strip of W columns, one warp per column; forward DST, spectral
+// y pass: one block per strip of W columns, kGroup threads per column; forward DST, spectral
 // multiply, second DST.  Multipliers are stored column-major in spectral space
-// (index I*(ny-1) + J) so a warp reads them contiguously.
-// Shared memory per warp: the column and the FFT scratch, n values each, padded to keep
-// 16-byte alignment.
+// (index I*(ny-1) + J) so a column reads them contiguously.
+// Shared memory per column: the line and the FFT scratch.
 // ------------------------------------------------------------------------------------------
 template <typename T, SpecOp OP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(512)
 k_ypass(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int W = blockDim.x >> 5;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n = ax.n;
-  const int ps = n + 16 / (int)sizeof(T);
-  T* P = reinterpret_cast<T*>(smem_raw);
-  T* S = P + W * ps;
+  const int W = blockDim.x / kGroup;
+  const int grp = threadIdx.x / kGroup, t = threadIdx.x % kGroup;
+  const int lb = line_buffer_values(ax.n), lv = line_values(ax.n);
+  T* p = reinterpret_cast<T*>(smem_raw) + grp * lv;
+  T* sc = p + lb;
+  T* D = sc + lb;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int nstrips = (ncol + W - 1) / W;
   for (int blk = blockIdx.x; blk < a.batch * nstrips; blk += gridDim.x) {
     const int b = blk / nstrips, I0 = (blk - b * nstrips) * W;
     const int64_t off = (int64_t)b * a.stride;
+    T* P = reinterpret_cast<T*>(smem_raw);
     for (int idx = threadIdx.x; idx < nrow * W; idx += blockDim.x) {
       const int J = idx / W, w = idx - J * W, I = I0 + w;
-      const int64_t gi = off + (int64_t)J * ncol + I;
-      P[w * ps + J + 1] = (I < ncol) ? a.in1[gi] : T(0);
+      P[w * lv + J + 1] = (I < ncol) ? a.in1[off + (int64_t)J * ncol + I] : T(0);
     }
     __syncthreads();
-    {
-      T* p = P + warp * ps;
-      T* sc = S + warp * ps;
-      const int I = I0 + warp;
-      dst1_warp<T>(p, sc, ax, lane);
-      const int64_t mo = (int64_t)b * a.mstride + (int64_t)min(I, ncol - 1) * nrow;
-      if (OP == SpecOp::kScale) {
-        for (int J = lane; J < nrow; J += 32) p[J + 1] *= __ldg(&a.m1[mo + J]);
-      } else {
-        for (int J = lane; J < nrow; J += 32) p[J + 1] *= a.scal;
-      }
-      __syncwarp();
-      if (OP != SpecOp::kFwd) dst1_warp<T>(p, sc, ax, lane);
+    const int I = I0 + grp;
+    dst1_line<T>(p, sc, D, ax, t);
+    const int64_t mo = (int64_t)b * a.mstride + (int64_t)min(I, ncol - 1) * nrow;
+    if (OP == SpecOp::kScale) {
+      for (int J = t; J < nrow; J += kGroup) p[J + 1] *= __ldg(&a.m1[mo + J]);
+    } else {
+      for (int J = t; J < nrow; J += kGroup) p[J + 1] *= a.scal;
     }
     __syncthreads();
+    if (OP != SpecOp::kFwd) dst1_line<T>(p, sc, D, ax, t);
     for (int idx = threadIdx.x; idx < nrow * W; idx += blockDim.x) {
-      const int J = idx / W, w = idx - J * W, I = I0 + w;
-      if (I < ncol) a.out[off + (int64_t)J * ncol + I] = P[w * ps + J + 1];
+      const int J = idx / W, w = idx - J * W, Ic = I0 + w;
+      if (Ic < ncol) a.out[off + (int64_t)J * ncol + Ic] = P[w * lv + J + 1];
     }
     __syncthreads();
   }
@@ -358,11 +407,12 @@ cudaError_t ensure_smem(const void* fn, size_t bytes) {
   return e;
 }
 
+// Radix plan of an M-point FFT: powers of two first (8s, then a 4/4, 4 or 2 remainder), then 3s,
+// then 5s, so the leading stages have power-of-two strides (k = j & (Ns-1)).
 int plan_radices(int M, int* radix) {
-  int m = M, ns = 0;
-  int p2 = 0;
-  while (m % 5 == 0) { radix[ns++] = 5; m /= 5; }
-  while (m % 3 == 0) { radix[ns++] = 3; m /= 3; }
+  int m = M, ns = 0, p2 = 0, n3 = 0, n5 = 0;
+  while (m % 5 == 0) { ++n5; m /= 5; }
+  while (m % 3 == 0) { ++n3; m /= 3; }
   while (m % 2 == 0) { ++p2; m /= 2; }
   if (m != 1) return -1;
   int a = p2 / 3, rem = p2 % 3;
@@ -370,6 +420,8 @@ int plan_radices(int M, int* radix) {
   else if (rem == 1) { radix[ns++] = 2; }
   else if (rem == 2) { radix[ns++] = 4; }
   for (int i = 0; i < a; ++i) radix[ns++] = 8;
+  for (int i = 0; i < n3; ++i) radix[ns++] = 3;
+  for (int i = 0; i < n5; ++i) radix[ns++] = 5;
   if (ns > kMaxStages) return -1;
   return ns;
 }
@@ -377,12 +429,12 @@ int plan_radices(int M, int* radix) {
 template <typename T, typename Tin, typename Tout, int PRO, int EPI, bool kBC>
 cudaError_t launch_x1(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
   const int total = a.batch * (g.ny - 1);
-  const int blocks = (total + kXWarps - 1) / kXWarps;
-  const size_t smem = (size_t)kXWarps * 2 * ax.n * sizeof(T);
+  const int blocks = (total + kXLines - 1) / kXLines;
+  const size_t smem = (size_t)kXLines * line_values(ax.n) * sizeof(T);
   auto k = k_xpass<T, Tin, Tout, PRO, EPI, kBC>;
   cudaError_t e = ensure_smem((const void*)k, smem);
   if (e != cudaSuccess) return e;
-  k<<<blocks, kXWarps * 32, smem, s>>>(g, ax, a);
+  k<<<blocks, kXLines * kGroup, smem, s>>>(g, ax, a);
   return cudaGetLastError();
 }
 
@@ -410,22 +462,22 @@ cudaError_t launch_x_epi(const Geometry& g, const DstAxis<T>& ax, const XArgs& a
 template <typename T>
 cudaError_t launch_y(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s) {
   ProfScope prof(kClassYPass, s);
-  const int nbuf = 2;
-  const int ps = ax.n + 16 / (int)sizeof(T);
-  int W = 8;
-  while (W > 1 && (size_t)nbuf * W * ps * sizeof(T) > 200 * 1024) W >>= 1;
-  const size_t smem = (size_t)nbuf * W * ps * sizeof(T);
+  const size_t per_col = (size_t)line_values(ax.n) * sizeof(T);
+  // 4 columns per block for a single array (more blocks than SMs), 8 for batches
+  int W = (a.batch > 1) ? 8 : 4;
+  while (W > 1 && (size_t)W * per_col > 200 * 1024) W >>= 1;
+  const size_t smem = (size_t)W * per_col;
   const int nstrips = (g.nx - 1 + W - 1) / W;
   const int blocks = a.batch * nstrips;
   cudaError_t e;
   if (a.op == SpecOp::kFwd) {
     auto k = k_ypass<T, SpecOp::kFwd>;
     if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
+    k<<<blocks, W * kGroup, smem, s>>>(g, ax, a);
   } else {
     auto k = k_ypass<T, SpecOp::kScale>;
     if ((e = ensure_smem((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, W * 32, smem, s>>>(g, ax, a);
+    k<<<blocks, W * kGroup, smem, s>>>(g, ax, a);
   }
   return cudaGetLastError();
 }

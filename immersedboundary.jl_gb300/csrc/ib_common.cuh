@@ -91,13 +91,14 @@ enum class SpecOp : int {
 // x pass: a 1-D sine transform along x of every row of `batch` arrays (compute type T).
 // prologue (how a row is formed before the transform):
 //   kProLoad   row = in                                  (in: Tin)
-//   kProResid  row = in - M x0, M x = mc*x + ma*rot(curl(x)), formed in FP64   (x0 = base)
+//   kProResid  row = in - M x0, M x = mc*x + ma*rot(curl(x)), formed in FP64
+//              (x0 = base, or base + base2 when base2 is given: an exact FP32 pair)
 // either optionally plus fac * apply_bc(bc) on the edges (bc != nullptr)
 // epilogue (what is stored):
 //   kEpiStore       out = row                              (out: Tout)
 //   kEpiSub         out = sub_from - row
-//   kEpiAddBase     out = base + row                       (FP64 sum)
-//   kEpiSubAddBase  out = sub_from - (base + row)
+//   kEpiAddBase     out = base [+ base2] + row             (FP64 sum)
+//   kEpiSubAddBase  out = sub_from - (base [+ base2] + row)
 enum XPro : int { kProLoad = 0, kProResid = 1 };
 enum XEpi : int { kEpiStore = 0, kEpiSub = 1, kEpiAddBase = 2, kEpiSubAddBase = 3 };
 
@@ -110,6 +111,7 @@ struct XArgs {
   double bcfac;
   const double* sub_from;   // kEpiSub / kEpiSubAddBase
   const float* base;        // x0 of the refinement (kProResid, kEpiAddBase)
+  const float* base2;       // optional second FP32 part of x0 (second refinement sweep)
   const double* mc;         // residual operator per slot (stride mstep)
   const double* ma;
   int mstep;

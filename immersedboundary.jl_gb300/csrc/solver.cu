@@ -66,6 +66,8 @@ struct ib_handle {
   double *mLap = nullptr, *mCN1 = nullptr, *mCN2 = nullptr;
   float *mLap32 = nullptr, *mCN1_32 = nullptr;  // FP32 copies (mixed precision)
   float *w32 = nullptr, *x032 = nullptr;        // mixed-precision work: transforms and x0
+  float *x132 = nullptr;                        // second FP32 part of the iterate (2 sweeps)
+  int refine = 1;                               // refinement sweeps per mixed-precision solve
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
   double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr, *d_alpha = nullptr;
@@ -179,11 +181,15 @@ cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, co
   return xpass<double, double, double>(h->g, h->axx.d, xb, h->stream);
 }
 
-// Mixed-precision solve: FP32 sine transforms, one refinement with an FP64 residual.
-//   x0 = F32 solve(b);  r = b - M x0 (FP64, fused into the next x pass);  x = x0 + F32 solve(r)
-// b, the result and the residual arithmetic are FP64; w32 / x032: FP32 work of batch arrays.
+// Mixed-precision solve: FP32 sine transforms refined with FP64 residuals.
+//   x0 = F32 solve(b)
+//   sweep 1: r = b - M x0 (FP64, fused into the next x pass);  d1 = F32 solve(r)
+//   sweep 2 (optional): r = b - M (x0 + d1) with x0 + d1 an exact FP32 pair;  d2 = F32 solve(r)
+//   x = x0 + d1 [+ d2] summed in FP64 (optionally subtracted from sub_from)
+// b, the result and the residual arithmetic are FP64; w32 / x032 / x132: FP32 work of batch
+// arrays.
 cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
-                          const double* sub_from, float* w32, float* x032) {
+                          const double* sub_from, float* w32, float* x032, float* x132) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   YPassArgs<float> ya{};
@@ -204,12 +210,23 @@ cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch
   CE(ypass<float>(g, h->axy32.d, ya, s));
   a.in = w32; a.out = x032; a.bc = nullptr;
   CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
-  // residual (FP64) fused with the forward transform of the correction
-  a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+  const bool two = h->refine >= 2 && x132;
+  // sweep 1: residual (FP64) fused with the forward transform of the correction
+  a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
+  a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
   CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
   CE(ypass<float>(g, h->axy32.d, ya, s));
-  // x = x0 + correction, in FP64 (optionally subtracted from sub_from)
+  if (two) {
+    a.in = w32; a.out = x132; a.bc = nullptr; a.pro = kProLoad; a.epi = kEpiStore; a.base = nullptr;
+    CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
+    // sweep 2: residual of the FP32 pair x0 + d1
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = x132;
+    CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+    CE(ypass<float>(g, h->axy32.d, ya, s));
+  }
+  // x = x0 [+ d1] + correction, in FP64 (optionally subtracted from sub_from)
   a.in = w32; a.out = out; a.bc = nullptr; a.pro = kProLoad; a.sub_from = sub_from;
+  a.base = x032; a.base2 = two ? x132 : nullptr;
   a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
   return xpass<float, float, double>(g, h->axx32.d, a, s);
 }
@@ -217,7 +234,8 @@ cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch
 // Solve with the handle's precision mode (batch <= nlevels: uses the step's work buffers).
 cudaError_t solve(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
                   const double* sub_from) {
-  if (h->precision == IB_PREC_MIXED) return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032);
+  if (h->precision == IB_PREC_MIXED)
+    return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032, h->x132);
   return poisson64(h, in, out, batch, bc, op, sub_from, h->w1);
 }
 
@@ -400,8 +418,8 @@ int prime_kernels(ib_handle* h) {
   CK(poisson64(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w1));
   CK(poisson64(h, h->w2, h->w2, 1, nullptr, op_lap(h), h->w2, h->w1));
   if (h->precision == IB_PREC_MIXED) {
-    CK(poisson_mixed(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w32, h->x032));
-    CK(poisson_mixed(h, h->w2, h->w2, 1, nullptr, op_cn1(h), h->w2, h->w32, h->x032));
+    CK(poisson_mixed(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w32, h->x032, h->x132));
+    CK(poisson_mixed(h, h->w2, h->w2, 1, nullptr, op_cn1(h), h->w2, h->w32, h->x032, h->x132));
   }
   CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
@@ -567,6 +585,8 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   h->nf = 2 * nb;
   h->precision = p->precision;
   h->hist_cap = p->history_capacity > 0 ? p->history_capacity : 4096;
+  if (p->refine_sweeps < 0 || p->refine_sweeps > 2) return bail(fail(h, IB_ERR_INVALID, "refine_sweeps must be 0, 1 or 2"));
+  h->refine = p->refine_sweeps > 0 ? p->refine_sweeps : 2;
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
   const Geometry& g = h->g;
   const int L = g.nlev;
@@ -596,6 +616,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (h->precision == IB_PREC_MIXED) {
     AL(h->mLap32, nG); AL(h->mCN1_32, L * nG);
     AL(h->w32, L * nG); AL(h->x032, L * nG);
+    if (h->refine >= 2) AL(h->x132, L * nG);
   }
   AL(h->status, 4); AL(h->d_counter, 1);
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));

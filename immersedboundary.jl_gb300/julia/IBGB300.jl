@@ -45,6 +45,7 @@ struct IbProblem
     precision::Int32
     device::Int32
     history_capacity::Int32
+    refine_sweeps::Int32
 end
 
 struct IBError <: Exception
@@ -83,7 +84,7 @@ function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, syn
         p = IbProblem(fluid.domain.nx, fluid.domain.ny, nlevels(grid), first(xs), first(ys),
                       gridstep(base), scheme.dt, scheme.β[1], scheme.β[2], fluid.Re,
                       length(npts), pointer(npts), pointer(xb), pointer(ds), 0, precision,
-                      device, 4096)
+                      device, 4096, 0)
         st = ccall((:ib_create, libibgb300), Cint, (Ref{IbProblem}, Ref{Ptr{Cvoid}}), p, handle)
         check(st, C_NULL)
     end

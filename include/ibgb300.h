@@ -42,7 +42,7 @@ extern "C" {
 /* arithmetic of the fluid solve (state, nonlinear term, Schur solve and forces are FP64 in
  * every mode) */
 #define IB_PREC_FP64 0   /* every sine transform in FP64 (the reference's arithmetic) */
-#define IB_PREC_MIXED 1  /* sine transforms in FP32 with one FP64-residual refinement per solve */
+#define IB_PREC_MIXED 1  /* sine transforms in FP32 refined with FP64 residuals (refine_sweeps) */
 
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */
@@ -65,6 +65,7 @@ typedef struct ib_problem {
   int32_t precision;            /* IB_PREC_* */
   int32_t device;               /* CUDA device ordinal */
   int32_t history_capacity;     /* steps of C_D / C_L kept on the device (0 -> 4096) */
+  int32_t refine_sweeps;        /* IB_PREC_MIXED: FP64-residual sweeps per solve, 1 or 2 (0 -> 2) */
 } ib_problem;
 
 typedef struct ib_handle ib_handle;

@@ -628,3 +628,116 @@ def solve(prob: Problem, st: State, t0: float, nsteps: int, solver: Solver | Non
         if record is not None:
             record(i + 1, st)
     return solver
+
+
+# ---------------------------------------------------------------------------
+# Moving bodies (corrected restatement): src/bodies/body-points.jl:47-76,
+# src/streamfcn/cnab/timestepping.jl:122-139, src/streamfcn/cnab/ops.jl:104-114.
+#
+# The reference's moving-body branch cannot run (update_bodies! reads a field :ω that
+# RelativeFrame names Ω, copies positions into velocities, and a LabFrame fluid keeps a
+# stale dense Binv).  This restatement applies the evident fixes:
+#   * r = r0 + R(θ) xb,  v = v0 + Ω R'(θ) xb      (body-points.jl:49-65, field Ω)
+#   * the stacked velocities are the points' v    (body-points.jl:73)
+#   * E / E^T weights rebuilt every step           (structure-ops.jl:37-61)
+#   * Fb solves B Fb = E(qs + q0) - ub h by CG      (timestepping.jl:122-139, ops.jl:104-114),
+#     warm-started from the previous Fb like cg!(qty.Fb, ...), stopping when
+#     ||r|| <= tol ||rhs|| (tol 1e-10; the reference's reltol is relative to the first residual)
+# ---------------------------------------------------------------------------
+def rigid_motion(xb_body, r0, v0, theta, omega):
+    """Positions and velocities of body-frame points xb_body (n, 2) under a rigid motion."""
+    c, s = math.cos(theta), math.sin(theta)
+    R = np.array([[c, -s], [s, c]])
+    Rv = omega * np.array([[-s, -c], [c, -s]])
+    r = np.asarray(r0)[None, :] + xb_body @ R.T
+    v = np.asarray(v0)[None, :] + xb_body @ Rv.T
+    return r, v
+
+
+def cg_solve(apply_B, rhs, x0, tol=1e-10, maxiter=5000):
+    """Unpreconditioned conjugate gradients (the iteration of IterativeSolvers.cg!, 0.9.2).
+
+    Stops when ||b - A x|| <= tol * ||b||.  Returns (x, iterations, residual norm)."""
+    x = np.array(x0, dtype=np.float64)
+    r = rhs - apply_B(x)
+    bn = np.linalg.norm(rhs)
+    target = tol * bn
+    rr = float(r @ r)
+    if math.sqrt(rr) <= target:
+        return x, 0, math.sqrt(rr)
+    p = r.copy()
+    for it in range(1, maxiter + 1):
+        Ap = apply_B(p)
+        alpha = rr / float(p @ Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        rr_new = float(r @ r)
+        if math.sqrt(rr_new) <= target:
+            return x, it, math.sqrt(rr_new)
+        p = r + (rr_new / rr) * p
+        rr = rr_new
+    return x, maxiter, math.sqrt(rr)
+
+
+@dataclass
+class MovingProblem:
+    """A problem whose bodies move rigidly: ``kinematics(t) -> [(r0, v0, θ, Ω) per body]``."""
+
+    grid: Grid
+    dt: float
+    Re: float
+    xb_body: list            # per body (n_b, 2) body-frame points
+    ds: np.ndarray           # (nb,) stacked segment lengths
+    kinematics: object
+    beta: tuple = (1.5, -0.5)
+    freestream: object = (1.0, 0.0)
+    cg_tol: float = 1e-10
+    cg_maxiter: int = 5000
+
+    @property
+    def body_npoints(self):
+        return [x.shape[0] for x in self.xb_body]
+
+    def uv(self, t):
+        f = self.freestream
+        return tuple(f(t)) if callable(f) else tuple(f)
+
+    def points(self, t):
+        rs, vs = [], []
+        for xb, (r0, v0, th, om) in zip(self.xb_body, self.kinematics(t)):
+            r, v = rigid_motion(xb, r0, v0, th, om)
+            rs.append(r)
+            vs.append(v)
+        return np.concatenate(rs), np.concatenate(vs)
+
+
+class MovingSolver(Solver):
+    """``advance!`` for moving bodies with the corrections listed above."""
+
+    def __init__(self, prob: MovingProblem):
+        g = prob.grid
+        self.prob = prob
+        self.g = g
+        self.lam = lap_eigs(g)
+        self.expl, self.impl = cn_multipliers(g, prob.dt, prob.Re)
+        self.cg_iterations = []
+
+    def advance(self, st: State, t: float, warm=None):
+        g, prob = self.g, self.prob
+        xb, vb = prob.points(t)                       # update_bodies!
+        self.reg = reg_update(xb, g)                  # update!(reg, points)
+        st.q0 = base_flux(g, *prob.uv(t))
+        qs, gs = self.trial_state(st)
+        Q = qs[0] + st.q0[0]
+        ftmp = reg_gather(Q, self.reg, g) - np.concatenate([vb[:, 0], vb[:, 1]]) * g.h
+        x0 = st.fb if warm is None else warm
+        apply_B = lambda z: b_times(z, self.reg, g, self.lam, self.impl[0])
+        st.fb, it, res = cg_solve(apply_B, ftmp, x0, prob.cg_tol, prob.cg_maxiter)
+        self.cg_iterations.append(it)
+        update_stress(st, prob)
+        st.gamma = gs.copy()
+        qtmp = reg_scatter(st.fb, self.reg, g)
+        st.gamma[0] -= laplacian_inv(rot(qtmp, g), self.impl[0], g)
+        st.psi, st.q = vort2flux(st.gamma, g, self.lam)
+        st.t = float(t)
+        st.points, st.velocities = xb, vb

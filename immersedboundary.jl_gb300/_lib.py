@@ -27,6 +27,10 @@ IB_PREC_FP64 = 0
 IB_PREC_MIXED = 1
 PRECISIONS = {"fp64": IB_PREC_FP64, "mixed": IB_PREC_MIXED}
 IB_MOTION_STATIC = 0
+IB_MOTION_PRESCRIBED = 1
+IB_WARM_PREVIOUS = 0
+IB_WARM_EXTRAPOLATE = 1
+IB_WARM_ZERO = 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -64,6 +68,11 @@ SIGNATURES = {
     "ib_advance": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double]),
     "ib_advance_n": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
     "ib_vort2flux": (C.c_int, [_vp]),
+    "ib_advance_kin": (C.c_int, [_vp, C.c_double, C.c_double, C.c_double, _dp]),
+    "ib_advance_n_kin": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
+    "ib_set_cg_options": (C.c_int, [_vp, C.c_double, C.c_int32, C.c_int32]),
+    "ib_get_cg_stats": (C.c_int, [_vp, C.c_int32, _ip, _dp]),
+    "ib_get_body_points": (C.c_int, [_vp, _dp, _dp]),
     "ib_get_stress": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ib_get_force_history": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
     "ib_step_count": (C.c_int64, [_vp]),

@@ -320,6 +320,15 @@ class StreamFcnQuantities:
     def stress(self) -> list:
         return self._state._stress_list()
 
+    @property
+    def points(self):
+        """``BodyGroupPoints`` (body-points.jl:6-10): (positions, velocities), each (nb, 2)."""
+        s = self._state._solver
+        if s is None:
+            xb = np.concatenate([b.xb for b in self._state.prob.bodies]) if len(self._state.prob.bodies) else np.zeros((0, 2))
+            return xb, np.zeros_like(xb)
+        return s.body_points()
+
     # Julia field names
     Γ = gamma
     ψ = psi
@@ -391,8 +400,10 @@ class Solver:
         if not isinstance(prob.scheme, SchemeCNAB):
             raise NotImplementedError(f"no solver for scheme {type(prob.scheme).__name__}")
         for b in prob.bodies:
-            if not isinstance(b.frame, GridFrame):
-                raise NotImplementedError("only bodies fixed in the grid frame are supported")
+            if not isinstance(b.frame, (GridFrame, RelativeFrame)):
+                raise NotImplementedError(f"unsupported body frame {type(b.frame).__name__}")
+        # bodies in a RelativeFrame move rigidly (their xb are body-frame coordinates)
+        self.moving = any(isinstance(b.frame, RelativeFrame) for b in prob.bodies)
         if not isinstance(prob.fluid.domain.frame, LabFrame):
             raise NotImplementedError("base_flux! is only defined for a LabFrame fluid")
         self.lib = _lib.load()
@@ -420,7 +431,7 @@ class Solver:
         p.body_npoints = _lib.iptr(self._npts) if self.nbodies else None
         p.xb = _lib.dptr(self._xb) if self.nb else None
         p.ds = _lib.dptr(self._ds) if self.nb else None
-        p.motion = _lib.IB_MOTION_STATIC
+        p.motion = _lib.IB_MOTION_PRESCRIBED if self.moving else _lib.IB_MOTION_STATIC
         if precision not in _lib.PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(_lib.PRECISIONS)}")
         self.precision = precision
@@ -476,9 +487,43 @@ class Solver:
         self._check(self.lib.ib_get_force_history(self.handle, count, _lib.dptr(cd), _lib.dptr(cl)))
         return cd[:, : self.nbodies], cl[:, : self.nbodies]
 
+    def kinematics(self, t: float) -> np.ndarray:
+        """Per body (r0x, r0y, v0x, v0y, θ, Ω) at t from the RelativeFrame closures
+        (src/dynamics.jl:23-29); bodies fixed in the grid get the identity motion."""
+        k = np.zeros((self.nbodies, 6))
+        for i, b in enumerate(self.prob.bodies):
+            f = b.frame
+            if isinstance(f, RelativeFrame):
+                r, v = f.r(t), f.v(t)
+                k[i] = (r[0], r[1], v[0], v[1], f.theta(t), f.omega(t))
+        return k
+
+    def set_cg_options(self, tol: float = 1e-10, maxiter: int = 5000, warm_start: str = "previous"):
+        """CG tolerance (||r|| / ||rhs||), cap and warm start ("previous", "extrapolate" or "zero")."""
+        mode = {"previous": _lib.IB_WARM_PREVIOUS, "extrapolate": _lib.IB_WARM_EXTRAPOLATE,
+                "zero": _lib.IB_WARM_ZERO}[warm_start]
+        self._check(self.lib.ib_set_cg_options(self.handle, float(tol), int(maxiter), mode))
+
+    def cg_stats(self, count: int):
+        it = np.zeros(count, dtype=np.int32)
+        res = np.zeros(count)
+        self._check(self.lib.ib_get_cg_stats(self.handle, count, _lib.iptr(it), _lib.dptr(res)))
+        return it, res
+
+    def body_points(self):
+        xb = np.zeros(2 * max(self.nb, 1))
+        vb = np.zeros(2 * max(self.nb, 1))
+        self._check(self.lib.ib_get_body_points(self.handle, _lib.dptr(xb), _lib.dptr(vb)))
+        n = self.nb
+        return xb[: 2 * n].reshape(2, n).T.copy(), vb[: 2 * n].reshape(2, n).T.copy()
+
     def advance(self, state: State, t: float):
         u, v = self.prob.fluid.freestream(t)
-        self._check(self.lib.ib_advance(self.handle, float(t), u, v))
+        if self.moving:
+            kin = np.ascontiguousarray(self.kinematics(t).reshape(-1))
+            self._check(self.lib.ib_advance_kin(self.handle, float(t), u, v, _lib.dptr(kin)))
+        else:
+            self._check(self.lib.ib_advance(self.handle, float(t), u, v))
         state.t = float(t)
         state._stale = True
 
@@ -492,7 +537,12 @@ class Solver:
         if ts.size == 0:
             return
         uv = np.ascontiguousarray(np.array([self.prob.fluid.freestream(t) for t in ts], dtype=np.float64).reshape(-1))
-        self._check(self.lib.ib_advance_n(self.handle, int(ts.size), _lib.dptr(ts), _lib.dptr(uv)))
+        if self.moving:
+            kin = np.ascontiguousarray(np.concatenate([self.kinematics(t).reshape(-1) for t in ts]))
+            self._check(self.lib.ib_advance_n_kin(self.handle, int(ts.size), _lib.dptr(ts), _lib.dptr(uv),
+                                                  _lib.dptr(kin)))
+        else:
+            self._check(self.lib.ib_advance_n(self.handle, int(ts.size), _lib.dptr(ts), _lib.dptr(uv)))
         state.t = float(ts[-1])
         state._stale = True
 

@@ -252,19 +252,19 @@ cudaError_t update_stress_hd(const double* fb, int nb, int nbodies, const int* b
 
 template cudaError_t reg_gather<double>(const Geometry&, const double*, const double*, const int*, const double*, int,
                                         double*, int, int64_t, int64_t, cudaStream_t);
-template cudaError_t reg_gather<float>(const Geometry&, const float*, const double*, const int*, const double*, int,
+template cudaError_t reg_gather<df64>(const Geometry&, const df64*, const double*, const int*, const double*, int,
                                        double*, int, int64_t, int64_t, cudaStream_t);
 template cudaError_t reg_scatter<double>(const Geometry&, const double*, const int*, const double*, int, double*, int*,
                                          cudaStream_t);
-template cudaError_t reg_scatter<float>(const Geometry&, const double*, const int*, const double*, int, float*, int*,
+template cudaError_t reg_scatter<df64>(const Geometry&, const double*, const int*, const double*, int, df64*, int*,
                                         cudaStream_t);
 template cudaError_t reg_scatter_rot<double>(const Geometry&, const double*, const int*, const double*, int, double*,
                                              double*, int, int64_t, int*, cudaStream_t);
-template cudaError_t reg_scatter_rot<float>(const Geometry&, const double*, const int*, const double*, int, float*,
-                                            float*, int, int64_t, int*, cudaStream_t);
+template cudaError_t reg_scatter_rot<df64>(const Geometry&, const double*, const int*, const double*, int, df64*,
+                                            df64*, int, int64_t, int*, cudaStream_t);
 template cudaError_t unit_scatter_rot<double>(const Geometry&, const int*, const double*, int, int, int, double*,
                                               cudaStream_t);
-template cudaError_t unit_scatter_rot<float>(const Geometry&, const int*, const double*, int, int, int, float*,
+template cudaError_t unit_scatter_rot<df64>(const Geometry&, const int*, const double*, int, int, int, df64*,
                                              cudaStream_t);
 
 }  // namespace ib

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 
 namespace ib {
@@ -271,6 +272,9 @@ constexpr int kXLines = 4;
 template <typename T, typename Tin, typename Tout, int PRO, int EPI, bool kBC>
 __global__ void __launch_bounds__(kXLines * kGroup)
 k_xpass(Geometry g, DstAxis<T> ax, XArgs a) {
+  // exact arithmetic of the prologue / epilogue: FP64 in the FP64 path, float-float when the
+  // pass reads or writes float-float state (mixed path)
+  using A = typename std::conditional<is_df64<Tin>::value || is_df64<Tout>::value, df64, double>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int grp = threadIdx.x / kGroup, t = threadIdx.x % kGroup;
   const int lb = line_buffer_values(ax.n);
@@ -288,33 +292,33 @@ k_xpass(Geometry g, DstAxis<T> ax, XArgs a) {
     const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
     if (active) {
       const Tin* src = in + off;
-      if (PRO == kProLoad && !kBC && sizeof(Tin) == sizeof(T)) {
+      if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
         for (int I = t; I < ncol; I += kGroup) s[I + 1] = (T)src[I];
       } else {
-        // formed in FP64: input, apply_bc edges (rows then columns, as the reference) and, for
-        // the refinement, the residual of the first solution
-        const double* bc = kBC ? a.bc + (int64_t)b * g.nbc : nullptr;
-        const double fac = a.bcfac;
+        // input, apply_bc edges (rows then columns, as the reference) and, for the
+        // refinement, the residual of the first solution, in exact arithmetic
+        const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
+        const A fac = A(a.bcfac);
         const float* x0 = (PRO == kProResid) ? a.base + off : nullptr;
         const float* x1 = (PRO == kProResid && a.base2) ? a.base2 + off : nullptr;
-        const double mc = (PRO == kProResid) ? a.mc[b * a.mstep] : 0.0;
-        const double ma = (PRO == kProResid) ? a.ma[b * a.mstep] : 0.0;
+        const A mc = (PRO == kProResid) ? A(a.mc[b * a.mstep]) : A(0.0);
+        const A ma = (PRO == kProResid) ? A(a.ma[b * a.mstep]) : A(0.0);
         for (int I = t; I < ncol; I += kGroup) {
-          double v = (double)src[I];
+          A v = A(src[I]);
           if (kBC) {
-            if (J == 0) v += fac * bc[g.B + 1 + I];
-            if (J == nrow - 1) v += fac * bc[g.T + 1 + I];
-            if (I == 0) v += fac * bc[g.L + 1 + J];
-            if (I == ncol - 1) v += fac * bc[g.R + 1 + J];
+            if (J == 0) v = v + fac * bc[g.B + 1 + I];
+            if (J == nrow - 1) v = v + fac * bc[g.T + 1 + I];
+            if (I == 0) v = v + fac * bc[g.L + 1 + J];
+            if (I == ncol - 1) v = v + fac * bc[g.R + 1 + J];
           }
           if (PRO == kProResid) {
-            auto X = [&](int i) { return x1 ? (double)x0[i] + (double)x1[i] : (double)x0[i]; };
-            const double xc = X(I);
-            double lap = 4.0 * xc;
-            if (I > 0) lap -= X(I - 1);
-            if (I < ncol - 1) lap -= X(I + 1);
-            if (J > 0) lap -= X(I - ncol);
-            if (J < nrow - 1) lap -= X(I + ncol);
+            auto X = [&](int i) { return x1 ? A(x0[i]) + A(x1[i]) : A(x0[i]); };
+            const A xc = X(I);
+            A lap = A(4.0) * xc;
+            if (I > 0) lap = lap - X(I - 1);
+            if (I < ncol - 1) lap = lap - X(I + 1);
+            if (J > 0) lap = lap - X(I - ncol);
+            if (J < nrow - 1) lap = lap - X(I + ncol);
             v = v - (mc * xc + ma * lap);
           }
           s[I + 1] = (T)v;
@@ -328,16 +332,16 @@ k_xpass(Geometry g, DstAxis<T> ax, XArgs a) {
       if (EPI == kEpiStore) {
         for (int I = t; I < ncol; I += kGroup) dst[I] = (Tout)s[I + 1];
       } else if (EPI == kEpiSub) {
-        const double* sf = a.sub_from + off;
-        for (int I = t; I < ncol; I += kGroup) dst[I] = (Tout)(sf[I] - (double)s[I + 1]);
+        const A* sf = static_cast<const A*>(a.sub_from) + off;
+        for (int I = t; I < ncol; I += kGroup) dst[I] = (Tout)(sf[I] - A(s[I + 1]));
       } else {
         const float* bs = a.base + off;
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
-        const double* sf = (EPI == kEpiSubAddBase) ? a.sub_from + off : nullptr;
+        const A* sf = (EPI == kEpiSubAddBase) ? static_cast<const A*>(a.sub_from) + off : nullptr;
         for (int I = t; I < ncol; I += kGroup) {
-          double xv = (double)bs[I];
-          if (bs2) xv += (double)bs2[I];
-          xv += (double)s[I + 1];
+          A xv = A(bs[I]);
+          if (bs2) xv = xv + A(bs2[I]);
+          xv = xv + A(s[I + 1]);
           dst[I] = (Tout)((EPI == kEpiSubAddBase) ? sf[I] - xv : xv);
         }
       }
@@ -553,12 +557,12 @@ cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a
 
 template struct AxisTables<double>;
 template struct AxisTables<float>;
-// FP64 path: double in, double out.  Mixed path: FP32 transforms fed from FP64 inputs,
-// FP32 intermediates, FP64 results.
+// FP64 path: double in, double out.  Mixed path: FP32 transforms fed from float-float inputs,
+// FP32 intermediates, float-float results.
 template cudaError_t xpass<double, double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
-template cudaError_t xpass<float, double, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t xpass<float, df64, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
 template cudaError_t xpass<float, float, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
-template cudaError_t xpass<float, float, double>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t xpass<float, float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
 template cudaError_t ypass<double>(const Geometry&, const DstAxis<double>&, const YPassArgs<double>&, cudaStream_t);
 template cudaError_t ypass<float>(const Geometry&, const DstAxis<float>&, const YPassArgs<float>&, cudaStream_t);
 

@@ -9,6 +9,8 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+
+#include "df64.cuh"
 #include <string>
 #include <vector>
 
@@ -107,9 +109,9 @@ struct XArgs {
   void* out;                // Tout
   int batch;
   int64_t stride;           // elements between batch slots (in, out, base, sub_from)
-  const double* bc;         // apply_bc ring per slot (stride nbc) or nullptr
-  double bcfac;
-  const double* sub_from;   // kEpiSub / kEpiSubAddBase
+  const void* bc;           // apply_bc ring per slot (stride nbc) or nullptr; element type is the
+  double bcfac;             //   pass's exact type (double, or df64 in the mixed path)
+  const void* sub_from;     // kEpiSub / kEpiSubAddBase (same element type as bc)
   const float* base;        // x0 of the refinement (kProResid, kEpiAddBase)
   const float* base2;       // optional second FP32 part of x0 (second refinement sweep)
   const double* mc;         // residual operator per slot (stride mstep)
@@ -210,6 +212,20 @@ cudaError_t unit_scatter_rot(const Geometry& g, const int* body_idx, const doubl
 // stress (optional) = per-body column-major (n x 2) surface stress blocks
 cudaError_t update_stress_hd(const double* fb, int nb, int nbodies, const int* body_start, const double* ds,
                              double h, double dt, double* cd_cl_out, double* stress_out, cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
+// moving bodies and the Schur CG (cg.cu)
+// ----------------------------------------------------------------------------------------------
+// points of rigidly moving bodies: kin[6b..6b+5] = r0x, r0y, v0x, v0y, theta, omega; xb_body in
+// the body frame; xb / vb stacked [x..., y...]
+cudaError_t body_points(const double* xb_body, const double* kin, const int* body_of, int nb, double* xb,
+                        double* vb, cudaStream_t s);
+cudaError_t vec_axpy(double* y, const double* v, double a, int n, cudaStream_t s);
+cudaError_t vec_dot(const double* a, const double* b, int n, double* out, cudaStream_t s);
+// CG scalars in device memory sc[0] = r.r, sc[1] = p.Ap, sc[2] = r.r after the update
+cudaError_t cg_update_xr(double* x, double* r, const double* p, const double* Ap, const double* sc, int n,
+                         cudaStream_t s);
+cudaError_t cg_update_p(double* p, const double* r, double* sc, int n, cudaStream_t s);
 
 // ----------------------------------------------------------------------------------------------
 // dense linear algebra (linalg.cu)

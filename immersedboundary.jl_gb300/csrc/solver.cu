@@ -67,6 +67,7 @@ struct ib_handle {
   float *mLap32 = nullptr, *mCN1_32 = nullptr;  // FP32 copies (mixed precision)
   float *w32 = nullptr, *x032 = nullptr;        // mixed-precision work: transforms and x0
   float *x132 = nullptr;                        // second FP32 part of the iterate (2 sweeps)
+  double* conv = nullptr;                       // mixed precision: FP64 copy-out buffer of the state
   int refine = 1;                               // refinement sweeps per mixed-precision solve
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
@@ -80,6 +81,18 @@ struct ib_handle {
   double *cdcl = nullptr, *stress = nullptr, *hist = nullptr;
   int hist_cap = 4096;
   int* d_counter = nullptr;
+  // moving bodies (IB_MOTION_PRESCRIBED)
+  int motion = IB_MOTION_STATIC;
+  double *xb_body = nullptr, *vb = nullptr, *d_kin = nullptr;
+  int* body_of = nullptr;
+  double *cg_r = nullptr, *cg_p = nullptr, *cg_Ap = nullptr, *cg_sc = nullptr, *fb_prev = nullptr;
+  double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
+  double* h_sc = nullptr;  // pinned CG scalars read back each iteration
+  double cg_tol = 1e-10;
+  int cg_maxiter = 5000;
+  int warm_start = IB_WARM_PREVIOUS;
+  std::vector<int> cg_iters;
+  std::vector<double> cg_res;
   int* status = nullptr;  // [0] out of grid, [1] non-finite flux, [2] singular Schur matrix
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool use_graph = true;
@@ -181,15 +194,15 @@ cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, co
   return xpass<double, double, double>(h->g, h->axx.d, xb, h->stream);
 }
 
-// Mixed-precision solve: FP32 sine transforms refined with FP64 residuals.
+// Mixed-precision solve: FP32 sine transforms refined with float-float residuals.
 //   x0 = F32 solve(b)
-//   sweep 1: r = b - M x0 (FP64, fused into the next x pass);  d1 = F32 solve(r)
+//   sweep 1: r = b - M x0 (df64, fused into the next x pass);  d1 = F32 solve(r)
 //   sweep 2 (optional): r = b - M (x0 + d1) with x0 + d1 an exact FP32 pair;  d2 = F32 solve(r)
-//   x = x0 + d1 [+ d2] summed in FP64 (optionally subtracted from sub_from)
-// b, the result and the residual arithmetic are FP64; w32 / x032 / x132: FP32 work of batch
-// arrays.
-cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
-                          const double* sub_from, float* w32, float* x032, float* x132) {
+//   x = x0 + d1 [+ d2] summed in df64 (optionally subtracted from sub_from)
+// b, the result and the residual arithmetic are float-float (df64.cuh), so the whole solve runs
+// on the FP32 pipe; w32 / x032 / x132: FP32 work of batch arrays.
+cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
+                          const df64* sub_from, float* w32, float* x032, float* x132) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   YPassArgs<float> ya{};
@@ -206,55 +219,66 @@ cudaError_t poisson_mixed(ib_handle* h, const double* in, double* out, int batch
   a.bcfac = 1.0;
   // first solve
   a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
-  CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+  CE((xpass<float, df64, float>(g, h->axx32.d, a, s)));
   CE(ypass<float>(g, h->axy32.d, ya, s));
   a.in = w32; a.out = x032; a.bc = nullptr;
   CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
   const bool two = h->refine >= 2 && x132;
-  // sweep 1: residual (FP64) fused with the forward transform of the correction
+  // sweep 1: residual (df64) fused with the forward transform of the correction
   a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
   a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
-  CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+  CE((xpass<float, df64, float>(g, h->axx32.d, a, s)));
   CE(ypass<float>(g, h->axy32.d, ya, s));
   if (two) {
     a.in = w32; a.out = x132; a.bc = nullptr; a.pro = kProLoad; a.epi = kEpiStore; a.base = nullptr;
     CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
     // sweep 2: residual of the FP32 pair x0 + d1
     a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = x132;
-    CE((xpass<float, double, float>(g, h->axx32.d, a, s)));
+    CE((xpass<float, df64, float>(g, h->axx32.d, a, s)));
     CE(ypass<float>(g, h->axy32.d, ya, s));
   }
-  // x = x0 [+ d1] + correction, in FP64 (optionally subtracted from sub_from)
+  // x = x0 [+ d1] + correction, in df64 (optionally subtracted from sub_from)
   a.in = w32; a.out = out; a.bc = nullptr; a.pro = kProLoad; a.sub_from = sub_from;
   a.base = x032; a.base2 = two ? x132 : nullptr;
   a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
-  return xpass<float, float, double>(g, h->axx32.d, a, s);
+  return xpass<float, float, df64>(g, h->axx32.d, a, s);
 }
 
-// Solve with the handle's precision mode (batch <= nlevels: uses the step's work buffers).
+// Solve with the step's work buffers (batch <= nlevels); the state type picks the precision:
+// double -> FP64 transforms, df64 -> the mixed-precision solve.
 cudaError_t solve(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
                   const double* sub_from) {
-  if (h->precision == IB_PREC_MIXED)
-    return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032, h->x132);
   return poisson64(h, in, out, batch, bc, op, sub_from, h->w1);
+}
+cudaError_t solve(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
+                  const df64* sub_from) {
+  return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032, h->x132);
+}
+
+// The handle's state arrays hold doubles (FP64 mode) or float-float pairs (mixed mode); both are
+// 8 bytes, so one set of allocations serves either and is viewed with the mode's type.
+template <typename S>
+S* view(double* p) {
+  return reinterpret_cast<S*>(p);
 }
 
 // Vort2Flux (src/streamfcn/fluid-ops.jl:438-472) on one L-level set.  If q is null only the
 // level-1 flux is formed, into q1.  gam is coarsened in place like the reference.
-cudaError_t vort2flux(ib_handle* h, double* gam, double* psi, double* q, double* q1, double* rings) {
+template <typename S>
+cudaError_t vort2flux(ib_handle* h, S* gam, S* psi, S* q, S* q1, S* rings) {
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t nG = g.nG;
-  for (int l = 1; l < L; ++l) CE(coarsify<double>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
+  for (int l = 1; l < L; ++l) CE(coarsify<S>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
   CE(solve(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, op_lap(h), nullptr));
-  if (q) CE(curl<double>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
-  else if (L == 1) CE(curl<double>(g, psi, nullptr, q1, 1, h->stream));
+  if (q) CE(curl<S>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
+  else if (L == 1) CE(curl<S>(g, psi, nullptr, q1, 1, h->stream));
   for (int l = L - 2; l >= 0; --l) {
-    double* ring = rings + (int64_t)l * g.nbc;
-    CE(get_bc<double>(g, psi + (l + 1) * nG, ring, 1, 1.0, h->stream));
+    S* ring = rings + (int64_t)l * g.nbc;
+    CE(get_bc<S>(g, psi + (l + 1) * nG, ring, 1, S(1.0), h->stream));
     CE(solve(h, gam + l * nG, psi + l * nG, 1, ring, op_lap(h), nullptr));
-    if (q) CE(curl<double>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
-    else if (l == 0) CE(curl<double>(g, psi, ring, q1, 1, h->stream));
+    if (q) CE(curl<S>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
+    else if (l == 0) CE(curl<S>(g, psi, ring, q1, 1, h->stream));
   }
   return cudaSuccess;
 }
@@ -267,51 +291,104 @@ __global__ void k_hist_append(const double* __restrict__ cdcl, double* __restric
   if (threadIdx.x == 0) *counter = *counter + 1;
 }
 
+// state conversions of the mixed mode: in place double -> df64, and df64 -> double
+__global__ void k_to_df64(double* p, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double v = p[t];
+    reinterpret_cast<df64*>(p)[t] = df64(v);
+  }
+}
+__global__ void k_from_df64(const df64* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    out[t] = static_cast<double>(in[t]);
+}
+int conv_blocks(int64_t n) {
+  const int64_t b = (n + 255) / 256;
+  return (int)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
 // Enqueue one advance! for buffer parity p (see the file header).
-cudaError_t enqueue_step(ib_handle* h, int p) {
+// d. trial state (GetTrialState, timestepping.jl:28-79): Gamma_s into the other Gamma buffer,
+// psi on every level and the trial flux on level 1 (the only level the step reads)
+template <typename S>
+cudaError_t enqueue_trial(ib_handle* h, int p) {
   const Geometry& g = h->g;
   const int L = g.nlev;
-  const int64_t nG = g.nG;
   cudaStream_t s = h->stream;
-  double* gam = h->G[p];
-  double* gs = h->G[p ^ 1];
-  double* nl_new = h->N[p];
-  double* nl_old = h->N[p ^ 1];
-  // d. trial state (GetTrialState, timestepping.jl:28-79)
-  CE(trial_rings<double>(g, gam, h->bcn, h->edges, h->d_fac, s));
-  NonlinArgs<double> na{};
-  na.q = h->q;
+  S* gam = view<S>(h->G[p]);
+  S* gs = view<S>(h->G[p ^ 1]);
+  CE(trial_rings<S>(g, gam, view<S>(h->bcn), view<S>(h->edges), h->d_fac, s));
+  NonlinArgs<S> na{};
+  na.q = view<S>(h->q);
   na.gamma = gam;
-  na.bcn = h->bcn;
-  na.nl_old = nl_old;
-  na.edges = h->edges;
-  na.nl_new = nl_new;
-  na.rhs = h->rhs;
+  na.bcn = view<S>(h->bcn);
+  na.nl_old = view<S>(h->N[p ^ 1]);
+  na.edges = view<S>(h->edges);
+  na.nl_new = view<S>(h->N[p]);
+  na.rhs = view<S>(h->rhs);
   na.q0 = h->d_q0;
   na.inv_hc2 = h->d_inv_hc2;
   na.alpha = h->d_alpha;
   na.dtb0 = h->dt * h->beta0;
   na.dtb1 = h->dt * h->beta1;
-  CE(nonlin_rhs<double>(g, na, s));
+  CE(nonlin_rhs<S>(g, na, s));
   // Gamma_s[l] = Ainv_l rhs[l] for every level in one batched solve
-  CE(solve(h, h->rhs, gs, L, nullptr, op_cn_all(h), nullptr));
-  // trial Vort2Flux: psi on every level, flux on level 1 only (the only one read)
-  CE(vort2flux(h, gs, h->psi, nullptr, h->qs1, h->rings));
+  CE(solve(h, view<S>(h->rhs), gs, L, nullptr, op_cn_all(h), nullptr));
+  return vort2flux<S>(h, gs, view<S>(h->psi), nullptr, view<S>(h->qs1), view<S>(h->rings));
+}
+
+// f. update_stress! (states.jl:53-84) and the device C_D / C_L history
+cudaError_t enqueue_stress(ib_handle* h) {
+  cudaStream_t s = h->stream;
+  CE(update_stress_hd(h->fb, h->nb, h->nbodies, h->body_start, h->ds, h->g.h, h->dt, h->cdcl, h->stress, s));
+  k_hist_append<<<1, 64, 0, s>>>(h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies, h->d_counter);
+  return cudaGetLastError();
+}
+
+// g. CircProjecter (timestepping.jl:156-171): Gamma_1 = Gamma_s1 - Ainv_1 C^T E^T Fb, then
+// h. Vort2Flux on the new state (timestepping.jl:285); the trial buffer becomes Gamma
+template <typename S>
+cudaError_t enqueue_project(ib_handle* h, int p) {
+  const Geometry& g = h->g;
+  S* gs = view<S>(h->G[p ^ 1]);
+  if (h->nb > 0) {
+    CE(reg_scatter_rot<S>(g, h->fb, h->body_idx, h->weight, h->nb, view<S>(h->qtmp), view<S>(h->gtmp), 1, h->nf,
+                          h->status + 1, h->stream));
+    CE(solve(h, view<S>(h->gtmp), gs, 1, nullptr, op_cn1(h), gs));
+  }
+  return vort2flux<S>(h, gs, view<S>(h->psi), view<S>(h->q), nullptr, view<S>(h->rings));
+}
+
+// Enqueue one advance! for bodies fixed in the grid (buffer parity p, see the file header).
+template <typename S>
+cudaError_t enqueue_step(ib_handle* h, int p) {
+  CE(enqueue_trial<S>(h, p));
   if (h->nb > 0) {
     // e. BoundaryForcer{RigidBody{GridFrame}} (timestepping.jl:106-120)
-    CE(reg_gather<double>(g, h->qs1, h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, g.nq, h->nf, s));
-    CE(gemv_rowmajor(h->binv_rm, h->ftmp, h->fb, h->nf, s));
-    // f. update_stress! (states.jl:53-84)
-    CE(update_stress_hd(h->fb, h->nb, h->nbodies, h->body_start, h->ds, g.h, h->dt, h->cdcl, h->stress, s));
-    k_hist_append<<<1, 64, 0, s>>>(h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies, h->d_counter);
-    CE(cudaGetLastError());
-    // g. CircProjecter (timestepping.jl:156-171): Gamma_1 = Gamma_s1 - Ainv_1 C^T E^T Fb
-    CE(reg_scatter_rot<double>(g, h->fb, h->body_idx, h->weight, h->nb, h->qtmp, h->gtmp, 1, h->nf, h->status + 1, s));
-    CE(solve(h, h->gtmp, gs, 1, nullptr, op_cn1(h), gs));
+    CE(reg_gather<S>(h->g, view<S>(h->qs1), h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, h->g.nq, h->nf,
+                     h->stream));
+    CE(gemv_rowmajor(h->binv_rm, h->ftmp, h->fb, h->nf, h->stream));
+    CE(enqueue_stress(h));
   }
-  // h. Vort2Flux on the new state (timestepping.jl:285): gs is the new Gamma
-  CE(vort2flux(h, gs, h->psi, h->q, nullptr, h->rings));
-  return cudaSuccess;
+  return enqueue_project<S>(h, p);
+}
+
+cudaError_t enqueue_step_mode(ib_handle* h, int p) {
+  return h->precision == IB_PREC_MIXED ? enqueue_step<df64>(h, p) : enqueue_step<double>(h, p);
+}
+
+// B z for the current weights (B_Times, cnab/ops.jl:125-143): E q1(Vort2Flux(Ainv_1 C^T E^T z)).
+template <typename S>
+cudaError_t schur_apply(ib_handle* h, const double* z, double* out) {
+  const Geometry& g = h->g;
+  cudaStream_t s = h->stream;
+  S* Gw = view<S>(h->Gw);
+  CE(reg_scatter_rot<S>(g, z, h->body_idx, h->weight, h->nb, view<S>(h->qtmp), view<S>(h->gtmp), 1, h->nf,
+                        h->status + 1, s));
+  CE(solve(h, view<S>(h->gtmp), Gw, 1, nullptr, op_cn1(h), nullptr));
+  if (g.nlev > 1) CE(cudaMemsetAsync(Gw + g.nG, 0, sizeof(S) * (g.nlev - 1) * g.nG, s));
+  CE(vort2flux<S>(h, Gw, view<S>(h->Pw), nullptr, view<S>(h->qw), view<S>(h->rings_w)));
+  return reg_gather<S>(g, view<S>(h->qw), nullptr, h->body_idx, h->weight, h->nb, out, 1, g.nq, h->nf, s);
 }
 
 int check_status(ib_handle* h) {
@@ -418,8 +495,9 @@ int prime_kernels(ib_handle* h) {
   CK(poisson64(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w1));
   CK(poisson64(h, h->w2, h->w2, 1, nullptr, op_lap(h), h->w2, h->w1));
   if (h->precision == IB_PREC_MIXED) {
-    CK(poisson_mixed(h, h->w2, h->w2, 1, h->rings, op_lap(h), nullptr, h->w32, h->x032, h->x132));
-    CK(poisson_mixed(h, h->w2, h->w2, 1, nullptr, op_cn1(h), h->w2, h->w32, h->x032, h->x132));
+    df64* w2 = view<df64>(h->w2);
+    CK(poisson_mixed(h, w2, w2, 1, view<df64>(h->rings), op_lap(h), nullptr, h->w32, h->x032, h->x132));
+    CK(poisson_mixed(h, w2, w2, 1, nullptr, op_cn1(h), w2, h->w32, h->x032, h->x132));
   }
   CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
@@ -432,7 +510,7 @@ int capture_graphs(ib_handle* h) {
     if (h->gexec[p]) { cudaGraphExecDestroy(h->gexec[p]); h->gexec[p] = nullptr; }
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = enqueue_step(h, p);
+    cudaError_t e = enqueue_step_mode(h, p);
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return fail(h, IB_ERR_CUDA, "step capture", e); }
     if (e2 != cudaSuccess) return fail(h, IB_ERR_CUDA, "step capture", e2);
@@ -462,6 +540,7 @@ void destroy_handle(ib_handle* h) {
     if (ge) cudaGraphExecDestroy(ge);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_q0) cudaFreeHost(h->h_q0);
+  if (h->h_sc) cudaFreeHost(h->h_sc);
   h->axx.release();
   h->axy.release();
   h->axx32.release();
@@ -470,13 +549,14 @@ void destroy_handle(ib_handle* h) {
   delete h;
 }
 
-int stage_q0(ib_handle* h, double u, double v) {
+int stage_q0(ib_handle* h, double u, double v, const double* kin = nullptr) {
   const int L = h->g.nlev;
+  const int slot_len = 2 * L + 6 * h->nbodies;
   if (h->q0_slot >= kQ0Slots) {
     CK(cudaStreamSynchronize(h->stream));
     h->q0_slot = 0;
   }
-  double* slot = h->h_q0 + (size_t)h->q0_slot * 2 * L;
+  double* slot = h->h_q0 + (size_t)h->q0_slot * slot_len;
   h->q0_slot++;
   for (int l = 0; l < L; ++l) {
     const double hc = h->g.h * std::ldexp(1.0, l);  // gridstep(grid, lev), fluids.jl:102
@@ -484,16 +564,102 @@ int stage_q0(ib_handle* h, double u, double v) {
     slot[2 * l + 1] = v * hc;
   }
   CK(cudaMemcpyAsync(h->d_q0, slot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, h->stream));
+  if (kin && h->motion == IB_MOTION_PRESCRIBED) {
+    std::memcpy(slot + 2 * L, kin, sizeof(double) * 6 * h->nbodies);
+    CK(cudaMemcpyAsync(h->d_kin, slot + 2 * L, sizeof(double) * 6 * h->nbodies, cudaMemcpyHostToDevice, h->stream));
+  }
   return IB_OK;
 }
 
+// Conjugate gradients for B Fb = ftmp (cg!(qty.Fb, B, ftmp), cnab/ops.jl:104-114), warm-started
+// from h->fb, stopping when ||r|| <= tol ||ftmp||.  The residual norm is read back each iteration.
+// The CG vectors are FP64 in both modes; S is the state type of the B products.
+template <typename S>
+int cg_solve(ib_handle* h) {
+  const int nf = h->nf;
+  cudaStream_t s = h->stream;
+  double *x = h->fb, *r = h->cg_r, *p = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
+  CK(schur_apply<S>(h, x, Ap));
+  CK(cudaMemcpyAsync(r, h->ftmp, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+  CK(vec_axpy(r, Ap, -1.0, nf, s));
+  CK(vec_dot(r, r, nf, sc + 0, s));
+  CK(vec_dot(h->ftmp, h->ftmp, nf, sc + 3, s));
+  CK(cudaMemcpyAsync(p, r, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->h_sc, sc, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const double target = h->cg_tol * std::sqrt(h->h_sc[3]);
+  double rn = std::sqrt(h->h_sc[0]);
+  if (!std::isfinite(rn)) return fail(h, IB_ERR_NONFINITE, "infinite flux");
+  int it = 0;
+  bool conv = rn <= target;
+  while (!conv && it < h->cg_maxiter) {
+    ++it;
+    CK(schur_apply<S>(h, p, Ap));
+    CK(vec_dot(p, Ap, nf, sc + 1, s));
+    CK(cg_update_xr(x, r, p, Ap, sc, nf, s));
+    CK(vec_dot(r, r, nf, sc + 2, s));
+    CK(cudaMemcpyAsync(h->h_sc + 2, sc + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    rn = std::sqrt(h->h_sc[2]);
+    if (!std::isfinite(rn)) return fail(h, IB_ERR_NONFINITE, "infinite flux");
+    conv = rn <= target;
+    if (!conv) CK(cg_update_p(p, r, sc, nf, s));
+  }
+  h->cg_iters.push_back(it);
+  h->cg_res.push_back(h->h_sc[3] > 0 ? rn / std::sqrt(h->h_sc[3]) : rn);
+  if (!conv) return fail(h, IB_ERR_CG_MAXITER, "Schur CG reached its iteration cap");
+  return IB_OK;
+}
+
+// advance! for rigidly moving bodies (corrected reference branch): points and weights from the
+// step's kinematics, the trial state, Fb by CG, stress, projection and Vort2Flux.
+template <typename S>
+int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
+  const Geometry& g = h->g;
+  cudaStream_t s = h->stream;
+  const int p = h->parity;
+  int rc = stage_q0(h, u, v, kin);
+  if (rc != IB_OK) return rc;
+  // a/b. update_bodies! and update!(reg, points)
+  CK(body_points(h->xb_body, h->d_kin, h->body_of, h->nb, h->xb, h->vb, s));
+  CK(reg_update(g, h->xb, h->nb, h->body_idx, h->weight, h->status, s));
+  CK(enqueue_trial<S>(h, p));
+  // e. BoundaryForcer for moving bodies (timestepping.jl:122-139): ftmp = E(qs + q0) - ub h
+  CK(reg_gather<S>(g, view<S>(h->qs1), h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, g.nq, h->nf, s));
+  CK(vec_axpy(h->ftmp, h->vb, -g.h, h->nf, s));
+  rc = check_status(h);
+  if (rc != IB_OK) return rc;
+  // warm start: the previous Fb (the reference's cg! on qty.Fb) or its linear extrapolation
+  if (h->warm_start == IB_WARM_EXTRAPOLATE && h->steps >= 2) {
+    CK(cudaMemcpyAsync(h->cg_p, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
+    CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
+    CK(cudaMemcpyAsync(h->fb_prev, h->cg_p, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
+  } else {
+    CK(cudaMemcpyAsync(h->fb_prev, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
+    if (h->warm_start == IB_WARM_ZERO) CK(cudaMemsetAsync(h->fb, 0, sizeof(double) * h->nf, s));
+  }
+  rc = cg_solve<S>(h);
+  if (rc != IB_OK) return rc;
+  CK(enqueue_stress(h));
+  CK(enqueue_project<S>(h, p));
+  h->parity ^= 1;
+  h->steps++;
+  h->t = t;
+  return check_status(h);
+}
+
+int moving_step_mode(ib_handle* h, double t, double u, double v, const double* kin) {
+  return h->precision == IB_PREC_MIXED ? moving_step<df64>(h, t, u, v, kin) : moving_step<double>(h, t, u, v, kin);
+}
+
 int one_step(ib_handle* h, double t, double u, double v) {
+  if (h->motion == IB_MOTION_PRESCRIBED) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics (ib_advance_kin)");
   int rc = stage_q0(h, u, v);
   if (rc != IB_OK) return rc;
   if (h->use_graph) {
     CK(cudaGraphLaunch(h->gexec[h->parity], h->stream));
   } else {
-    CK(enqueue_step(h, h->parity));
+    CK(enqueue_step_mode(h, h->parity));
   }
   h->parity ^= 1;
   h->steps++;
@@ -553,7 +719,8 @@ int ib_create(const ib_problem* p, ib_handle** out) {
                 "nx and ny must be multiples of 4, at most 2048, with n/2 a product of 2, 3 and 5");
   if (p->precision != IB_PREC_FP64 && p->precision != IB_PREC_MIXED)
     return fail(nullptr, IB_ERR_UNSUPPORTED, "precision mode not available");
-  if (p->motion != IB_MOTION_STATIC) return fail(nullptr, IB_ERR_UNSUPPORTED, "moving bodies not available");
+  if (p->motion != IB_MOTION_STATIC && p->motion != IB_MOTION_PRESCRIBED)
+    return fail(nullptr, IB_ERR_INVALID, "unknown body motion");
   int nb = 0;
   if (p->nbodies < 0) return fail(nullptr, IB_ERR_INVALID, "negative body count");
   for (int b = 0; b < p->nbodies; ++b) {
@@ -584,6 +751,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   h->nb = nb;
   h->nf = 2 * nb;
   h->precision = p->precision;
+  h->motion = p->motion;
   h->hist_cap = p->history_capacity > 0 ? p->history_capacity : 4096;
   if (p->refine_sweeps < 0 || p->refine_sweeps > 2) return bail(fail(h, IB_ERR_INVALID, "refine_sweeps must be 0, 1 or 2"));
   h->refine = p->refine_sweeps > 0 ? p->refine_sweeps : 2;
@@ -617,12 +785,13 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     AL(h->mLap32, nG); AL(h->mCN1_32, L * nG);
     AL(h->w32, L * nG); AL(h->x032, L * nG);
     if (h->refine >= 2) AL(h->x132, L * nG);
+    AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
   }
   AL(h->status, 4); AL(h->d_counter, 1);
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->hist, (int64_t)h->hist_cap * 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->stress, h->nf);
-  if ((e = cudaMallocHost(&h->h_q0, sizeof(double) * kQ0Slots * 2 * L)) != cudaSuccess) {
+  if ((e = cudaMallocHost(&h->h_q0, sizeof(double) * kQ0Slots * (2 * L + 6 * (h->nbodies + 1)))) != cudaSuccess) {
     h->h_q0 = nullptr;
     return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
   }
@@ -654,32 +823,52 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     }
   }
   if (nb > 0) {
+    const bool moving = h->motion == IB_MOTION_PRESCRIBED;
     AL(h->xb, 2 * nb); AL(h->ds, nb); AL(h->weight, (int64_t)nb * 2 * kWin2);
-    AL(h->body_idx, 2 * nb); AL(h->body_start, h->nbodies + 1);
-    AL(h->bmat, (int64_t)h->nf * h->nf); AL(h->binv_cm, (int64_t)h->nf * h->nf);
-    AL(h->binv_rm, (int64_t)h->nf * h->nf); AL(h->ftmp, h->nf);
-    std::vector<int> bs(h->nbodies + 1, 0);
-    for (int b = 0; b < h->nbodies; ++b) bs[b + 1] = bs[b] + p->body_npoints[b];
-    if ((e = cudaMemcpy(h->xb, p->xb, sizeof(double) * 2 * nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+    AL(h->body_idx, 2 * nb); AL(h->body_start, h->nbodies + 1); AL(h->ftmp, h->nf);
+    if (!moving) {
+      AL(h->bmat, (int64_t)h->nf * h->nf); AL(h->binv_cm, (int64_t)h->nf * h->nf);
+      AL(h->binv_rm, (int64_t)h->nf * h->nf);
+    } else {
+      AL(h->xb_body, 2 * nb); AL(h->vb, 2 * nb); AL(h->d_kin, 6 * h->nbodies); AL(h->body_of, nb);
+      AL(h->cg_r, h->nf); AL(h->cg_p, h->nf); AL(h->cg_Ap, h->nf); AL(h->cg_sc, 4); AL(h->fb_prev, h->nf);
+      AL(h->Gw, L * nG); AL(h->Pw, L * nG); AL(h->qw, g.nq); AL(h->rings_w, (int64_t)L * g.nbc);
+      if ((e = cudaMallocHost(&h->h_sc, sizeof(double) * 4)) != cudaSuccess) {
+        h->h_sc = nullptr;
+        return bail(fail(h, IB_ERR_CUDA, "pinned CG scalars", e));
+      }
+    }
+    std::vector<int> bs(h->nbodies + 1, 0), bof(nb);
+    for (int b = 0; b < h->nbodies; ++b) {
+      bs[b + 1] = bs[b] + p->body_npoints[b];
+      for (int k = bs[b]; k < bs[b + 1]; ++k) bof[k] = b;
+    }
+    if ((e = cudaMemcpy(moving ? h->xb_body : h->xb, p->xb, sizeof(double) * 2 * nb, cudaMemcpyHostToDevice)) !=
+            cudaSuccess ||
         (e = cudaMemcpy(h->ds, p->ds, sizeof(double) * nb, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->body_start, bs.data(), sizeof(int) * bs.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "body upload", e));
-    if ((e = reg_update(g, h->xb, nb, h->body_idx, h->weight, h->status, h->stream)) != cudaSuccess)
-      return bail(fail(h, IB_ERR_CUDA, "delta weights", e));
-    int rc = check_status(h);
-    if (rc != IB_OK) return bail(rc);
+    if (moving && (e = cudaMemcpy(h->body_of, bof.data(), sizeof(int) * nb, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "body upload", e));
+    if (!moving) {
+      if ((e = reg_update(g, h->xb, nb, h->body_idx, h->weight, h->status, h->stream)) != cudaSuccess)
+        return bail(fail(h, IB_ERR_CUDA, "delta weights", e));
+      int rc = check_status(h);
+      if (rc != IB_OK) return bail(rc);
+    }
   }
 #undef AL
   {
     int rc = prime_kernels(h);
     if (rc != IB_OK) return bail(rc);
   }
-  if (nb > 0) {
+  if (nb > 0 && h->motion == IB_MOTION_STATIC) {
     int rc = assemble_schur(h);
     if (rc != IB_OK) return bail(rc);
     rc = check_status(h);
     if (rc != IB_OK) return bail(rc);
   }
+  if (h->motion == IB_MOTION_PRESCRIBED) h->use_graph = false;
   if (h->use_graph) {
     int rc = capture_graphs(h);
     if (rc != IB_OK) return bail(rc);
@@ -710,6 +899,16 @@ int ib_set_state(ib_handle* h, const double* gamma, const double* q, const doubl
   if (nonlin1) CK(cudaMemcpyAsync(h->N[p], nonlin1, nGL, cudaMemcpyHostToDevice, s));
   if (nonlin2) CK(cudaMemcpyAsync(h->N[p ^ 1], nonlin2, nGL, cudaMemcpyHostToDevice, s));
   if (fb && h->nf) CK(cudaMemcpyAsync(h->fb, fb, sizeof(double) * h->nf, cudaMemcpyHostToDevice, s));
+  if (h->precision == IB_PREC_MIXED) {
+    // the mixed mode keeps its state as float-float pairs: convert in place
+    const int64_t nG = (int64_t)g.nlev * g.nG, nq = (int64_t)g.nlev * g.nq;
+    if (gamma) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->G[p], nG);
+    if (q) k_to_df64<<<conv_blocks(nq), 256, 0, s>>>(h->q, nq);
+    if (psi) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->psi, nG);
+    if (nonlin1) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->N[p], nG);
+    if (nonlin2) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->N[p ^ 1], nG);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(s));
   h->t = t;
   return IB_OK;
@@ -723,11 +922,22 @@ int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* no
   const size_t nGL = sizeof(double) * g.nlev * g.nG, nqL = sizeof(double) * g.nlev * g.nq;
   const int p = h->parity;
   cudaStream_t s = h->stream;
-  if (gamma) CK(cudaMemcpyAsync(gamma, h->G[p], nGL, cudaMemcpyDeviceToHost, s));
-  if (q) CK(cudaMemcpyAsync(q, h->q, nqL, cudaMemcpyDeviceToHost, s));
-  if (psi) CK(cudaMemcpyAsync(psi, h->psi, nGL, cudaMemcpyDeviceToHost, s));
-  if (nonlin1) CK(cudaMemcpyAsync(nonlin1, h->N[p], nGL, cudaMemcpyDeviceToHost, s));
-  if (nonlin2) CK(cudaMemcpyAsync(nonlin2, h->N[p ^ 1], nGL, cudaMemcpyDeviceToHost, s));
+  // mixed mode: each float-float array is widened into the conversion buffer, then copied
+  auto pull = [&](double* dst, double* src, size_t bytes) -> cudaError_t {
+    if (h->precision != IB_PREC_MIXED) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+    const int64_t n = (int64_t)(bytes / sizeof(double));
+    k_from_df64<<<conv_blocks(n), 256, 0, s>>>(view<df64>(src), h->conv, n);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(dst, h->conv, bytes, cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);  // the buffer is reused by the next array
+  };
+  if (gamma) CK(pull(gamma, h->G[p], nGL));
+  if (q) CK(pull(q, h->q, nqL));
+  if (psi) CK(pull(psi, h->psi, nGL));
+  if (nonlin1) CK(pull(nonlin1, h->N[p], nGL));
+  if (nonlin2) CK(pull(nonlin2, h->N[p ^ 1], nGL));
   if (fb && h->nf) CK(cudaMemcpyAsync(fb, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (t) *t = h->t;
@@ -752,10 +962,69 @@ int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv) {
   return check_status(h);
 }
 
+int ib_advance_kin(ib_handle* h, double t, double u, double v, const double* kin) {
+  if (!h) return IB_ERR_INVALID;
+  if (h->motion != IB_MOTION_PRESCRIBED) {
+    if (kin) return fail(h, IB_ERR_INVALID, "kinematics given for bodies fixed in the grid");
+    return ib_advance(h, t, u, v);
+  }
+  if (!kin) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics");
+  CK(cudaSetDevice(h->device));
+  return moving_step_mode(h, t, u, v, kin);
+}
+
+int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv, const double* kin) {
+  if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
+  if (h->motion != IB_MOTION_PRESCRIBED) return ib_advance_n(h, n, t, uv);
+  if (n > 0 && !kin) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics");
+  CK(cudaSetDevice(h->device));
+  for (int i = 0; i < n; ++i) {
+    int rc = moving_step_mode(h, t[i], uv[2 * i], uv[2 * i + 1], kin + (size_t)i * 6 * h->nbodies);
+    if (rc != IB_OK) return rc;
+  }
+  return IB_OK;
+}
+
+int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_start) {
+  if (!h || !(tol > 0) || maxiter < 1 || warm_start < IB_WARM_PREVIOUS || warm_start > IB_WARM_ZERO)
+    return IB_ERR_INVALID;
+  h->cg_tol = tol;
+  h->cg_maxiter = maxiter;
+  h->warm_start = warm_start;
+  return IB_OK;
+}
+
+int ib_get_cg_stats(ib_handle* h, int32_t count, int32_t* iterations, double* residuals) {
+  if (!h || count < 0 || count > (int32_t)h->cg_iters.size()) return IB_ERR_INVALID;
+  const size_t off = h->cg_iters.size() - (size_t)count;
+  for (int i = 0; i < count; ++i) {
+    if (iterations) iterations[i] = h->cg_iters[off + i];
+    if (residuals) residuals[i] = h->cg_res[off + i];
+  }
+  return IB_OK;
+}
+
+int ib_get_body_points(ib_handle* h, double* xb, double* vb) {
+  if (!h) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  if (h->nb == 0) return IB_OK;
+  if (xb) CK(cudaMemcpyAsync(xb, h->xb, sizeof(double) * 2 * h->nb, cudaMemcpyDeviceToHost, h->stream));
+  if (vb) {
+    if (h->vb) CK(cudaMemcpyAsync(vb, h->vb, sizeof(double) * 2 * h->nb, cudaMemcpyDeviceToHost, h->stream));
+    else std::memset(vb, 0, sizeof(double) * 2 * h->nb);
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  return IB_OK;
+}
+
 int ib_vort2flux(ib_handle* h) {
   if (!h) return IB_ERR_INVALID;
   CK(cudaSetDevice(h->device));
-  CK(vort2flux(h, h->G[h->parity], h->psi, h->q, nullptr, h->rings));
+  if (h->precision == IB_PREC_MIXED)
+    CK(vort2flux<df64>(h, view<df64>(h->G[h->parity]), view<df64>(h->psi), view<df64>(h->q), nullptr,
+                       view<df64>(h->rings)));
+  else
+    CK(vort2flux<double>(h, h->G[h->parity], h->psi, h->q, nullptr, h->rings));
   CK(cudaStreamSynchronize(h->stream));
   return IB_OK;
 }
@@ -1017,7 +1286,7 @@ int ib_op_vort2flux(ib_handle* h, double* gamma, double* psi, double* q) {
   OP_BEGIN();
   double* rings;
   CK(cudaMalloc(&rings, sizeof(double) * g.nlev * g.nbc));
-  cudaError_t e = vort2flux(h, gamma, psi, q, nullptr, rings);
+  cudaError_t e = vort2flux<double>(h, gamma, psi, q, nullptr, rings);
   cudaStreamSynchronize(s);
   cudaFree(rings);
   CK(e);
@@ -1051,6 +1320,7 @@ int ib_get_schur(ib_handle* h, double* bmat, double* binv) {
   OP_BEGIN();
   const size_t bytes = sizeof(double) * (size_t)h->nf * h->nf;
   if (h->nf == 0) return IB_OK;
+  if (!h->bmat) return fail(h, IB_ERR_INVALID, "no assembled Schur matrix for moving bodies");
   if (bmat) CK(cudaMemcpyAsync(bmat, h->bmat, bytes, cudaMemcpyDeviceToHost, s));
   if (binv) CK(cudaMemcpyAsync(binv, h->binv_cm, bytes, cudaMemcpyDeviceToHost, s));
   OP_END();

@@ -53,9 +53,7 @@ __global__ void k_get_bc(Geometry g, const T* __restrict__ r, T* __restrict__ bc
   const int64_t total = (int64_t)batch * g.nbc;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(t / g.nbc), idx = (int)(t - (int64_t)b * g.nbc);
-    T v = ring_value(g, r + (int64_t)b * g.nG, idx);
-    if (extra != T(1)) v *= extra;
-    bc[t] = v;
+    bc[t] = ring_value(g, r + (int64_t)b * g.nG, idx) * extra;
   }
 }
 
@@ -162,10 +160,10 @@ struct LevelView {
   int nx, ny, ncol;
   // avg_flux!: Qx at (Jq in 1..ny-1, Iq in 0..nx), Qy at (Jq in 0..ny, Iq in 1..nx-1)
   __device__ __forceinline__ T Qx(int Jq, int Iq) const {
-    return (((qx[Jq * (nx + 1) + Iq] + qx[(Jq - 1) * (nx + 1) + Iq]) + q0x) + q0x) / T(2);
+    return (((qx[Jq * (nx + 1) + Iq] + qx[(Jq - 1) * (nx + 1) + Iq]) + q0x) + q0x) * T(0.5);
   }
   __device__ __forceinline__ T Qy(int Jq, int Iq) const {
-    return (((qy[Jq * nx + Iq] + qy[Jq * nx + Iq - 1]) + q0y) + q0y) / T(2);
+    return (((qy[Jq * nx + Iq] + qy[Jq * nx + Iq - 1]) + q0y) + q0y) * T(0.5);
   }
   __device__ __forceinline__ T Gm(int J, int I) const { return G[J * ncol + I]; }
 };
@@ -173,16 +171,16 @@ struct LevelView {
 // fqx at (Jf, If), If in 1..nx-1 (direct_product_loops!, fluid-ops.jl:329-362)
 template <typename T>
 __device__ __forceinline__ T fqx_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qyHi, T qyLo) {
-  if (Jf == 0) return (qyHi * v.Gm(0, If - 1) + qyLo * v.bc[g.B + If]) / T(2);
-  if (Jf == v.ny - 1) return (qyLo * v.Gm(v.ny - 2, If - 1) + qyHi * v.bc[g.T + If]) / T(2);
-  return (qyHi * v.Gm(Jf, If - 1) + qyLo * v.Gm(Jf - 1, If - 1)) / T(2);
+  if (Jf == 0) return (qyHi * v.Gm(0, If - 1) + qyLo * v.bc[g.B + If]) * T(0.5);
+  if (Jf == v.ny - 1) return (qyLo * v.Gm(v.ny - 2, If - 1) + qyHi * v.bc[g.T + If]) * T(0.5);
+  return (qyHi * v.Gm(Jf, If - 1) + qyLo * v.Gm(Jf - 1, If - 1)) * T(0.5);
 }
 // fqy at (Jf, If), Jf in 1..ny-1 (fluid-ops.jl:365-398); qxHi = Qx(Jf, If+1), qxLo = Qx(Jf, If)
 template <typename T>
 __device__ __forceinline__ T fqy_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qxHi, T qxLo) {
-  if (If == 0) return -(qxHi * v.Gm(Jf - 1, 0) + qxLo * v.bc[g.L + Jf]) / T(2);
-  if (If == v.nx - 1) return -(qxLo * v.Gm(Jf - 1, v.nx - 2) + qxHi * v.bc[g.R + Jf]) / T(2);
-  return -(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1)) / T(2);
+  if (If == 0) return -(qxHi * v.Gm(Jf - 1, 0) + qxLo * v.bc[g.L + Jf]) * T(0.5);
+  if (If == v.nx - 1) return -(qxLo * v.Gm(Jf - 1, v.nx - 2) + qxHi * v.bc[g.R + Jf]) * T(0.5);
+  return -(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1)) * T(0.5);
 }
 
 template <typename T>
@@ -334,7 +332,7 @@ cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s) {
   template cudaError_t fill<T>(T*, T, int64_t, cudaStream_t);                                        \
   template cudaError_t axpby<T>(T*, const T*, T, T, int64_t, cudaStream_t);
 IB_INST(double)
-IB_INST(float)
+IB_INST(df64)
 #undef IB_INST
 
 }  // namespace ib

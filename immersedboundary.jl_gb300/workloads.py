@@ -10,6 +10,9 @@ seeded initial vorticity noise (NumPy PCG64), identical for the GPU path and the
                        Re=200, dt=0.001
 * ``four_cylinders``   2048x2048, h=0.0025, 5 levels, four cylinders D=0.5 on a 2x2 lattice of
                        spacing 1.5 (629 points each), Re=150, dt=0.0005
+* ``heaving_plate``    768x512, h=0.005, 4 levels, flat plate chord 1 (201 points) heaving
+                       y = 0.5 sin(2 pi f t) and pitching 30 deg sin(2 pi f t + pi/2) about its
+                       quarter chord, f = 0.2, Re=1000, dt=0.001
 * ``scaled(...)``      the same bodies on coarser grids, for tests
 """
 from __future__ import annotations
@@ -19,8 +22,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .api import (BodyGroup, GridFrame, MultiLevel, Problem, RigidBody, SchemeCNAB, StreamFcnFluid,
-                  UniformGrid)
+from .api import (BodyGroup, GridFrame, MultiLevel, Problem, RelativeFrame, RigidBody, SchemeCNAB,
+                  StreamFcnFluid, UniformGrid)
 
 NOISE = 1e-4
 
@@ -100,6 +103,30 @@ def four_cylinders(nsteps: int = 2000, seed: int = 0) -> Workload:
                     seed=seed)
 
 
+def heave_pitch_frame(f: float = 0.2, heave: float = 0.5, pitch_deg: float = 30.0) -> RelativeFrame:
+    """RelativeFrame of a plate heaving y = A sin(2 pi f t) and pitching about the frame origin
+    theta = P sin(2 pi f t + pi/2)."""
+    w = 2 * math.pi * f
+    p = math.radians(pitch_deg)
+    return RelativeFrame(GridFrame(),
+                         r=lambda t: (0.0, heave * math.sin(w * t)),
+                         v=lambda t: (0.0, heave * w * math.cos(w * t)),
+                         theta=lambda t: p * math.sin(w * t + math.pi / 2),
+                         omega=lambda t: p * w * math.cos(w * t + math.pi / 2))
+
+
+def moving_plate(n: int, chord: float = 1.0, frame=None) -> RigidBody:
+    """Body-frame plate of n points with the pitch axis (frame origin) at the quarter chord."""
+    s = np.linspace(-0.25 * chord, 0.75 * chord, n)
+    xb = np.stack([s, np.zeros(n)], axis=1)
+    return RigidBody(frame or heave_pitch_frame(), xb, np.full(n, chord / (n - 1)))
+
+
+def heaving_plate(nsteps: int = 4000, f: float = 0.2, seed: int = 0) -> Workload:
+    return Workload("heaving_plate", 0.005, (-1.0, 2.84), (-1.28, 1.28), 4, 1000.0, 0.001, nsteps,
+                    [moving_plate(201, frame=heave_pitch_frame(f))], seed=seed)
+
+
 def scaled(base: Workload, nx: int, ny: int | None = None, nlevels: int | None = None,
            nsteps: int | None = None) -> Workload:
     """The same domain and bodies on an nx x ny finest grid (body points re-spaced to ~h)."""
@@ -119,6 +146,6 @@ def scaled(base: Workload, nx: int, ny: int | None = None, nlevels: int | None =
                       np.append(xb[:, 0], xb[0, 0]) if closed else xb[:, 0])
         y = np.interp(idx, np.arange(xb.shape[0] + (1 if closed else 0)),
                       np.append(xb[:, 1], xb[0, 1]) if closed else xb[:, 1])
-        bodies.append(RigidBody(GridFrame(), np.stack([x, y], 1), np.full(n, length / (n if closed else n - 1))))
+        bodies.append(RigidBody(b.frame, np.stack([x, y], 1), np.full(n, length / (n if closed else n - 1))))
     return Workload(f"{base.name}_{nx}x{ny}", h, base.xlims, ylims, nlevels or base.nlevels, base.Re,
                     base.dt * (h / base.h), nsteps or base.nsteps, bodies, base.freestream, base.seed)

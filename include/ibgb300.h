@@ -46,6 +46,13 @@ extern "C" {
 
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */
+#define IB_MOTION_PRESCRIBED 1      /* RigidBody{RelativeFrame}: xb in the body frame, rigid
+                                       kinematics per step, E rebuilt and Fb solved by CG */
+
+/* warm start of the moving-body Schur CG */
+#define IB_WARM_PREVIOUS 0          /* previous step's Fb (cg! on qty.Fb, cnab/ops.jl:110) */
+#define IB_WARM_EXTRAPOLATE 1       /* 2 Fb(n-1) - Fb(n-2) */
+#define IB_WARM_ZERO 2              /* Fb = 0 (cold start, for comparisons) */
 
 typedef struct ib_problem {
   /* MultiLevel(UniformGrid(h, (x0, x1), (y0, y1)), nlevels), src/fluids/fluids.jl:53-95 */
@@ -103,6 +110,29 @@ int ib_vort2flux(ib_handle* h);
  * advance! at t[i] with freestream (uv[2i], uv[2i+1]).  Replays the captured step graph;
  * synchronises once at the end and returns the first error. */
 int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv);
+
+/* advance! for moving bodies (RigidBody{RelativeFrame}; update_bodies!, src/bodies/body-points.jl:
+ * 47-76, and the CG Binv of src/streamfcn/cnab/ops.jl:104-114, with the corrections the
+ * reference's branch needs to run: the Ω field, point velocities, E rebuilt every step).
+ * kin[6b..6b+5] = r0x, r0y, v0x, v0y, θ, Ω of body b at t (the frame's r, v, θ, Ω closures,
+ * src/dynamics.jl:23-29, evaluated by the caller; bodies fixed in the grid pass zeros).
+ * Fb solves B Fb = E(qs + q0) - ub h by conjugate gradients to ||r|| <= tol ||rhs||;
+ * IB_ERR_CG_MAXITER if the cap is reached.  For static handles kin must be NULL. */
+int ib_advance_kin(ib_handle* h, double t, double u_inf, double v_inf, const double* kin);
+
+/* n moving-body steps: kin is [n][nbodies][6] */
+int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv, const double* kin);
+
+/* CG options (the reference hard-codes maxiter=5000, cnab/ops.jl:110): tolerance on
+ * ||r|| / ||rhs||, iteration cap and IB_WARM_* warm start.  Defaults 1e-10, 5000, PREVIOUS. */
+int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_start);
+
+/* CG iterations and final relative residuals of the last `count` moving-body steps */
+int ib_get_cg_stats(ib_handle* h, int32_t count, int32_t* iterations, double* residuals);
+
+/* state.qty.points (BodyGroupPoints, src/bodies/body-points.jl:6-10): current positions and
+ * velocities, stacked [x..., y...] */
+int ib_get_body_points(ib_handle* h, double* xb, double* vb);
 
 /* state.qty.stress of the last step (BodyStress, src/streamfcn/states.jl:3-7,53-84):
  * cd[b], cl[b] per body and, if fb_surface != NULL, the surface stress of every body as

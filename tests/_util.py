@@ -59,3 +59,23 @@ class Dev:
     def get(self, t):
         self.torch.cuda.synchronize()
         return t.cpu().numpy()
+
+
+def oracle_moving_problem(O, wl, prob, tol):
+    """The oracle's MovingProblem for a workload whose bodies may move (RelativeFrame)."""
+    import ibgb300 as ib
+    g = O.grid_from_limits(wl.h, wl.xlims, wl.ylims, wl.nlevels)
+    bodies = list(prob.bodies)
+
+    def kin(t):
+        out = []
+        for b in bodies:
+            f = b.frame
+            if isinstance(f, ib.RelativeFrame):
+                out.append((tuple(f.r(t)), tuple(f.v(t)), f.theta(t), f.omega(t)))
+            else:
+                out.append(((0.0, 0.0), (0.0, 0.0), 0.0, 0.0))
+        return out
+    ds = np.concatenate([b.ds for b in bodies])
+    return O.MovingProblem(g, wl.dt, wl.Re, [b.xb for b in bodies], ds, kin, freestream=wl.freestream,
+                           cg_tol=tol)

@@ -1,0 +1,85 @@
+"""Moving bodies (RigidBody{RelativeFrame}): device kinematics, weights rebuilt every step and the
+Schur solve by device CG, against the corrected moving-body oracle.
+
+Both sides run CG to ||r|| <= 1e-13 ||rhs|| so the comparison measures arithmetic rather than
+where each CG stopped (at 1e-10 the two stopping points may differ by ~tol * cond(B))."""
+import numpy as np
+import pytest
+
+from _util import oracle_moving_problem, rel
+
+pytestmark = pytest.mark.gpu
+
+TOL_CG = 1e-13
+
+
+def small_heaving(ib, nx=128, ny=96, L=2, nsteps=8):
+    base = ib.workloads.heaving_plate(nsteps=nsteps)
+    wl = ib.workloads.scaled(base, nx, ny, nlevels=L, nsteps=nsteps)
+    wl.Re = 200.0
+    wl.dt = 0.01
+    return wl
+
+
+@pytest.mark.parametrize("precision,gtol,ctol", [("fp64", 1e-10, 1e-8), ("mixed", 1e-8, 1e-6)])
+def test_moving_plate_parity(ib, O, precision, gtol, ctol):
+    wl = small_heaving(ib)
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = wl.initial_gamma()
+    s = ib.initsolver(prob, st, precision=precision)
+    s.set_cg_options(tol=TOL_CG, maxiter=5000)
+    s.vort2flux(st)
+    op = oracle_moving_problem(O, wl, prob, TOL_CG)
+    g = op.grid
+    ost = O.init_state(op)
+    ost.gamma[0] = wl.initial_gamma()[0].reshape(g.gshape)
+    ost.psi, ost.q = O.vort2flux(ost.gamma, g, O.lap_eigs(g))
+    osol = O.MovingSolver(op)
+    worst_c = 0.0
+    for i in range(wl.nsteps):
+        t = i * wl.dt
+        ib.advance_(st, s, t)
+        osol.advance(ost, t)
+        cd = st.qty.stress[0].CD
+        cl = st.qty.stress[0].CL
+        worst_c = max(worst_c, abs(cd - ost.cd[0]) / max(1, abs(ost.cd[0])),
+                      abs(cl - ost.cl[0]) / max(1, abs(ost.cl[0])))
+    xb, vb = st.qty.points
+    np.testing.assert_allclose(xb, ost.points, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(vb, ost.velocities, rtol=0, atol=1e-14)
+    assert rel(st.qty.gamma, ost.gamma.reshape(g.nlevels, -1)) < gtol
+    assert worst_c < ctol, worst_c
+    it, res = s.cg_stats(wl.nsteps)
+    assert np.all(res <= TOL_CG) and np.all(it > 0)
+    s.close()
+
+
+def test_warm_starts_converge_and_save_iterations(ib):
+    """Every warm start reaches the same residual; starting from the previous Fb (the
+    reference's cg! on qty.Fb) takes fewer iterations than starting from zero."""
+    wl = small_heaving(ib, nsteps=12)
+    counts = {}
+    for mode in ("zero", "previous", "extrapolate"):
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        s = ib.initsolver(prob, st)
+        s.set_cg_options(tol=1e-10, warm_start=mode)
+        ib.solve_(st, prob, (0.0, (wl.nsteps - 1) * wl.dt), solver=s)
+        it, res = s.cg_stats(wl.nsteps)
+        assert np.all(res <= 1e-10)
+        counts[mode] = int(it[4:].sum())
+        s.close()
+    assert counts["previous"] < counts["zero"], counts
+
+
+def test_cg_cap_is_reported(ib):
+    wl = small_heaving(ib, nsteps=1)
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    s = ib.initsolver(prob, st)
+    s.set_cg_options(tol=1e-14, maxiter=3)
+    with pytest.raises(ib.IBError) as e:
+        ib.advance_(st, s, 0.0)
+    assert e.value.status == 6
+    s.close()

@@ -7,7 +7,7 @@ force solve and the projection).  ``value`` is cell-steps/s (cells = nlevels * n
 step) over all ranks with the state resident on the device; ``e2e`` is the same metric
 through the public ``solve`` API with a per-step host callback reading C_D / C_L.  Under
 torchrun each rank advances an independent replica on its own GPU (the step has no
-data-parallel split; see DESIGN.md).
+data-parallel split).
 
 ``--impl reference`` times the CPU implementation of the same step on this host's cores (the
 FP64 restatement of the reference; Julia is not available) on the same workload.
@@ -29,14 +29,11 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = None  # read from the benchmark spec when present
+METRIC = "cell-steps/s on 1 GB300: learned+mixed vs plain FP64 GPU at C_L/C_D err \u22641e-6"
 
 
 def baseline_metric() -> str:
-    try:
-        return json.loads((ROOT / "BASELINE.json").read_text())["metric"]
-    except Exception:
-        return "cell-steps/s on 1 GB300"
+    return METRIC
 
 
 def dist_env():
@@ -168,7 +165,7 @@ def cpu_reference(ib, wl, nsteps: int, warmup: int):
 
 
 # ----------------------------------------------------------------------------------------------
-# algorithmic bytes / flops of the sine-transform passes (per step), see the design doc
+# algorithmic bytes / flops of the sine-transform passes (per step)
 # ----------------------------------------------------------------------------------------------
 def pass_model(wl, precision: str):
     """Algorithmic DRAM bytes, launches and flops of the x and y passes of one step.

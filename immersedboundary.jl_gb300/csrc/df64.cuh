@@ -60,6 +60,27 @@ __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
   p.lo = fmaf(a.lo, b.hi, p.lo);
   return fast_two_sum(p.hi, p.lo);
 }
+// Dekker's add: error below 2 ulp of max(|a|, |b|) in the float-float sense, i.e. about 2^-46
+// relative to the larger operand (not to the sum); enough wherever the sum's absolute error
+// is what matters.
+__device__ __forceinline__ df64 add_sloppy(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+
+// 4 c - (w + e + s + n) of five floats, to float-float accuracy: the neighbour sum is formed
+// with error-free sums (its three small parts add up in float with an error ~2^-48 of the
+// sum), the difference with the exactly scaled centre with one more error-free sum.
+__device__ __forceinline__ df64 lap5_exact(float c, float w, float e, float s, float n) {
+  const df64 a = two_sum(w, e);
+  const df64 b = two_sum(s, n);
+  const df64 t = two_sum(a.hi, b.hi);
+  const float small = (a.lo + b.lo) + t.lo;
+  const df64 u = two_sum(4.0f * c, -t.hi);
+  return fast_two_sum(u.hi, u.lo - small);
+}
+
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
 __device__ __forceinline__ df64& operator*=(df64& a, df64 b) { return a = a * b; }

@@ -19,6 +19,7 @@
 // F is half of FFTW's RODFT00 output; the factor 2 per axis is folded into the
 // spectral multipliers, which are multiplied by 16 (exact in binary floating point).
 #include "ib_common.cuh"
+#include "fft_small.cuh"
 
 #include <cmath>
 #include <cstring>
@@ -32,85 +33,6 @@ namespace ib {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-
-// ------------------------------------------------------------------------------------------
-// small forward DFTs
-// ------------------------------------------------------------------------------------------
-template <typename T, int R> struct Dft;
-
-template <typename T> struct Dft<T, 2> {
-  template <typename V> __device__ __forceinline__ static void run(V* v) {
-    V a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
-  }
-};
-
-template <typename T> struct Dft<T, 4> {
-  template <typename V> __device__ __forceinline__ static void run(V* v) {
-    V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-    V t2 = cadd(v[1], v[3]), t3 = cmul_mi(csub(v[1], v[3]));
-    v[0] = cadd(t0, t2);
-    v[2] = csub(t0, t2);
-    v[1] = cadd(t1, t3);
-    v[3] = csub(t1, t3);
-  }
-};
-
-template <typename T> struct Dft<T, 8> {
-  template <typename V> __device__ __forceinline__ static void run(V* v) {
-    const T r2 = T(0.70710678118654752440);
-    V e[4] = {v[0], v[2], v[4], v[6]};
-    V o[4] = {v[1], v[3], v[5], v[7]};
-    Dft<T, 4>::run(e);
-    Dft<T, 4>::run(o);
-    // o1 *= (1 - i)/sqrt2 ; o2 *= -i ; o3 *= (-1 - i)/sqrt2
-    V o1 = mk<V>(r2 * (o[1].x + o[1].y), r2 * (o[1].y - o[1].x));
-    V o2 = cmul_mi(o[2]);
-    V o3 = mk<V>(r2 * (o[3].y - o[3].x), -r2 * (o[3].x + o[3].y));
-    v[0] = cadd(e[0], o[0]);
-    v[4] = csub(e[0], o[0]);
-    v[1] = cadd(e[1], o1);
-    v[5] = csub(e[1], o1);
-    v[2] = cadd(e[2], o2);
-    v[6] = csub(e[2], o2);
-    v[3] = cadd(e[3], o3);
-    v[7] = csub(e[3], o3);
-  }
-};
-
-template <typename T> struct Dft<T, 3> {
-  template <typename V> __device__ __forceinline__ static void run(V* v) {
-    const T s = T(0.86602540378443864676);
-    V t1 = cadd(v[1], v[2]);
-    V d = csub(v[1], v[2]);
-    V t2 = mk<V>(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
-    V t3 = mk<V>(s * d.y, -s * d.x);  // -i s (x1 - x2)
-    v[0] = cadd(v[0], t1);
-    v[1] = cadd(t2, t3);
-    v[2] = csub(t2, t3);
-  }
-};
-
-template <typename T> struct Dft<T, 5> {
-  template <typename V> __device__ __forceinline__ static void run(V* v) {
-    const T c1 = T(0.30901699437494742410), c2 = T(-0.80901699437494742410);
-    const T s1 = T(0.95105651629515357212), s2 = T(0.58778525229247312917);
-    V a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
-    V a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
-    V x0 = v[0];
-    V r1 = mk<V>(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
-    V r2 = mk<V>(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
-    V i1 = mk<V>(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
-    V i2 = mk<V>(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
-    v[0] = mk<V>(x0.x + a1.x + a2.x, x0.y + a1.y + a2.y);
-    // y = r -/+ i*ii :  -i*(a+ib) = (b, -a)
-    v[1] = mk<V>(r1.x + i1.y, r1.y - i1.x);
-    v[4] = mk<V>(r1.x - i1.y, r1.y + i1.x);
-    v[2] = mk<V>(r2.x + i2.y, r2.y - i2.x);
-    v[3] = mk<V>(r2.x - i2.y, r2.y + i2.x);
-  }
-};
 
 constexpr int kGroup = 64;  // threads per line
 
@@ -145,10 +67,6 @@ __device__ __forceinline__ void fft_stage(const c2_t<T>* __restrict__ src, c2_t<
     for (int r = 0; r < R; ++r) dst[cpad(base + r * Ns)] = v[r];
   }
 }
-
-template <typename T> __device__ __forceinline__ T fmaT(T a, T b, T c);
-template <> __device__ __forceinline__ double fmaT(double a, double b, double c) { return fma(a, b, c); }
-template <> __device__ __forceinline__ float fmaT(float a, float b, float c) { return fmaf(a, b, c); }
 
 // Shared-memory values per line buffer: the padded complex FFT layout of n reals, rounded to a
 // multiple of 4 values so consecutive buffers stay 16-byte aligned.
@@ -488,6 +406,22 @@ cudaError_t launch_y(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>
 
 }  // namespace
 
+cudaError_t set_smem_limit(const void* fn, size_t bytes) { return ensure_smem(fn, bytes); }
+
+// Warp-per-line transforms need M = n/2 = 32 P with P = 2^k or 3 2^k, P <= 32.
+static int warp_p(int n) {
+  if (n % 2) return 0;
+  const int M = n / 2;
+  if (M % 32) return 0;
+  const int P = M / 32;
+  switch (P) {
+    case 1: case 2: case 3: case 4: case 6: case 8: case 12: case 16: case 24: case 32: return P;
+    default: return 0;
+  }
+}
+
+bool wdst_axis_supported(int n) { return dst_axis_supported(n) && warp_p(n) > 0; }
+
 bool dst_axis_supported(int n) {
   if (n < 8 || n % 4 != 0 || n / 2 > 1024) return false;
   int r[kMaxStages];
@@ -515,18 +449,60 @@ cudaError_t AxisTables<T>::build(int n) {
     post[k] = mk<V>((T)cosl(ang), (T)sinl(ang));
   }
   for (int j = 0; j <= n / 2; ++j) sn[j] = (T)sinl(pi * (long double)j / (long double)n);
+  // lane-ordered tables of the warp-per-line transforms
+  const int P = warp_p(n);
+  d.wP = P;
+  const int G = !P ? 1 : (32 % P == 0 ? 32 / P : 32);
+  int lg = 0;
+  while ((1 << lg) < G) ++lg;
+  std::vector<V> w1((size_t)P * 32), w2((size_t)P * 32), w3((size_t)(lg > 0 ? lg : 1) * 32), ws((size_t)P * 32);
+  auto cis = [&](long double num, long double den) {  // e^{-2 pi i num / den}
+    const long double ang = -2.0L * pi * num / den;
+    return mk<V>((T)cosl(ang), (T)sinl(ang));
+  };
+  for (int a = 0; a < P; ++a)
+    for (int l = 0; l < 32; ++l) {
+      w1[a * 32 + l] = cis((long double)(l * a), (long double)M);
+      w2[a * 32 + l] = cis((long double)((l % G) * a), 32.0L);
+      const int m = l + 32 * a;
+      ws[a * 32 + l] = mk<V>((T)sinl(pi * (long double)(2 * m) / (long double)n),
+                             (T)sinl(pi * (long double)(2 * m + 1) / (long double)n));
+    }
+  for (int s = 0; s < lg; ++s) {
+    const int h = G >> (s + 1);
+    for (int l = 0; l < 32; ++l) {
+      const int j = (l % G) % (2 * h);
+      w3[s * 32 + l] = j >= h ? cis((long double)(j - h), (long double)(2 * h)) : mk<V>((T)1, (T)0);
+    }
+  }
   const size_t b_tw = tw.size() * sizeof(V), b_post = post.size() * sizeof(V), b_sn = sn.size() * sizeof(T);
-  const size_t o_post = (b_tw + 255) / 256 * 256;
-  const size_t o_sn = o_post + (b_post + 255) / 256 * 256;
-  cudaError_t e = cudaMalloc(&mem, o_sn + b_sn);
+  const size_t b_w = (size_t)P * 32 * sizeof(V), b_w3 = w3.size() * sizeof(V);
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t o_post = up(b_tw);
+  const size_t o_sn = o_post + up(b_post);
+  const size_t o_w1 = o_sn + up(b_sn);
+  const size_t o_w2 = o_w1 + up(b_w);
+  const size_t o_w3 = o_w2 + up(b_w);
+  const size_t o_ws = o_w3 + up(b_w3);
+  cudaError_t e = cudaMalloc(&mem, o_ws + up(b_w));
   if (e != cudaSuccess) { mem = nullptr; return e; }
   char* base = (char*)mem;
   if ((e = cudaMemcpy(base, tw.data(), b_tw, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
   if ((e = cudaMemcpy(base + o_post, post.data(), b_post, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
   if ((e = cudaMemcpy(base + o_sn, sn.data(), b_sn, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  if (P) {
+    if ((e = cudaMemcpy(base + o_w1, w1.data(), b_w, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    if ((e = cudaMemcpy(base + o_w2, w2.data(), b_w, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    if ((e = cudaMemcpy(base + o_w3, w3.data(), b_w3, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    if ((e = cudaMemcpy(base + o_ws, ws.data(), b_w, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+  }
   d.tw = (const V*)base;
   d.post = (const V*)(base + o_post);
   d.sintab = (const T*)(base + o_sn);
+  d.wtw1 = P ? (const V*)(base + o_w1) : nullptr;
+  d.wtw2 = P ? (const V*)(base + o_w2) : nullptr;
+  d.wtw3 = P ? (const V*)(base + o_w3) : nullptr;
+  d.wsn = P ? (const V*)(base + o_ws) : nullptr;
   return cudaSuccess;
 }
 

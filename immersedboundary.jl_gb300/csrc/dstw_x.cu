@@ -1,0 +1,337 @@
+// Warp-per-line x passes (see dstw.cuh): the first and last pass of every Poisson / CN solve
+// on grids whose axes have warp-per-line tables.
+//
+//   k_wxf: rows of the input -> prologue (load, apply_bc edges, refinement residual) -> S_x
+//          -> stored transposed (column by column) for the y pass
+//   k_wxi: transposed intermediate -> S_x -> epilogue (store, subtract, add the FP32 base
+//          iterate) into row-major output
+// A block owns kWarps consecutive rows; the transposing copies go through the rows' shared
+// buffers so that both the row-major and the column-major side are contiguous in memory.
+#include "dstw.cuh"
+
+namespace ib {
+namespace {
+
+using wdst::kWarps;
+using wdst::Shape;
+using wdst::warp_dst;
+
+template <typename T, typename Tin, int P, int PRO, bool kBC>
+__global__ void __launch_bounds__(kWarps * 32)
+k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
+  // exact arithmetic of the prologue: FP64, or float-float when the input is float-float
+  using A = typename std::conditional<is_df64<Tin>::value, df64, double>::type;
+  using Sh = Shape<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* U = sm + w * Sh::kStride;
+  T* D = U + Sh::kU;
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int total = a.batch * nrow;
+  const Tin* in = static_cast<const Tin*>(a.in);
+  T* out = static_cast<T*>(a.out);
+  for (int base = blockIdx.x * kWarps; base < total; base += gridDim.x * kWarps) {
+    const int row = base + w;
+    if (row < total) {
+      const int b = row / nrow, J = row - b * nrow;
+      const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
+      const Tin* src = in + off;
+      if constexpr (PRO == kProResid && is_df64<Tin>::value) {
+        // refinement residual r = b [+ apply_bc] - M x, x = x0 [+ x1] (FP32 parts), with
+        // M x = mc x + ma (4 x - neighbours) to float-float accuracy.  Only float(r) is kept
+        // (it feeds an FP32 transform), so the final difference needs no more than float
+        // arithmetic on the float-float parts.
+        const float* x0 = a.base + off;
+        const float* x1 = a.base2 ? a.base2 + off : nullptr;
+        const double mcd = a.mc[b * a.mstep];
+        const df64 mc = df64(mcd), ma = df64(a.ma[b * a.mstep]);
+        const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
+        const bool fac1 = a.bcfac == 1.0;
+        const df64 fac = df64(a.bcfac);
+#pragma unroll 2
+        for (int I = lane; I < ncol; I += 32) {
+          auto nb = [&](const float* x, float& c, float& w, float& e, float& s, float& n) {
+            c = x[I];
+            w = I > 0 ? x[I - 1] : 0.0f;
+            e = I < ncol - 1 ? x[I + 1] : 0.0f;
+            s = J > 0 ? x[I - ncol] : 0.0f;
+            n = J < nrow - 1 ? x[I + ncol] : 0.0f;
+          };
+          float c0, w0, e0, s0, n0;
+          nb(x0, c0, w0, e0, s0, n0);
+          df64 lap = lap5_exact(c0, w0, e0, s0, n0);
+          df64 xv = df64(c0);
+          if (x1) {
+            float c1, w1, e1, s1, n1;
+            nb(x1, c1, w1, e1, s1, n1);
+            lap = add_sloppy(lap, lap5_exact(c1, w1, e1, s1, n1));
+            xv = two_sum(c0, c1);
+          }
+          df64 mx = ma * lap;
+          if (mcd == 1.0) mx = add_sloppy(mx, xv);
+          else if (mcd != 0.0) mx = add_sloppy(mx, mc * xv);
+          df64 v = src[I];
+          if (kBC) {
+            auto addbc = [&](df64 q) { v = add_sloppy(v, fac1 ? q : fac * q); };
+            if (J == 0) addbc(bc[g.B + 1 + I]);
+            if (J == nrow - 1) addbc(bc[g.T + 1 + I]);
+            if (I == 0) addbc(bc[g.L + 1 + J]);
+            if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
+          }
+          U[I + 1] = (T)((v.hi - mx.hi) + (v.lo - mx.lo));
+        }
+      } else if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
+        for (int I0 = lane; I0 < ncol; I0 += 8 * 32) {
+          T v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = (I0 + 32 * u < ncol) ? (T)src[I0 + 32 * u] : T(0);
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (I0 + 32 * u < ncol) U[I0 + 32 * u + 1] = v[u];
+        }
+      } else {
+        const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
+        const A fac = A(a.bcfac);
+        const float* x0 = (PRO == kProResid) ? a.base + off : nullptr;
+        const float* x1 = (PRO == kProResid && a.base2) ? a.base2 + off : nullptr;
+        const A mc = (PRO == kProResid) ? A(a.mc[b * a.mstep]) : A(0.0);
+        const A ma = (PRO == kProResid) ? A(a.ma[b * a.mstep]) : A(0.0);
+#pragma unroll 4
+        for (int I = lane; I < ncol; I += 32) {
+          A v = A(src[I]);
+          if (kBC) {
+            if (J == 0) v = v + fac * bc[g.B + 1 + I];
+            if (J == nrow - 1) v = v + fac * bc[g.T + 1 + I];
+            if (I == 0) v = v + fac * bc[g.L + 1 + J];
+            if (I == ncol - 1) v = v + fac * bc[g.R + 1 + J];
+          }
+          if (PRO == kProResid) {
+            auto X = [&](int i) { return x1 ? A(x0[i]) + A(x1[i]) : A(x0[i]); };
+            const A xc = X(I);
+            A lap = A(4.0) * xc;
+            if (I > 0) lap = lap - X(I - 1);
+            if (I < ncol - 1) lap = lap - X(I + 1);
+            if (J > 0) lap = lap - X(I - ncol);
+            if (J < nrow - 1) lap = lap - X(I + ncol);
+            v = v - (mc * xc + ma * lap);
+          }
+          U[I + 1] = (T)v;
+        }
+      }
+      __syncwarp();
+      warp_dst<T, P>(U, D, ax, lane);
+    }
+    __syncthreads();
+    // transposed store: thread (ww = tid mod kWarps) copies row base + ww, kWarps consecutive
+    // threads write the block's rows of one column I next to each other
+    {
+      const int ww = threadIdx.x & (kWarps - 1);
+      const int rr = base + ww;
+      if (rr < total) {
+        const int b = rr / nrow, J = rr - b * nrow;
+        T* o = out + (int64_t)b * a.stride + J;
+        const T* srow = sm + ww * Sh::kStride + 1;
+        constexpr int step = kWarps * 32 / kWarps;
+#pragma unroll 8
+        for (int I = threadIdx.x / kWarps; I < ncol; I += step) o[(int64_t)I * nrow] = srow[I];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, typename Tout, int P, int EPI>
+__global__ void __launch_bounds__(kWarps * 32)
+k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
+  using A = typename std::conditional<is_df64<Tout>::value, df64, double>::type;
+  using Sh = Shape<T, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* U = sm + w * Sh::kStride;
+  T* D = U + Sh::kU;
+  const int ncol = g.nx - 1, nrow = g.ny - 1;
+  const int total = a.batch * nrow;
+  const T* in = static_cast<const T*>(a.in);
+  Tout* out = static_cast<Tout*>(a.out);
+  for (int base = blockIdx.x * kWarps; base < total; base += gridDim.x * kWarps) {
+    // transposed load (the mirror of k_wxf's store), eight loads in flight per thread
+    {
+      const int ww = threadIdx.x & (kWarps - 1);
+      const int rr = base + ww;
+      if (rr < total) {
+        const int b = rr / nrow, J = rr - b * nrow;
+        const T* src = in + (int64_t)b * a.stride + J;
+        T* drow = sm + ww * Sh::kStride + 1;
+        constexpr int step = kWarps * 32 / kWarps;
+        for (int I0 = threadIdx.x / kWarps; I0 < ncol; I0 += 8 * step) {
+          T v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int I = I0 + u * step;
+            v[u] = I < ncol ? src[(int64_t)I * nrow] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int I = I0 + u * step;
+            if (I < ncol) drow[I] = v[u];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const int row = base + w;
+    if (row < total) {
+      const int b = row / nrow, J = row - b * nrow;
+      const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
+      warp_dst<T, P>(U, D, ax, lane);
+      Tout* dst = out + off;
+      if (EPI == kEpiStore) {
+#pragma unroll 8
+        for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)U[I + 1];
+      } else if (EPI == kEpiSub) {
+        const A* sf = static_cast<const A*>(a.sub_from) + off;
+#pragma unroll 4
+        for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - A(U[I + 1]));
+      } else if constexpr (is_df64<Tout>::value) {
+        // x = x0 [+ x1] + d: the FP32 parts summed error-free, the (small) correction added
+        // to the low part
+        const float* bs = a.base + off;
+        const float* bs2 = a.base2 ? a.base2 + off : nullptr;
+        const df64* sf = (EPI == kEpiSubAddBase) ? static_cast<const df64*>(a.sub_from) + off : nullptr;
+#pragma unroll 4
+        for (int I = lane; I < ncol; I += 32) {
+          const df64 x01 = bs2 ? two_sum(bs[I], bs2[I]) : df64(bs[I]);
+          const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
+          dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(sf[I], -xv) : xv;
+        }
+      } else {
+        const float* bs = a.base + off;
+        const float* bs2 = a.base2 ? a.base2 + off : nullptr;
+        const A* sf = (EPI == kEpiSubAddBase) ? static_cast<const A*>(a.sub_from) + off : nullptr;
+#pragma unroll 4
+        for (int I = lane; I < ncol; I += 32) {
+          A xv = A(bs[I]);
+          if (bs2) xv = xv + A(bs2[I]);
+          xv = xv + A(U[I + 1]);
+          dst[I] = (Tout)((EPI == kEpiSubAddBase) ? sf[I] - xv : xv);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int P>
+size_t smem_bytes() {
+  return (size_t)kWarps * Shape<T, P>::kStride * sizeof(T);
+}
+
+template <typename T, typename Tin, int P, int PRO, bool kBC>
+cudaError_t launch_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  auto k = k_wxf<T, Tin, P, PRO, kBC>;
+  const size_t smem = smem_bytes<T, P>();
+  cudaError_t e = set_smem_limit((const void*)k, smem);
+  if (e != cudaSuccess) return e;
+  const int total = a.batch * (g.ny - 1);
+  k<<<(total + kWarps - 1) / kWarps, kWarps * 32, smem, s>>>(g, ax, a);
+  return cudaGetLastError();
+}
+
+template <typename T, typename Tin, int P>
+cudaError_t fwd_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  const bool bc = a.bc != nullptr;
+  if (a.pro == kProResid) {
+    // the refinement residual belongs to the mixed path (float-float input)
+    if constexpr (is_df64<Tin>::value) {
+      if (!a.base || !a.mc || !a.ma) return cudaErrorInvalidValue;
+      return bc ? launch_fwd<T, Tin, P, kProResid, true>(g, ax, a, s)
+                : launch_fwd<T, Tin, P, kProResid, false>(g, ax, a, s);
+    }
+    return cudaErrorInvalidValue;
+  }
+  return bc ? launch_fwd<T, Tin, P, kProLoad, true>(g, ax, a, s) : launch_fwd<T, Tin, P, kProLoad, false>(g, ax, a, s);
+}
+
+template <typename T, typename Tout, int P, int EPI>
+cudaError_t launch_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  auto k = k_wxi<T, Tout, P, EPI>;
+  const size_t smem = smem_bytes<T, P>();
+  cudaError_t e = set_smem_limit((const void*)k, smem);
+  if (e != cudaSuccess) return e;
+  const int total = a.batch * (g.ny - 1);
+  k<<<(total + kWarps - 1) / kWarps, kWarps * 32, smem, s>>>(g, ax, a);
+  return cudaGetLastError();
+}
+
+// epilogues per output type: FP64 path store / subtract; mixed path FP32 store of the iterate
+// and float-float sums with the base iterate
+template <typename T, typename Tout, int P>
+cudaError_t inv_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  if (a.bc) return cudaErrorInvalidValue;
+  if constexpr (std::is_same<Tout, T>::value) {
+    if (a.epi == kEpiStore) return launch_inv<T, Tout, P, kEpiStore>(g, ax, a, s);
+    if constexpr (std::is_same<T, double>::value) {
+      if (a.epi == kEpiSub) return launch_inv<T, Tout, P, kEpiSub>(g, ax, a, s);
+    }
+    return cudaErrorInvalidValue;
+  } else {
+    if (!a.base) return cudaErrorInvalidValue;
+    if (a.epi == kEpiAddBase) return launch_inv<T, Tout, P, kEpiAddBase>(g, ax, a, s);
+    if (a.epi == kEpiSubAddBase) return launch_inv<T, Tout, P, kEpiSubAddBase>(g, ax, a, s);
+    return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace
+
+template <typename T, typename Tin>
+cudaError_t wx_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  if (ax.n != g.nx || !ax.wP) return cudaErrorInvalidValue;
+  if (a.batch <= 0) return cudaSuccess;
+  ProfScope prof(kClassXPass, s);
+  switch (ax.wP) {
+    case 1: return fwd_p<T, Tin, 1>(g, ax, a, s);
+    case 2: return fwd_p<T, Tin, 2>(g, ax, a, s);
+    case 3: return fwd_p<T, Tin, 3>(g, ax, a, s);
+    case 4: return fwd_p<T, Tin, 4>(g, ax, a, s);
+    case 6: return fwd_p<T, Tin, 6>(g, ax, a, s);
+    case 8: return fwd_p<T, Tin, 8>(g, ax, a, s);
+    case 12: return fwd_p<T, Tin, 12>(g, ax, a, s);
+    case 16: return fwd_p<T, Tin, 16>(g, ax, a, s);
+    case 24: return fwd_p<T, Tin, 24>(g, ax, a, s);
+    case 32: return fwd_p<T, Tin, 32>(g, ax, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <typename T, typename Tout>
+cudaError_t wx_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  if (ax.n != g.nx || !ax.wP) return cudaErrorInvalidValue;
+  if (a.batch <= 0) return cudaSuccess;
+  ProfScope prof(kClassXPass, s);
+  switch (ax.wP) {
+    case 1: return inv_p<T, Tout, 1>(g, ax, a, s);
+    case 2: return inv_p<T, Tout, 2>(g, ax, a, s);
+    case 3: return inv_p<T, Tout, 3>(g, ax, a, s);
+    case 4: return inv_p<T, Tout, 4>(g, ax, a, s);
+    case 6: return inv_p<T, Tout, 6>(g, ax, a, s);
+    case 8: return inv_p<T, Tout, 8>(g, ax, a, s);
+    case 12: return inv_p<T, Tout, 12>(g, ax, a, s);
+    case 16: return inv_p<T, Tout, 16>(g, ax, a, s);
+    case 24: return inv_p<T, Tout, 24>(g, ax, a, s);
+    case 32: return inv_p<T, Tout, 32>(g, ax, a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// FP64 path: double in and out.  Mixed path: FP32 transforms fed from float-float inputs,
+// FP32 iterates, float-float results.
+template cudaError_t wx_fwd<double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_fwd<float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_inv<double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_inv<float, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_inv<float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+
+}  // namespace ib

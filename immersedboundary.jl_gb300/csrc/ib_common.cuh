@@ -49,6 +49,13 @@ template <typename T> struct DstAxis {
   const c2_t<T>* tw;        // [M]      e^{-2 pi i p / M}
   const T* sintab;          // [n/2+1]  sin(pi j / n)
   const c2_t<T>* post;      // [M/2+1]  e^{-2 pi i k / n}
+  // warp-per-line transforms (dstw.cuh), axes with M = 32 wP, wP in {1,2,4,8,16,32}; 0 otherwise.
+  // Tables in lane order (entry [s][lane] at s*32 + lane), G = 32 / wP:
+  int wP;
+  const c2_t<T>* wtw1;      // [wP][32]     e^{-2 pi i lane a / M}
+  const c2_t<T>* wtw2;      // [wP][32]     e^{-2 pi i (lane mod G) c / 32}
+  const c2_t<T>* wtw3;      // [log2 G][32] radix-2 twiddles of the cross-lane stages
+  const c2_t<T>* wsn;       // [wP][32]     (sin(pi 2m/n), sin(pi (2m+1)/n)), m = lane + 32 r
 };
 
 struct Geometry {
@@ -79,6 +86,11 @@ template <typename T> struct AxisTables {
 };
 
 bool dst_axis_supported(int n);
+// both axes have warp-per-line tables: the solves use the dstw passes (transposed intermediate)
+bool wdst_axis_supported(int n);
+
+// Raise a kernel's dynamic shared-memory limit (once per device; never inside stream capture).
+cudaError_t set_smem_limit(const void* fn, size_t bytes);
 
 // ----------------------------------------------------------------------------------------------
 // DST passes (dst.cu)
@@ -133,6 +145,18 @@ struct YPassArgs {
 
 template <typename T>
 cudaError_t ypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s);
+
+// Warp-per-line passes (dstw_*.cu), for axes with wdst_axis_supported.  The intermediate of a
+// solve is stored transposed, column by column: element (I, J) of slot b at b*stride + I*(ny-1) + J.
+//   wx_fwd: prologue (XArgs.pro, bc) -> x transform -> transposed store into a.out (type T)
+//   wypass: per column of the transposed array: S_y, multiply (or scale), S_y (kScale only)
+//   wx_inv: transposed load of a.in (type T) -> x transform -> epilogue (XArgs.epi) into a.out
+template <typename T, typename Tin>
+cudaError_t wx_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s);
+template <typename T>
+cudaError_t wypass(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& a, cudaStream_t s);
+template <typename T, typename Tout>
+cudaError_t wx_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s);
 
 
 // ----------------------------------------------------------------------------------------------

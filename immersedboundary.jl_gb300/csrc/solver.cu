@@ -69,6 +69,7 @@ struct ib_handle {
   float *x132 = nullptr;                        // second FP32 part of the iterate (2 sweeps)
   double* conv = nullptr;                       // mixed precision: FP64 copy-out buffer of the state
   int refine = 1;                               // refinement sweeps per mixed-precision solve
+  bool wdst = false;                            // both axes use the warp-per-line passes
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
   double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr, *d_alpha = nullptr;
@@ -164,6 +165,21 @@ SolveOp op_cn1(const ib_handle* h) { return {h->mCN1, h->mCN1_32, 0, h->d_one, h
 // subtract epilogue out = sub_from - (...).  w: FP64 work of batch arrays.
 cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
                       const double* sub_from, double* w) {
+  if (h->wdst) {
+    // warp-per-line passes; w holds the transposed intermediate
+    XArgs xa{};
+    xa.in = in; xa.out = w; xa.batch = batch; xa.stride = h->g.nG; xa.bc = bc; xa.bcfac = 1.0;
+    xa.pro = kProLoad; xa.epi = kEpiStore;
+    CE((wx_fwd<double, double>(h->g, h->axx.d, xa, h->stream)));
+    YPassArgs<double> ya{};
+    ya.in1 = w; ya.out = w; ya.batch = batch; ya.stride = h->g.nG; ya.m1 = op.m64; ya.mstride = op.mstride;
+    ya.op = SpecOp::kScale;
+    CE(wypass<double>(h->g, h->axy.d, ya, h->stream));
+    XArgs xb{};
+    xb.in = w; xb.out = out; xb.batch = batch; xb.stride = h->g.nG; xb.sub_from = sub_from;
+    xb.pro = kProLoad; xb.epi = sub_from ? kEpiSub : kEpiStore;
+    return wx_inv<double, double>(h->g, h->axx.d, xb, h->stream);
+  }
   XArgs xa{};
   xa.in = in;
   xa.out = w;
@@ -217,6 +233,30 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
   a.batch = batch;
   a.stride = g.nG;
   a.bcfac = 1.0;
+  if (h->wdst) {
+    // warp-per-line passes; w32 holds the transposed intermediate
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
+    CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
+    CE(wypass<float>(g, h->axy32.d, ya, s));
+    a.in = w32; a.out = x032; a.bc = nullptr;
+    CE((wx_inv<float, float>(g, h->axx32.d, a, s)));
+    const bool two = h->refine >= 2 && x132;
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
+    a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+    CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
+    CE(wypass<float>(g, h->axy32.d, ya, s));
+    if (two) {
+      a.in = w32; a.out = x132; a.bc = nullptr; a.pro = kProLoad; a.epi = kEpiStore; a.base = nullptr;
+      CE((wx_inv<float, float>(g, h->axx32.d, a, s)));
+      a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = x132;
+      CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
+      CE(wypass<float>(g, h->axy32.d, ya, s));
+    }
+    a.in = w32; a.out = out; a.bc = nullptr; a.pro = kProLoad; a.sub_from = sub_from;
+    a.base = x032; a.base2 = two ? x132 : nullptr;
+    a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
+    return wx_inv<float, df64>(g, h->axx32.d, a, s);
+  }
   // first solve
   a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
   CE((xpass<float, df64, float>(g, h->axx32.d, a, s)));
@@ -756,6 +796,12 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (p->refine_sweeps < 0 || p->refine_sweeps > 2) return bail(fail(h, IB_ERR_INVALID, "refine_sweeps must be 0, 1 or 2"));
   h->refine = p->refine_sweeps > 0 ? p->refine_sweeps : 2;
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
+  // transform kernels: warp-per-line where both axes allow it (IBGB300_DST=stockham selects the
+  // shared-memory Stockham passes for every grid)
+  h->wdst = wdst_axis_supported(p->nx) && wdst_axis_supported(p->ny);
+  if (const char* env = std::getenv("IBGB300_DST")) {
+    if (std::strcmp(env, "stockham") == 0) h->wdst = false;
+  }
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t nG = g.nG;
@@ -1162,10 +1208,20 @@ int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out) {
   // RODFT00 in both dimensions = 4 F_y F_x (F: the half-scaled transform of dst.cu)
   XArgs xa{};
   xa.in = in; xa.out = w; xa.batch = batch; xa.stride = g.nG; xa.pro = kProLoad; xa.epi = kEpiStore;
-  cudaError_t e = xpass<double, double, double>(g, h->axx.d, xa, s);
   YPassArgs<double> ya{};
   ya.in1 = w; ya.out = out; ya.batch = batch; ya.stride = g.nG; ya.op = SpecOp::kFwd; ya.scal = 4.0;
-  if (e == cudaSuccess) e = ypass<double>(g, h->axy.d, ya, s);
+  cudaError_t e;
+  if (h->wdst) {
+    // warp-per-line passes leave the result transposed ([I][J] per slot): transpose it back
+    e = wx_fwd<double, double>(g, h->axx.d, xa, s);
+    ya.out = w;
+    if (e == cudaSuccess) e = wypass<double>(g, h->axy.d, ya, s);
+    for (int b = 0; b < batch && e == cudaSuccess; ++b)
+      e = transpose(w + (int64_t)b * g.nG, out + (int64_t)b * g.nG, g.nx - 1, g.ny - 1, s);
+  } else {
+    e = xpass<double, double, double>(g, h->axx.d, xa, s);
+    if (e == cudaSuccess) e = ypass<double>(g, h->axy.d, ya, s);
+  }
   cudaStreamSynchronize(s);
   cudaFree(w);
   CK(e);

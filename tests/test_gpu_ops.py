@@ -31,7 +31,10 @@ def ogrid(O, prob):
     return O.Grid(b.nx, b.ny, d.discrete.nlevels, float(b.xs[0]), float(b.ys[0]), b.h)
 
 
-@pytest.mark.parametrize("nx,ny", [(16, 24), (40, 32), (200, 200), (256, 384), (1024, 768), (2048, 64)])
+# axes of 64 P cells (P = 2^k or 3 2^k, P <= 32) on both sides run the warp-per-line passes, the
+# others the shared-memory Stockham passes
+@pytest.mark.parametrize("nx,ny", [(16, 24), (40, 32), (200, 200), (256, 384), (1024, 768), (2048, 64),
+                                   (256, 128), (64, 2048), (1024, 1024), (768, 512), (192, 1536)])
 def test_dst2_matches_rodft00(ib, lib, dev, nx, ny):
     prob, s = make(ib, nx, ny, 1)
     rng = np.random.default_rng(nx + ny)
@@ -59,8 +62,9 @@ def test_dst2_pure_mode(ib, lib, dev):
     s.close()
 
 
-def test_laplacian_inv_and_cn(ib, lib, dev, O):
-    prob, s = make(ib, 96, 80, 3)
+@pytest.mark.parametrize("nx,ny", [(96, 80), (128, 256), (2048, 64), (768, 384)])
+def test_laplacian_inv_and_cn(ib, lib, dev, O, nx, ny):
+    prob, s = make(ib, nx, ny, 3)
     g = ogrid(O, prob)
     rng = np.random.default_rng(5)
     b = rng.standard_normal((2,) + g.gshape)

@@ -1,6 +1,6 @@
 """Step-level parity of the CUDA advance! against the FP64 oracle, through the C ABI.
 
-Tolerances (the spec bar for the FP64 path): per-step vorticity relative L2 <= 1e-10 and
+Tolerances (the bar for the FP64 path): per-step vorticity relative L2 <= 1e-10 and
 C_L / C_D <= 1e-8 (relative to max(1, |C|)), over the whole run; bitwise run-to-run.
 """
 import os
@@ -148,7 +148,7 @@ def test_errors_are_reported_not_faulted(ib):
     s.close()
 
 
-# Mixed precision (FP32 sine transforms + one FP64-residual refinement per solve): the bar is
+# Mixed precision (FP32 sine transforms + two float-float residual refinement sweeps per solve): the bar is
 # C_L / C_D within 1e-6 of the FP64 oracle; vorticity is checked at 1e-8 relative L2.
 M_GTOL = 1e-8
 M_CTOL = 1e-6
@@ -164,3 +164,29 @@ def test_mixed_parity_cylinder_small_full_size(ib, O):
     wl = ib.workloads.cylinder_small(nsteps=100)
     wg, wc = run_parity(ib, O, wl, 100, check_every=10, precision="mixed", gtol=M_GTOL, ftol=1e-6)
     assert wg < M_GTOL and wc < M_CTOL, (wg, wc)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-9)])
+def test_warp_and_stockham_transforms_agree(ib, monkeypatch, precision, tol):
+    """The warp-per-line passes (both axes 64 P cells) and the shared-memory Stockham passes
+    (selected with IBGB300_DST=stockham) give the same steps to round-off."""
+    wl = ib.workloads.scaled(ib.workloads.two_body_large(), 256, 256, nlevels=3)
+    out = {}
+    for mode in ("warp", "stockham"):
+        if mode == "stockham":
+            monkeypatch.setenv("IBGB300_DST", "stockham")
+        else:
+            monkeypatch.delenv("IBGB300_DST", raising=False)
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision=precision)
+        s.vort2flux(st)
+        cds = []
+        for i in range(10):
+            ib.advance_(st, s, i * wl.dt)
+            cds.append([b.CD for b in st.qty.stress])
+        out[mode] = (st.qty.gamma.copy(), np.array(cds))
+        s.close()
+    assert rel(out["warp"][0], out["stockham"][0]) < tol
+    assert np.max(np.abs(out["warp"][1] - out["stockham"][1])) < tol * 100

@@ -254,10 +254,11 @@ def run_ours(args, rank, world, local):
     out = {
         "metric": baseline_metric(), "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + f64 residual/state",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + float-float (2xf32) residual/state",
         "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
         "config": {"workload": describe(wl), "precision": prec,
-                   "refine_sweeps": (args.refine_sweeps or 2) if prec == "mixed" else 0,
+                   "refine_sweeps": ({0: "2 (1 on levels >= 3 of Vort2Flux)"}.get(args.refine_sweeps, args.refine_sweeps)
+                                     if prec == "mixed" else 0),
                    "cells_per_step": wl.cells_per_step,
                    "parallelism": "replicas",
                    "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),
@@ -386,7 +387,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="arithmetic of the timed arm (mixed: FP32 transforms + FP64 residual refinement)")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip timing the FP64 GPU path beside it")
-    ap.add_argument("--refine-sweeps", type=int, default=0, help="mixed precision: FP64-residual sweeps (0: default)")
+    ap.add_argument("--refine-sweeps", type=int, default=0,
+                    help="mixed precision: residual sweeps per solve (0: default policy, 1 or 2 everywhere)")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()

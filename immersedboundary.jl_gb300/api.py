@@ -390,9 +390,10 @@ class Solver:
     """``CNAB.Solver`` (cnab/timestepping.jl:173-249) backed by a libibgb300 handle.
 
     ``precision``: ``"fp64"`` (every sine transform in FP64, the reference's arithmetic) or
-    ``"mixed"`` (FP32 sine transforms refined with FP64 residuals, ``refine_sweeps`` sweeps per
-    Poisson solve, 0 = the library default of 2; state, nonlinear term, Schur solve and forces
-    stay FP64).
+    ``"mixed"`` (FP32 sine transforms refined with float-float residuals, ``refine_sweeps`` sweeps per
+    Poisson solve: 1 or 2 everywhere, or 0 = the library default of 2 with 1 for the Vort2Flux
+    solves of the third and coarser levels; state, stencils and the nonlinear term in float-float
+    arithmetic; Schur solve and forces FP64).
     """
 
     def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096,

@@ -27,7 +27,7 @@ namespace ib {
 namespace wdst {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kWarps = 8;  // lines (warps) per block
+constexpr int kWarps = 4;  // lines (warps) per block
 
 // cos(2 pi t / 96) for t = 0..24 (a quarter period); the rest by symmetry.  96 = lcm of the
 // in-lane transform sizes 2^k and 3 2^k (k <= 5).
@@ -133,10 +133,12 @@ struct Shape {
   static constexpr int kU = N + 64;
   // prefix-sum workspace, chunk of P padded by one: index k + k / P
   static constexpr int kD = M + 32;
-  // per-line stride: 16-byte aligned and 4 (mod 32) words apart, so that the eight lines of
-  // a block sit in different banks for the column-wise (transposing) copies
+  // per-line stride: 16-byte aligned and 32 / kWarps (mod 32) words apart, so that the lines
+  // of a block sit in different banks for the column-wise (transposing) copies
   static constexpr int words = (int)(sizeof(T) / 4);
-  static constexpr int stride_from(int s) { return ((s * words) % 32 == 4) ? s : stride_from(s + 1); }
+  static constexpr int stride_from(int s) {
+    return ((s * words) % 32 == 32 / kWarps && (s * (int)sizeof(T)) % 16 == 0) ? s : stride_from(s + 1);
+  }
   static constexpr int kStride = stride_from(kU + kD);
 };
 

@@ -49,37 +49,68 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
         const bool fac1 = a.bcfac == 1.0;
         const df64 fac = df64(a.bcfac);
-#pragma unroll 2
-        for (int I = lane; I < ncol; I += 32) {
-          auto nb = [&](const float* x, float& c, float& w, float& e, float& s, float& n) {
-            c = x[I];
-            w = I > 0 ? x[I - 1] : 0.0f;
-            e = I < ncol - 1 ? x[I + 1] : 0.0f;
-            s = J > 0 ? x[I - ncol] : 0.0f;
-            n = J < nrow - 1 ? x[I + ncol] : 0.0f;
-          };
-          float c0, w0, e0, s0, n0;
-          nb(x0, c0, w0, e0, s0, n0);
-          df64 lap = lap5_exact(c0, w0, e0, s0, n0);
-          df64 xv = df64(c0);
+        df64* rout = a.resid_out ? static_cast<df64*>(a.resid_out) + off : nullptr;
+        const float* xs = J > 0 ? x0 - ncol : nullptr;
+        const float* xn = J < nrow - 1 ? x0 + ncol : nullptr;
+        const float* ys = (x1 && J > 0) ? x1 - ncol : nullptr;
+        const float* yn = (x1 && J < nrow - 1) ? x1 + ncol : nullptr;
+        // eight elements per lane per round, every load of a round issued before any use
+        constexpr int R = 8;
+        for (int I0 = lane; I0 < ncol; I0 += 32 * R) {
+          float c0[R], w0[R], e0[R], s0[R], n0[R];
+          df64 v[R];
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            const int I = I0 + 32 * u;
+            const bool ok = I < ncol;
+            c0[u] = ok ? x0[I] : 0.0f;
+            w0[u] = (ok && I > 0) ? x0[I - 1] : 0.0f;
+            e0[u] = (I < ncol - 1) ? x0[I + 1] : 0.0f;
+            s0[u] = (ok && xs) ? xs[I] : 0.0f;
+            n0[u] = (ok && xn) ? xn[I] : 0.0f;
+            v[u] = ok ? src[I] : df64(0.0f);
+          }
+          df64 lap[R], xv[R];
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            lap[u] = lap5_exact(c0[u], w0[u], e0[u], s0[u], n0[u]);
+            xv[u] = df64(c0[u]);
+          }
           if (x1) {
-            float c1, w1, e1, s1, n1;
-            nb(x1, c1, w1, e1, s1, n1);
-            lap = add_sloppy(lap, lap5_exact(c1, w1, e1, s1, n1));
-            xv = two_sum(c0, c1);
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+              const int I = I0 + 32 * u;
+              const bool ok = I < ncol;
+              c0[u] = ok ? x1[I] : 0.0f;
+              w0[u] = (ok && I > 0) ? x1[I - 1] : 0.0f;
+              e0[u] = (I < ncol - 1) ? x1[I + 1] : 0.0f;
+              s0[u] = (ok && ys) ? ys[I] : 0.0f;
+              n0[u] = (ok && yn) ? yn[I] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+              lap[u] = add_sloppy(lap[u], lap5_exact(c0[u], w0[u], e0[u], s0[u], n0[u]));
+              xv[u] = two_sum(xv[u].hi, c0[u]);
+            }
           }
-          df64 mx = ma * lap;
-          if (mcd == 1.0) mx = add_sloppy(mx, xv);
-          else if (mcd != 0.0) mx = add_sloppy(mx, mc * xv);
-          df64 v = src[I];
-          if (kBC) {
-            auto addbc = [&](df64 q) { v = add_sloppy(v, fac1 ? q : fac * q); };
-            if (J == 0) addbc(bc[g.B + 1 + I]);
-            if (J == nrow - 1) addbc(bc[g.T + 1 + I]);
-            if (I == 0) addbc(bc[g.L + 1 + J]);
-            if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            const int I = I0 + 32 * u;
+            if (I >= ncol) break;
+            df64 mx = ma * lap[u];
+            if (mcd == 1.0) mx = add_sloppy(mx, xv[u]);
+            else if (mcd != 0.0) mx = add_sloppy(mx, mc * xv[u]);
+            df64 vv = v[u];
+            if (kBC) {
+              auto addbc = [&](df64 q) { vv = add_sloppy(vv, fac1 ? q : fac * q); };
+              if (J == 0) addbc(bc[g.B + 1 + I]);
+              if (J == nrow - 1) addbc(bc[g.T + 1 + I]);
+              if (I == 0) addbc(bc[g.L + 1 + J]);
+              if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
+            }
+            U[I + 1] = (T)((vv.hi - mx.hi) + (vv.lo - mx.lo));
+            if (rout) rout[I] = add_sloppy(vv, -mx);
           }
-          U[I + 1] = (T)((v.hi - mx.hi) + (v.lo - mx.lo));
         }
       } else if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
         for (int I0 = lane; I0 < ncol; I0 += 8 * 32) {
@@ -200,11 +231,26 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* bs = a.base + off;
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
         const df64* sf = (EPI == kEpiSubAddBase) ? static_cast<const df64*>(a.sub_from) + off : nullptr;
-#pragma unroll 4
-        for (int I = lane; I < ncol; I += 32) {
-          const df64 x01 = bs2 ? two_sum(bs[I], bs2[I]) : df64(bs[I]);
-          const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
-          dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(sf[I], -xv) : xv;
+        constexpr int R = 8;
+        for (int I0 = lane; I0 < ncol; I0 += 32 * R) {
+          float b0[R], b1[R];
+          df64 f[R];
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            const int I = I0 + 32 * u;
+            const bool ok = I < ncol;
+            b0[u] = ok ? bs[I] : 0.0f;
+            b1[u] = (ok && bs2) ? bs2[I] : 0.0f;
+            if (EPI == kEpiSubAddBase) f[u] = ok ? sf[I] : df64(0.0f);
+          }
+#pragma unroll
+          for (int u = 0; u < R; ++u) {
+            const int I = I0 + 32 * u;
+            if (I >= ncol) break;
+            const df64 x01 = two_sum(b0[u], b1[u]);
+            const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
+            dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(f[u], -xv) : xv;
+          }
         }
       } else {
         const float* bs = a.base + off;

@@ -130,6 +130,7 @@ struct XArgs {
   const double* ma;
   int mstep;
   int pro, epi;
+  void* resid_out;          // optional (warp passes, float-float input): the residual itself, float-float
 };
 
 template <typename T, typename Tin, typename Tout>

@@ -16,6 +16,7 @@
 #include "ibgb300_ops.h"
 #include "ibgb300_diag.h"
 
+#include <algorithm>
 #include <chrono>
 
 #include <cmath>
@@ -67,8 +68,11 @@ struct ib_handle {
   float *mLap32 = nullptr, *mCN1_32 = nullptr;  // FP32 copies (mixed precision)
   float *w32 = nullptr, *x032 = nullptr;        // mixed-precision work: transforms and x0
   float *x132 = nullptr;                        // second FP32 part of the iterate (2 sweeps)
+  double* r1 = nullptr;                         // first refinement residual (float-float, 2 sweeps)
   double* conv = nullptr;                       // mixed precision: FP64 copy-out buffer of the state
   int refine = 1;                               // refinement sweeps per mixed-precision solve
+  int refine_coarse = 2;                        // sweeps of the coarse-level Vort2Flux solves
+  int coarse_from = 2;                          // first (0-based) level counted as coarse
   bool wdst = false;                            // both axes use the warp-per-line passes
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
@@ -218,7 +222,7 @@ cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, co
 // b, the result and the residual arithmetic are float-float (df64.cuh), so the whole solve runs
 // on the FP32 pipe; w32 / x032 / x132: FP32 work of batch arrays.
 cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
-                          const df64* sub_from, float* w32, float* x032, float* x132) {
+                          const df64* sub_from, float* w32, float* x032, float* x132, int sweeps) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   YPassArgs<float> ya{};
@@ -240,15 +244,19 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
     CE(wypass<float>(g, h->axy32.d, ya, s));
     a.in = w32; a.out = x032; a.bc = nullptr;
     CE((wx_inv<float, float>(g, h->axx32.d, a, s)));
-    const bool two = h->refine >= 2 && x132;
+    const bool two = sweeps >= 2 && x132;
+    // sweep 1: r1 = b [+ bc] - M x0, kept in float-float for the second sweep
+    df64* r1 = two ? reinterpret_cast<df64*>(h->r1) : nullptr;
     a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
-    a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+    a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep; a.resid_out = r1;
     CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
     CE(wypass<float>(g, h->axy32.d, ya, s));
+    a.resid_out = nullptr;
     if (two) {
       a.in = w32; a.out = x132; a.bc = nullptr; a.pro = kProLoad; a.epi = kEpiStore; a.base = nullptr;
       CE((wx_inv<float, float>(g, h->axx32.d, a, s)));
-      a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = x132;
+      // sweep 2: r2 = b - M (x0 + d1) = r1 - M d1 (the boundary terms are in r1)
+      a.in = r1; a.out = w32; a.bc = nullptr; a.pro = kProResid; a.base = x132; a.base2 = nullptr;
       CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
       CE(wypass<float>(g, h->axy32.d, ya, s));
     }
@@ -263,7 +271,7 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
   CE(ypass<float>(g, h->axy32.d, ya, s));
   a.in = w32; a.out = x032; a.bc = nullptr;
   CE((xpass<float, float, float>(g, h->axx32.d, a, s)));
-  const bool two = h->refine >= 2 && x132;
+  const bool two = sweeps >= 2 && x132;
   // sweep 1: residual (df64) fused with the forward transform of the correction
   a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
   a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
@@ -291,8 +299,12 @@ cudaError_t solve(ib_handle* h, const double* in, double* out, int batch, const 
   return poisson64(h, in, out, batch, bc, op, sub_from, h->w1);
 }
 cudaError_t solve(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
-                  const df64* sub_from) {
-  return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032, h->x132);
+                  const df64* sub_from, int sweeps = 0) {
+  return poisson_mixed(h, in, out, batch, bc, op, sub_from, h->w32, h->x032, h->x132, sweeps > 0 ? sweeps : h->refine);
+}
+cudaError_t solve(ib_handle* h, const double* in, double* out, int batch, const double* bc, const SolveOp& op,
+                  const double* sub_from, int /*sweeps*/) {
+  return poisson64(h, in, out, batch, bc, op, sub_from, h->w1);
 }
 
 // The handle's state arrays hold doubles (FP64 mode) or float-float pairs (mixed mode); both are
@@ -310,13 +322,16 @@ cudaError_t vort2flux(ib_handle* h, S* gam, S* psi, S* q, S* q1, S* rings) {
   const int L = g.nlev;
   const int64_t nG = g.nG;
   for (int l = 1; l < L; ++l) CE(coarsify<S>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
-  CE(solve(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, op_lap(h), nullptr));
+  // mixed precision: the coarse levels only feed the finer levels' boundary rings
+  const int coarse = std::min(h->refine, h->refine_coarse);
+  CE(solve(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, op_lap(h), nullptr,
+           L - 1 >= h->coarse_from ? coarse : 0));
   if (q) CE(curl<S>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
   else if (L == 1) CE(curl<S>(g, psi, nullptr, q1, 1, h->stream));
   for (int l = L - 2; l >= 0; --l) {
     S* ring = rings + (int64_t)l * g.nbc;
     CE(get_bc<S>(g, psi + (l + 1) * nG, ring, 1, S(1.0), h->stream));
-    CE(solve(h, gam + l * nG, psi + l * nG, 1, ring, op_lap(h), nullptr));
+    CE(solve(h, gam + l * nG, psi + l * nG, 1, ring, op_lap(h), nullptr, l >= h->coarse_from ? coarse : 0));
     if (q) CE(curl<S>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
     else if (l == 0) CE(curl<S>(g, psi, ring, q1, 1, h->stream));
   }
@@ -536,8 +551,10 @@ int prime_kernels(ib_handle* h) {
   CK(poisson64(h, h->w2, h->w2, 1, nullptr, op_lap(h), h->w2, h->w1));
   if (h->precision == IB_PREC_MIXED) {
     df64* w2 = view<df64>(h->w2);
-    CK(poisson_mixed(h, w2, w2, 1, view<df64>(h->rings), op_lap(h), nullptr, h->w32, h->x032, h->x132));
-    CK(poisson_mixed(h, w2, w2, 1, nullptr, op_cn1(h), w2, h->w32, h->x032, h->x132));
+    for (int sw = 1; sw <= h->refine; ++sw) {
+      CK(poisson_mixed(h, w2, w2, 1, view<df64>(h->rings), op_lap(h), nullptr, h->w32, h->x032, h->x132, sw));
+      CK(poisson_mixed(h, w2, w2, 1, nullptr, op_cn1(h), w2, h->w32, h->x032, h->x132, sw));
+    }
   }
   CK(cudaMemsetAsync(h->w1, 0, sizeof(double) * g.nlev * g.nG, h->stream));
   CK(cudaMemsetAsync(h->w2, 0, sizeof(double) * g.nlev * g.nG, h->stream));
@@ -794,13 +811,29 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   h->motion = p->motion;
   h->hist_cap = p->history_capacity > 0 ? p->history_capacity : 4096;
   if (p->refine_sweeps < 0 || p->refine_sweeps > 2) return bail(fail(h, IB_ERR_INVALID, "refine_sweeps must be 0, 1 or 2"));
-  h->refine = p->refine_sweeps > 0 ? p->refine_sweeps : 2;
+  h->refine = p->refine_sweeps == 1 ? 1 : 2;
+  h->refine_coarse = p->refine_sweeps == 0 ? 1 : h->refine;
+  h->coarse_from = 2;
+  if (const char* env = std::getenv("IBGB300_REFINE_COARSE")) {
+    const int v = std::atoi(env);
+    if (v >= 1 && v <= 2) h->refine_coarse = v;
+  }
+  if (const char* env = std::getenv("IBGB300_COARSE_FROM")) {
+    const int v = std::atoi(env);
+    if (v >= 1) h->coarse_from = v;
+  }
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
-  // transform kernels: warp-per-line where both axes allow it (IBGB300_DST=stockham selects the
-  // shared-memory Stockham passes for every grid)
-  h->wdst = wdst_axis_supported(p->nx) && wdst_axis_supported(p->ny);
+  // transform kernels, by measurement on GB300: FP32 (mixed) transforms run faster one warp
+  // per line where both axes allow it; FP64 transforms are FP64-pipe bound and the shared-memory
+  // Stockham passes, with fewer twiddle multiplies and no transposing copies, are faster up to
+  // 1024-cell axes (3.85 vs 4.35 ms per 1024^2 4-level step), the warp passes at 2048 cells
+  // (19.3 vs 21.4 ms per 2048^2 5-level step).
+  // IBGB300_DST=warp|stockham overrides the choice for both precisions.
+  const bool wsup = wdst_axis_supported(p->nx) && wdst_axis_supported(p->ny);
+  h->wdst = wsup && (p->precision == IB_PREC_MIXED || std::max(p->nx, p->ny) >= 2048);
   if (const char* env = std::getenv("IBGB300_DST")) {
     if (std::strcmp(env, "stockham") == 0) h->wdst = false;
+    if (std::strcmp(env, "warp") == 0) h->wdst = wsup;
   }
   const Geometry& g = h->g;
   const int L = g.nlev;
@@ -830,7 +863,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (h->precision == IB_PREC_MIXED) {
     AL(h->mLap32, nG); AL(h->mCN1_32, L * nG);
     AL(h->w32, L * nG); AL(h->x032, L * nG);
-    if (h->refine >= 2) AL(h->x132, L * nG);
+    if (h->refine >= 2) { AL(h->x132, L * nG); AL(h->r1, L * nG); }
     AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
   }
   AL(h->status, 4); AL(h->d_counter, 1);

@@ -42,7 +42,8 @@ extern "C" {
 /* arithmetic of the fluid solve (state, nonlinear term, Schur solve and forces are FP64 in
  * every mode) */
 #define IB_PREC_FP64 0   /* every sine transform in FP64 (the reference's arithmetic) */
-#define IB_PREC_MIXED 1  /* sine transforms in FP32 refined with FP64 residuals (refine_sweeps) */
+#define IB_PREC_MIXED 1  /* FP32 sine transforms refined with float-float residuals (refine_sweeps);
+                            state and stencils in float-float (two-float) arithmetic */
 
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */
@@ -72,7 +73,9 @@ typedef struct ib_problem {
   int32_t precision;            /* IB_PREC_* */
   int32_t device;               /* CUDA device ordinal */
   int32_t history_capacity;     /* steps of C_D / C_L kept on the device (0 -> 4096) */
-  int32_t refine_sweeps;        /* IB_PREC_MIXED: FP64-residual sweeps per solve, 1 or 2 (0 -> 2) */
+  int32_t refine_sweeps;        /* IB_PREC_MIXED: residual sweeps per solve: 1 or 2 everywhere, or
+                                   0 (default): 2, except 1 for the Vort2Flux solves of the third
+                                   and coarser levels (they only feed boundary rings) */
 } ib_problem;
 
 typedef struct ib_handle ib_handle;

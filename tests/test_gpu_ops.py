@@ -31,11 +31,13 @@ def ogrid(O, prob):
     return O.Grid(b.nx, b.ny, d.discrete.nlevels, float(b.xs[0]), float(b.ys[0]), b.h)
 
 
-# axes of 64 P cells (P = 2^k or 3 2^k, P <= 32) on both sides run the warp-per-line passes, the
-# others the shared-memory Stockham passes
+# IBGB300_DST=warp: axes of 64 P cells (P = 2^k or 3 2^k, P <= 32) on both sides run the
+# warp-per-line passes, the others the shared-memory Stockham passes
+@pytest.mark.parametrize("dst", ["warp", "stockham"])
 @pytest.mark.parametrize("nx,ny", [(16, 24), (40, 32), (200, 200), (256, 384), (1024, 768), (2048, 64),
                                    (256, 128), (64, 2048), (1024, 1024), (768, 512), (192, 1536)])
-def test_dst2_matches_rodft00(ib, lib, dev, nx, ny):
+def test_dst2_matches_rodft00(ib, lib, dev, monkeypatch, nx, ny, dst):
+    monkeypatch.setenv("IBGB300_DST", dst)
     prob, s = make(ib, nx, ny, 1)
     rng = np.random.default_rng(nx + ny)
     x = rng.standard_normal((3, ny - 1, nx - 1))
@@ -62,8 +64,10 @@ def test_dst2_pure_mode(ib, lib, dev):
     s.close()
 
 
+@pytest.mark.parametrize("dst", ["warp", "stockham"])
 @pytest.mark.parametrize("nx,ny", [(96, 80), (128, 256), (2048, 64), (768, 384)])
-def test_laplacian_inv_and_cn(ib, lib, dev, O, nx, ny):
+def test_laplacian_inv_and_cn(ib, lib, dev, O, monkeypatch, nx, ny, dst):
+    monkeypatch.setenv("IBGB300_DST", dst)
     prob, s = make(ib, nx, ny, 3)
     g = ogrid(O, prob)
     rng = np.random.default_rng(5)

@@ -168,15 +168,12 @@ def test_mixed_parity_cylinder_small_full_size(ib, O):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-9)])
 def test_warp_and_stockham_transforms_agree(ib, monkeypatch, precision, tol):
-    """The warp-per-line passes (both axes 64 P cells) and the shared-memory Stockham passes
-    (selected with IBGB300_DST=stockham) give the same steps to round-off."""
+    """The warp-per-line passes (both axes 64 P cells; IBGB300_DST=warp) and the shared-memory
+    Stockham passes (IBGB300_DST=stockham) give the same steps to round-off."""
     wl = ib.workloads.scaled(ib.workloads.two_body_large(), 256, 256, nlevels=3)
     out = {}
     for mode in ("warp", "stockham"):
-        if mode == "stockham":
-            monkeypatch.setenv("IBGB300_DST", "stockham")
-        else:
-            monkeypatch.delenv("IBGB300_DST", raising=False)
+        monkeypatch.setenv("IBGB300_DST", mode)
         prob = wl.problem()
         st = ib.initstate(prob)
         st._gamma[:] = wl.initial_gamma()

@@ -31,9 +31,13 @@ IB_MOTION_PRESCRIBED = 1
 IB_WARM_PREVIOUS = 0
 IB_WARM_EXTRAPOLATE = 1
 IB_WARM_ZERO = 2
+IB_WARM_LEARNED = 3
+IB_PC_NONE = 0
+IB_PC_SCHUR_REF = 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
+_fp = C.POINTER(C.c_float)
 _vp = C.c_void_p
 
 
@@ -72,6 +76,8 @@ SIGNATURES = {
     "ib_advance_n_kin": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ib_set_cg_options": (C.c_int, [_vp, C.c_double, C.c_int32, C.c_int32]),
     "ib_get_cg_stats": (C.c_int, [_vp, C.c_int32, _ip, _dp]),
+    "ib_set_cg_preconditioner": (C.c_int, [_vp, C.c_int32, C.c_int32]),
+    "ib_get_cg_preconditioner_stats": (C.c_int, [_vp, _ip, C.POINTER(C.c_int64)]),
     "ib_get_body_points": (C.c_int, [_vp, _dp, _dp]),
     "ib_get_stress": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ib_get_force_history": (C.c_int, [_vp, C.c_int32, _dp, _dp]),
@@ -103,6 +109,18 @@ SIGNATURES = {
     "ib_profiler_start": (C.c_int, []),
     "ib_profiler_stop": (C.c_int, []),
     "ib_get_reg": (C.c_int, [_vp, _ip, _dp]),
+    # learned warm start
+    "ib_learn_init": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32, C.c_uint64]),
+    "ib_learn_collect": (C.c_int, [_vp, C.c_int32]),
+    "ib_learn_sample_count": (C.c_int, [_vp, _ip]),
+    "ib_learn_train": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_double, C.c_uint64, _dp]),
+    "ib_learn_layout": (C.c_int, [_vp, _ip, _ip, C.c_int32]),
+    "ib_learn_validation": (C.c_int, [_vp, _dp, _dp]),
+    "ib_learn_param_count": (C.c_int, [_vp, C.POINTER(C.c_int64)]),
+    "ib_learn_get_params": (C.c_int, [_vp, _fp]),
+    "ib_learn_set_params": (C.c_int, [_vp, _fp]),
+    "ib_learn_gradients": (C.c_int, [_vp, C.c_int32, _fp, _fp, _fp, _dp]),
+    "ib_get_cg_start_residuals": (C.c_int, [_vp, C.c_int32, _dp]),
 }
 
 _LIB = None
@@ -141,6 +159,14 @@ def dptr(a: np.ndarray | None):
         return None
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(_dp)
+
+
+def fptr(a: np.ndarray | None):
+    """Pointer to a C-contiguous float32 array (or NULL)."""
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_fp)
 
 
 def iptr(a: np.ndarray | None):

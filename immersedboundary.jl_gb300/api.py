@@ -500,16 +500,90 @@ class Solver:
         return k
 
     def set_cg_options(self, tol: float = 1e-10, maxiter: int = 5000, warm_start: str = "previous"):
-        """CG tolerance (||r|| / ||rhs||), cap and warm start ("previous", "extrapolate" or "zero")."""
+        """CG tolerance (||r|| / ||rhs||), cap and warm start ("previous", "extrapolate", "zero" or
+        "learned": the trained network of ``learn_init`` / ``learn_train``)."""
         mode = {"previous": _lib.IB_WARM_PREVIOUS, "extrapolate": _lib.IB_WARM_EXTRAPOLATE,
-                "zero": _lib.IB_WARM_ZERO}[warm_start]
+                "zero": _lib.IB_WARM_ZERO, "learned": _lib.IB_WARM_LEARNED}[warm_start]
         self._check(self.lib.ib_set_cg_options(self.handle, float(tol), int(maxiter), mode))
 
-    def cg_stats(self, count: int):
+    def set_cg_preconditioner(self, mode: str = "schur_ref", refresh_steps: int = 0):
+        """``"none"`` (plain CG, the reference's) or ``"schur_ref"``: PCG with the inverse Schur
+        matrix of a reference configuration, re-assembled every ``refresh_steps`` steps or, with 0,
+        when the iterations have doubled since the last assembly."""
+        m = {"none": _lib.IB_PC_NONE, "schur_ref": _lib.IB_PC_SCHUR_REF}[mode]
+        self._check(self.lib.ib_set_cg_preconditioner(self.handle, m, int(refresh_steps)))
+
+    def cg_preconditioner_stats(self):
+        n, last = C.c_int32(), C.c_int64()
+        self._check(self.lib.ib_get_cg_preconditioner_stats(self.handle, C.byref(n), C.byref(last)))
+        return n.value, last.value
+
+    def cg_stats(self, count: int, start: bool = False):
+        """Iterations and final relative residuals of the last `count` CG solves (and, with
+        ``start``, the initial relative residuals of their warm starts)."""
         it = np.zeros(count, dtype=np.int32)
         res = np.zeros(count)
         self._check(self.lib.ib_get_cg_stats(self.handle, count, _lib.iptr(it), _lib.dptr(res)))
-        return it, res
+        if not start:
+            return it, res
+        r0 = np.zeros(count)
+        self._check(self.lib.ib_get_cg_start_residuals(self.handle, count, _lib.dptr(r0)))
+        return it, res, r0
+
+    # learned warm start (include/ibgb300_learn.h)
+    def learn_init(self, hidden: int = 256, layers: int = 3, capacity: int = 4096, seed: int = 0):
+        self._check(self.lib.ib_learn_init(self.handle, int(hidden), int(layers), int(capacity), int(seed)))
+
+    def learn_collect(self, on: bool = True):
+        self._check(self.lib.ib_learn_collect(self.handle, 1 if on else 0))
+
+    def learn_samples(self) -> int:
+        n = C.c_int32()
+        self._check(self.lib.ib_learn_sample_count(self.handle, C.byref(n)))
+        return n.value
+
+    def learn_train(self, epochs: int = 200, batch: int = 64, lr: float = 1e-3, seed: int = 0) -> float:
+        loss = C.c_double()
+        self._check(self.lib.ib_learn_train(self.handle, int(epochs), int(batch), float(lr), int(seed),
+                                            C.byref(loss)))
+        return loss.value
+
+    def learn_validation(self):
+        """(blend, held-out error relative to plain extrapolation) of the last training."""
+        b, r = C.c_double(), C.c_double()
+        self._check(self.lib.ib_learn_validation(self.handle, C.byref(b), C.byref(r)))
+        return b.value, r.value
+
+    def learn_layout(self):
+        nl = C.c_int32()
+        dims = np.zeros(16, dtype=np.int32)
+        self._check(self.lib.ib_learn_layout(self.handle, C.byref(nl), _lib.iptr(dims), 16))
+        return [int(d) for d in dims[: nl.value + 1]]
+
+    def learn_params(self, params: np.ndarray | None = None) -> np.ndarray:
+        """Get (or, given ``params``, set) the FP32 parameter vector."""
+        n = C.c_int64()
+        self._check(self.lib.ib_learn_param_count(self.handle, C.byref(n)))
+        if params is not None:
+            p = np.ascontiguousarray(params, dtype=np.float32)
+            assert p.size == n.value
+            self._check(self.lib.ib_learn_set_params(self.handle, _lib.fptr(p)))
+            return p
+        out = np.zeros(n.value, dtype=np.float32)
+        self._check(self.lib.ib_learn_get_params(self.handle, _lib.fptr(out)))
+        return out
+
+    def learn_gradients(self, x: np.ndarray, y: np.ndarray):
+        """(loss, gradient) of the raw network on rows x, targets y (no normalisation)."""
+        n = C.c_int64()
+        self._check(self.lib.ib_learn_param_count(self.handle, C.byref(n)))
+        xa = np.ascontiguousarray(x, dtype=np.float32)
+        ya = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(n.value, dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.ib_learn_gradients(self.handle, int(xa.shape[0]), _lib.fptr(xa), _lib.fptr(ya),
+                                                _lib.fptr(g), C.byref(loss)))
+        return loss.value, g
 
     def body_points(self):
         xb = np.zeros(2 * max(self.nb, 1))

@@ -12,7 +12,9 @@
 // 5-point stencil it diagonalises (I - alpha_l rot curl); it is fused into the nonlinear-term
 // kernel, so each level's trial solve is one Poisson-type solve (equal up to round-off).
 #include "ib_common.cuh"
+#include "mlp.cuh"
 #include "ibgb300.h"
+#include "ibgb300_learn.h"
 #include "ibgb300_ops.h"
 #include "ibgb300_diag.h"
 
@@ -90,7 +92,17 @@ struct ib_handle {
   int motion = IB_MOTION_STATIC;
   double *xb_body = nullptr, *vb = nullptr, *d_kin = nullptr;
   int* body_of = nullptr;
-  double *cg_r = nullptr, *cg_p = nullptr, *cg_Ap = nullptr, *cg_sc = nullptr, *fb_prev = nullptr;
+  double *cg_r = nullptr, *cg_p = nullptr, *cg_Ap = nullptr, *cg_sc = nullptr;
+  double *fb_prev = nullptr, *fb_last = nullptr;  // F_{n-2}, F_{n-1} at the start of a step
+  double* cg_z = nullptr;                         // preconditioned residual
+  learn::Mlp* mlp = nullptr;                      // learned warm start (ib_learn_init)
+  bool collect = false;                           // record (features, F_n) every moving step
+  std::vector<double> cg_res0;                    // initial relative residual of each CG solve
+  int precond = IB_PC_NONE;                       // moving-body CG preconditioner
+  int pc_refresh = 0;                             // re-assembly period in steps (0: adaptive)
+  int pc_base_iters = -1;                         // iterations of the first solve after an assembly
+  int64_t pc_step = -1;                           // step of the last assembly
+  int pc_assemblies = 0;
   double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
   double* h_sc = nullptr;  // pinned CG scalars read back each iteration
   double cg_tol = 1e-10;
@@ -598,6 +610,7 @@ void destroy_handle(ib_handle* h) {
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_q0) cudaFreeHost(h->h_q0);
   if (h->h_sc) cudaFreeHost(h->h_sc);
+  delete h->mlp;
   h->axx.release();
   h->axy.release();
   h->axx32.release();
@@ -631,22 +644,31 @@ int stage_q0(ib_handle* h, double u, double v, const double* kin = nullptr) {
 // Conjugate gradients for B Fb = ftmp (cg!(qty.Fb, B, ftmp), cnab/ops.jl:104-114), warm-started
 // from h->fb, stopping when ||r|| <= tol ||ftmp||.  The residual norm is read back each iteration.
 // The CG vectors are FP64 in both modes; S is the state type of the B products.
+//
+// With a preconditioner (IB_PC_SCHUR_REF) this is PCG with z = P r, P the inverse Schur matrix of
+// a reference configuration (row-major h->binv_rm); the stopping rule is unchanged.
+// Scalars: sc[0] = r.z, sc[1] = p.Ap, sc[2] = new r.z, sc[3] = rhs.rhs, sc[4] = r.r.
 template <typename S>
 int cg_solve(ib_handle* h) {
   const int nf = h->nf;
   cudaStream_t s = h->stream;
   double *x = h->fb, *r = h->cg_r, *p = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
+  const bool pc = h->precond == IB_PC_SCHUR_REF && h->binv_rm && h->pc_step >= 0;
+  double* z = pc ? h->cg_z : r;
   CK(schur_apply<S>(h, x, Ap));
   CK(cudaMemcpyAsync(r, h->ftmp, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
   CK(vec_axpy(r, Ap, -1.0, nf, s));
-  CK(vec_dot(r, r, nf, sc + 0, s));
+  CK(vec_dot(r, r, nf, sc + 4, s));
   CK(vec_dot(h->ftmp, h->ftmp, nf, sc + 3, s));
-  CK(cudaMemcpyAsync(p, r, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
-  CK(cudaMemcpyAsync(h->h_sc, sc, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+  if (pc) CK(gemv_rowmajor(h->binv_rm, r, z, nf, s));
+  CK(vec_dot(r, z, nf, sc + 0, s));
+  CK(cudaMemcpyAsync(p, z, sizeof(double) * nf, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->h_sc, sc, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   const double target = h->cg_tol * std::sqrt(h->h_sc[3]);
-  double rn = std::sqrt(h->h_sc[0]);
+  double rn = std::sqrt(h->h_sc[4]);
   if (!std::isfinite(rn)) return fail(h, IB_ERR_NONFINITE, "infinite flux");
+  h->cg_res0.push_back(h->h_sc[3] > 0 ? rn / std::sqrt(h->h_sc[3]) : rn);
   int it = 0;
   bool conv = rn <= target;
   while (!conv && it < h->cg_maxiter) {
@@ -654,13 +676,21 @@ int cg_solve(ib_handle* h) {
     CK(schur_apply<S>(h, p, Ap));
     CK(vec_dot(p, Ap, nf, sc + 1, s));
     CK(cg_update_xr(x, r, p, Ap, sc, nf, s));
-    CK(vec_dot(r, r, nf, sc + 2, s));
-    CK(cudaMemcpyAsync(h->h_sc + 2, sc + 2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(vec_dot(r, r, nf, sc + 4, s));
+    CK(cudaMemcpyAsync(h->h_sc + 4, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    rn = std::sqrt(h->h_sc[2]);
+    rn = std::sqrt(h->h_sc[4]);
     if (!std::isfinite(rn)) return fail(h, IB_ERR_NONFINITE, "infinite flux");
     conv = rn <= target;
-    if (!conv) CK(cg_update_p(p, r, sc, nf, s));
+    if (!conv) {
+      if (pc) {
+        CK(gemv_rowmajor(h->binv_rm, r, z, nf, s));
+        CK(vec_dot(r, z, nf, sc + 2, s));
+      } else {
+        CK(vec_dot(r, r, nf, sc + 2, s));
+      }
+      CK(cg_update_p(p, z, sc, nf, s));
+    }
   }
   h->cg_iters.push_back(it);
   h->cg_res.push_back(h->h_sc[3] > 0 ? rn / std::sqrt(h->h_sc[3]) : rn);
@@ -686,17 +716,55 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
   CK(vec_axpy(h->ftmp, h->vb, -g.h, h->nf, s));
   rc = check_status(h);
   if (rc != IB_OK) return rc;
-  // warm start: the previous Fb (the reference's cg! on qty.Fb) or its linear extrapolation
-  if (h->warm_start == IB_WARM_EXTRAPOLATE && h->steps >= 2) {
-    CK(cudaMemcpyAsync(h->cg_p, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
-    CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
-    CK(cudaMemcpyAsync(h->fb_prev, h->cg_p, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
-  } else {
-    CK(cudaMemcpyAsync(h->fb_prev, h->fb, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
-    if (h->warm_start == IB_WARM_ZERO) CK(cudaMemsetAsync(h->fb, 0, sizeof(double) * h->nf, s));
+  // warm start (h->fb holds F_{n-1}, h->fb_prev F_{n-2}): the previous Fb (the reference's cg!
+  // on qty.Fb), its linear extrapolation, zero, or the learned prediction (extrapolation until a
+  // network is trained)
+  const size_t fbytes = sizeof(double) * h->nf;
+  const bool hist2 = h->steps >= 2;
+  CK(cudaMemcpyAsync(h->fb_last, h->fb, fbytes, cudaMemcpyDeviceToDevice, s));
+  const bool use_mlp = h->mlp && (h->collect || h->warm_start == IB_WARM_LEARNED);
+  if (use_mlp) CK(h->mlp->features(h->d_kin, 6 * h->nbodies, h->fb_last, h->fb_prev, h->nf));
+  switch (h->warm_start) {
+    case IB_WARM_ZERO: CK(cudaMemsetAsync(h->fb, 0, fbytes, s)); break;
+    case IB_WARM_EXTRAPOLATE:
+      if (hist2) CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
+      break;
+    case IB_WARM_LEARNED:
+      if (hist2 && h->mlp && h->mlp->trained) CK(h->mlp->predict(h->fb_last, h->fb_prev, h->fb));
+      else if (hist2) CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
+      break;
+    default: break;
+  }
+  // preconditioner: the inverse Schur matrix of the current configuration, assembled at the first
+  // step and again every pc_refresh steps, or (pc_refresh = 0) when the iterations have grown to
+  // twice (and 10 more than) those right after the last assembly
+  if (h->precond == IB_PC_SCHUR_REF) {
+    const int last_it = h->cg_iters.empty() ? 0 : h->cg_iters.back();
+    const bool due = h->pc_step < 0 ||
+                     (h->pc_refresh > 0 ? h->steps - h->pc_step >= h->pc_refresh
+                                        : (h->pc_base_iters >= 0 && last_it >= 2 * h->pc_base_iters &&
+                                           last_it >= h->pc_base_iters + 10));
+    if (due) {
+      if (!h->bmat) {
+        const int64_t n2 = (int64_t)h->nf * h->nf;
+        CK(h->alloc(&h->bmat, n2));
+        CK(h->alloc(&h->binv_cm, n2));
+        CK(h->alloc(&h->binv_rm, n2));
+      }
+      rc = assemble_schur(h);
+      if (rc != IB_OK) return rc;
+      rc = check_status(h);
+      if (rc != IB_OK) return rc;
+      h->pc_step = h->steps;
+      h->pc_base_iters = -1;
+      h->pc_assemblies++;
+    }
   }
   rc = cg_solve<S>(h);
   if (rc != IB_OK) return rc;
+  if (h->precond == IB_PC_SCHUR_REF && h->pc_base_iters < 0) h->pc_base_iters = h->cg_iters.back();
+  if (h->mlp && h->collect && hist2) CK(h->mlp->record(h->fb));
+  CK(cudaMemcpyAsync(h->fb_prev, h->fb_last, fbytes, cudaMemcpyDeviceToDevice, s));
   CK(enqueue_stress(h));
   CK(enqueue_project<S>(h, p));
   h->parity ^= 1;
@@ -910,9 +978,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
       AL(h->binv_rm, (int64_t)h->nf * h->nf);
     } else {
       AL(h->xb_body, 2 * nb); AL(h->vb, 2 * nb); AL(h->d_kin, 6 * h->nbodies); AL(h->body_of, nb);
-      AL(h->cg_r, h->nf); AL(h->cg_p, h->nf); AL(h->cg_Ap, h->nf); AL(h->cg_sc, 4); AL(h->fb_prev, h->nf);
+      AL(h->cg_r, h->nf); AL(h->cg_p, h->nf); AL(h->cg_Ap, h->nf); AL(h->cg_sc, 8); AL(h->fb_prev, h->nf);
+      AL(h->fb_last, h->nf); AL(h->cg_z, h->nf);
       AL(h->Gw, L * nG); AL(h->Pw, L * nG); AL(h->qw, g.nq); AL(h->rings_w, (int64_t)L * g.nbc);
-      if ((e = cudaMallocHost(&h->h_sc, sizeof(double) * 4)) != cudaSuccess) {
+      if ((e = cudaMallocHost(&h->h_sc, sizeof(double) * 8)) != cudaSuccess) {
         h->h_sc = nullptr;
         return bail(fail(h, IB_ERR_CUDA, "pinned CG scalars", e));
       }
@@ -1065,11 +1134,29 @@ int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv,
 }
 
 int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_start) {
-  if (!h || !(tol > 0) || maxiter < 1 || warm_start < IB_WARM_PREVIOUS || warm_start > IB_WARM_ZERO)
+  if (!h || !(tol > 0) || maxiter < 1 || warm_start < IB_WARM_PREVIOUS || warm_start > IB_WARM_LEARNED)
     return IB_ERR_INVALID;
   h->cg_tol = tol;
   h->cg_maxiter = maxiter;
   h->warm_start = warm_start;
+  return IB_OK;
+}
+
+int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps) {
+  if (!h || (mode != IB_PC_NONE && mode != IB_PC_SCHUR_REF) || refresh_steps < 0) return IB_ERR_INVALID;
+  if (mode != IB_PC_NONE && h->motion != IB_MOTION_PRESCRIBED)
+    return fail(h, IB_ERR_INVALID, "a CG preconditioner applies to moving bodies only");
+  h->precond = mode;
+  h->pc_refresh = refresh_steps;
+  h->pc_step = -1;
+  h->pc_base_iters = -1;
+  return IB_OK;
+}
+
+int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step) {
+  if (!h) return IB_ERR_INVALID;
+  if (assemblies) *assemblies = h->pc_assemblies;
+  if (last_step) *last_step = h->pc_step;
   return IB_OK;
 }
 
@@ -1409,7 +1496,7 @@ int ib_get_schur(ib_handle* h, double* bmat, double* binv) {
   OP_BEGIN();
   const size_t bytes = sizeof(double) * (size_t)h->nf * h->nf;
   if (h->nf == 0) return IB_OK;
-  if (!h->bmat) return fail(h, IB_ERR_INVALID, "no assembled Schur matrix for moving bodies");
+  if (!h->bmat) return fail(h, IB_ERR_INVALID, "no assembled Schur matrix (moving bodies without preconditioner)");
   if (bmat) CK(cudaMemcpyAsync(bmat, h->bmat, bytes, cudaMemcpyDeviceToHost, s));
   if (binv) CK(cudaMemcpyAsync(binv, h->binv_cm, bytes, cudaMemcpyDeviceToHost, s));
   OP_END();
@@ -1421,6 +1508,105 @@ int ib_get_reg(ib_handle* h, int32_t* body_idx, double* weight) {
   if (body_idx) CK(cudaMemcpyAsync(body_idx, h->body_idx, sizeof(int) * 2 * h->nb, cudaMemcpyDeviceToHost, s));
   if (weight) CK(cudaMemcpyAsync(weight, h->weight, sizeof(double) * h->nb * 2 * kWin2, cudaMemcpyDeviceToHost, s));
   OP_END();
+}
+
+// ------------------------------------------------------------------------------------------------
+// learned warm start (include/ibgb300_learn.h)
+// ------------------------------------------------------------------------------------------------
+int ib_learn_init(ib_handle* h, int32_t hidden, int32_t hidden_layers, int32_t capacity, uint64_t seed) {
+  if (!h) return IB_ERR_INVALID;
+  if (h->motion != IB_MOTION_PRESCRIBED || h->nf == 0)
+    return fail(h, IB_ERR_INVALID, "the learned warm start needs moving bodies");
+  if (hidden < 1 || hidden > 4096 || hidden_layers < 1 || hidden_layers > 8 || capacity < 2 || capacity > (1 << 20))
+    return fail(h, IB_ERR_INVALID, "network size or sample capacity out of range");
+  CK(cudaSetDevice(h->device));
+  delete h->mlp;
+  h->mlp = new learn::Mlp();
+  const int din = 6 * h->nbodies + 2 * h->nf;
+  cudaError_t e = h->mlp->init(din, h->nf, hidden, hidden_layers, capacity, seed, h->stream);
+  if (e != cudaSuccess) {
+    delete h->mlp;
+    h->mlp = nullptr;
+    return fail(h, IB_ERR_CUDA, "network allocation", e);
+  }
+  return IB_OK;
+}
+
+int ib_learn_collect(ib_handle* h, int32_t on) {
+  if (!h || !h->mlp) return h ? fail(h, IB_ERR_INVALID, "no network (ib_learn_init)") : IB_ERR_INVALID;
+  h->collect = on != 0;
+  return IB_OK;
+}
+
+int ib_learn_sample_count(ib_handle* h, int32_t* count) {
+  if (!h || !count) return IB_ERR_INVALID;
+  *count = h->mlp ? h->mlp->count : 0;
+  return IB_OK;
+}
+
+int ib_learn_train(ib_handle* h, int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss) {
+  if (!h || !h->mlp) return h ? fail(h, IB_ERR_INVALID, "no network (ib_learn_init)") : IB_ERR_INVALID;
+  if (epochs < 1 || batch < 1 || batch > learn::kMaxBatch || !(lr > 0))
+    return fail(h, IB_ERR_INVALID, "epochs, batch (1..512) and learning rate must be positive");
+  if (h->mlp->count < 2) return fail(h, IB_ERR_INVALID, "fewer than two recorded samples");
+  CK(cudaSetDevice(h->device));
+  cudaError_t e = h->mlp->train(epochs, batch, (float)lr, seed, final_loss);
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "training", e);
+  return IB_OK;
+}
+
+int ib_learn_validation(ib_handle* h, double* blend, double* rel_err) {
+  if (!h || !h->mlp) return IB_ERR_INVALID;
+  if (blend) *blend = h->mlp->blend;
+  if (rel_err) *rel_err = h->mlp->val_rel;
+  return IB_OK;
+}
+
+int ib_learn_layout(ib_handle* h, int32_t* nlayers, int32_t* dims, int32_t max_dims) {
+  if (!h || !h->mlp || !nlayers) return IB_ERR_INVALID;
+  *nlayers = h->mlp->nl;
+  if (dims)
+    for (int i = 0; i <= h->mlp->nl && i < max_dims; ++i) dims[i] = h->mlp->dims[i];
+  return IB_OK;
+}
+
+int ib_learn_param_count(ib_handle* h, int64_t* nparam) {
+  if (!h || !h->mlp || !nparam) return IB_ERR_INVALID;
+  *nparam = h->mlp->nparam;
+  return IB_OK;
+}
+
+int ib_learn_get_params(ib_handle* h, float* params) {
+  if (!h || !h->mlp || !params) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemcpyAsync(params, h->mlp->master, sizeof(float) * h->mlp->nparam, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return IB_OK;
+}
+
+int ib_learn_set_params(ib_handle* h, const float* params) {
+  if (!h || !h->mlp || !params) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  CK(cudaMemcpyAsync(h->mlp->master, params, sizeof(float) * h->mlp->nparam, cudaMemcpyHostToDevice, h->stream));
+  CK(h->mlp->sync_bf16());
+  CK(cudaStreamSynchronize(h->stream));
+  return IB_OK;
+}
+
+int ib_learn_gradients(ib_handle* h, int32_t rows, const float* x, const float* y, float* grad, double* loss) {
+  if (!h || !h->mlp || !x || !y || rows < 1 || rows > learn::kMaxBatch) return IB_ERR_INVALID;
+  CK(cudaSetDevice(h->device));
+  cudaError_t e = h->mlp->gradients(rows, x, y, grad, loss);
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "network gradients", e);
+  return IB_OK;
+}
+
+int ib_get_cg_start_residuals(ib_handle* h, int32_t count, double* r0) {
+  if (!h || count < 0 || count > (int32_t)h->cg_res0.size()) return IB_ERR_INVALID;
+  const size_t off = h->cg_res0.size() - (size_t)count;
+  for (int i = 0; i < count; ++i)
+    if (r0) r0[i] = h->cg_res0[off + i];
+  return IB_OK;
 }
 
 }  // extern "C"

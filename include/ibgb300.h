@@ -54,6 +54,8 @@ extern "C" {
 #define IB_WARM_PREVIOUS 0          /* previous step's Fb (cg! on qty.Fb, cnab/ops.jl:110) */
 #define IB_WARM_EXTRAPOLATE 1       /* 2 Fb(n-1) - Fb(n-2) */
 #define IB_WARM_ZERO 2              /* Fb = 0 (cold start, for comparisons) */
+#define IB_WARM_LEARNED 3           /* learned prediction (include/ibgb300_learn.h); extrapolation
+                                       until a network is trained */
 
 typedef struct ib_problem {
   /* MultiLevel(UniformGrid(h, (x0, x1), (y0, y1)), nlevels), src/fluids/fluids.jl:53-95 */
@@ -129,6 +131,19 @@ int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv,
 /* CG options (the reference hard-codes maxiter=5000, cnab/ops.jl:110): tolerance on
  * ||r|| / ||rhs||, iteration cap and IB_WARM_* warm start.  Defaults 1e-10, 5000, PREVIOUS. */
 int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_start);
+
+/* Preconditioner of the moving-body CG (no reference counterpart; the reference runs plain cg!):
+ * IB_PC_SCHUR_REF uses the inverse Schur matrix B_ref^-1 of a reference configuration (FP64,
+ * assembled on the device like the static Binv of cnab/ops.jl:79-96) as P in preconditioned CG.
+ * It is assembled at the next step, then again every `refresh_steps` steps, or, with
+ * refresh_steps = 0, whenever a solve needs twice (and at least 10 more) the iterations of the
+ * first solve after the last assembly.  The stopping rule ||r|| <= tol ||rhs|| is unchanged. */
+#define IB_PC_NONE 0
+#define IB_PC_SCHUR_REF 1
+int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps);
+
+/* number of preconditioner assemblies so far and the step of the last one (-1: none) */
+int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step);
 
 /* CG iterations and final relative residuals of the last `count` moving-body steps */
 int ib_get_cg_stats(ib_handle* h, int32_t count, int32_t* iterations, double* residuals);

@@ -1,0 +1,89 @@
+"""Learned warm start of the moving-body Schur CG (include/ibgb300_learn.h): the device
+network's loss and gradients against the float64 oracle, and what the trained network gains
+over linear extrapolation on steps it was not trained on."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+def heaving(ib, nx=128, ny=96, L=2, f=0.5, heave=0.25, pitch_deg=15.0, dt=0.005):
+    """A plate heaving and pitching at f (period 1/(f dt) = 400 steps); stable at this time step
+    (at f = 1 it needs dt = 0.0025: the explicit advection near the plate edges limits dt)."""
+    W = ib.workloads
+    frame = W.heave_pitch_frame(f=f, heave=heave, pitch_deg=pitch_deg)
+    base = W.Workload("heaving_test", 0.005, (-1.0, 2.84), (-1.28, 1.28), L, 200.0, dt, 10,
+                      [W.moving_plate(201, frame=frame)])
+    wl = W.scaled(base, nx, ny, nlevels=L, nsteps=10)
+    wl.Re = 200.0
+    wl.dt = dt
+    return wl
+
+
+def test_gradients_match_oracle(ib):
+    wl = heaving(ib)
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    s = ib.initsolver(prob, st)
+    s.learn_init(hidden=48, layers=3, capacity=16, seed=1)
+    dims = s.learn_layout()
+    assert dims[0] == 6 + 2 * 2 * s.nb and dims[-1] == 2 * s.nb and dims[1:-1] == [48, 48, 48]
+    rng = np.random.default_rng(7)
+    p = (0.3 * rng.standard_normal(s.learn_params().size)).astype(np.float32)
+    s.learn_params(p)
+    np.testing.assert_array_equal(s.learn_params(), p)
+    x = rng.standard_normal((37, dims[0])).astype(np.float32)
+    y = rng.standard_normal((37, dims[-1])).astype(np.float32)
+    loss, g = s.learn_gradients(x, y)
+    oloss, og = M.loss_and_grad(p, dims, x, y)
+    assert abs(loss - oloss) <= 1e-5 * oloss
+    off = 0
+    for l in range(len(dims) - 1):
+        for n in (dims[l] * dims[l + 1], dims[l + 1]):  # W_l then b_l
+            a, b = g[off: off + n], og[off: off + n]
+            assert np.linalg.norm(a - b) <= 1e-4 * np.linalg.norm(b), (l, n)
+            off += n
+    assert off == g.size
+    s.close()
+
+
+def run(ib, wl, warm, n_train, n_eval, train_kw):
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    s = ib.initsolver(prob, st)
+    s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+    s.learn_init(hidden=128, layers=3, capacity=1024, seed=0)
+    s.learn_collect(True)
+    for i in range(n_train):
+        ib.advance_(st, s, i * wl.dt)
+    loss = None
+    if warm == "learned":
+        loss = s.learn_train(**train_kw)
+        loss = (loss,) + s.learn_validation()
+        s.set_cg_options(tol=1e-10, warm_start="learned")
+    for i in range(n_train, n_train + n_eval):
+        ib.advance_(st, s, i * wl.dt)
+    it, res, r0 = s.cg_stats(n_eval, start=True)
+    samples = s.learn_samples()
+    s.close()
+    return it, res, r0, loss, samples
+
+
+def test_learned_warm_start_beats_extrapolation_on_held_out_steps(ib):
+    wl = heaving(ib)
+    n_train, n_eval = 500, 40
+    kw = dict(epochs=400, batch=32, lr=1e-3, seed=0)
+    it_e, res_e, r0_e, _, _ = run(ib, wl, "extrapolate", n_train, n_eval, kw)
+    it_l, res_l, r0_l, loss, samples = run(ib, wl, "learned", n_train, n_eval, kw)
+    assert samples == n_train + n_eval - 2  # recording continues while the network is used
+    # plain CG judges both: the same tolerance is reached on every step
+    assert np.all(res_e <= 1e-10) and np.all(res_l <= 1e-10)
+    print(f"loss {loss[0]:.3e} blend {loss[1]:.3f} held-out rel err {loss[2]:.3e}  "
+          f"r0 extrapolated {np.mean(r0_e):.3e}  learned {np.mean(r0_l):.3e}  "
+          f"iterations {it_e.sum()} -> {it_l.sum()}")
+    # the validated blend never makes the start worse than extrapolation on held-out rows
+    assert 0.0 <= loss[1] <= 1.0 and loss[2] <= 1.0
+    assert np.mean(r0_l) <= 1.05 * np.mean(r0_e)
+    assert it_l.sum() <= it_e.sum() * 1.01

@@ -201,3 +201,34 @@ def test_coarsify_get_bc_apply_bc_index_maps(O):
     r = np.zeros(g.gshape)
     O.apply_bc(r, bc, 2.0, g)
     assert r[0, 0] == pytest.approx(2.0 * (bc[g.B + 1] + bc[g.L + 1]))
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The network oracle's backward pass (float64, unrounded weights) against central
+    differences of its loss."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(3)
+    dims = [7, 5, 6, 4]
+    n = sum(dims[i] * dims[i + 1] + dims[i + 1] for i in range(len(dims) - 1))
+    p = rng.standard_normal(n) * 0.5
+    x = rng.standard_normal((9, dims[0]))
+    y = rng.standard_normal((9, dims[-1]))
+    loss, g = M.loss_and_grad(p, dims, x, y, bf16=False)
+    eps = 1e-6
+    fd = np.zeros(n)
+    for i in range(n):
+        e = np.zeros(n)
+        e[i] = eps
+        fd[i] = (M.loss_and_grad(p + e, dims, x, y, bf16=False)[0] - M.loss_and_grad(p - e, dims, x, y, bf16=False)[0]) / (2 * eps)
+    assert np.max(np.abs(fd - g)) < 1e-7 * max(1.0, np.max(np.abs(g)))
+    assert loss > 0
+
+
+def test_bf16_rounding_is_nearest_even():
+    from oracle import mlp_oracle as M
+    v = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 2 ** -7, 1.0 + 3 * 2 ** -8, -2.5, 3.0e-3], dtype=np.float32)
+    r = M.bf16_round(v)
+    assert r[0] == 1.0 and r[1] == 1.0 and r[2] == np.float32(1.0 + 2 ** -7)
+    assert r[3] == np.float32(1.0 + 2 ** -6)  # tie between 1+2^-7 and 1+2^-6 goes to the even mantissa
+    assert r[4] == -2.5
+    assert abs(r[5] - 3.0e-3) <= 2 ** -8 * 3.0e-3  # half an ulp of an 8-bit significand

@@ -78,8 +78,99 @@ class Dist:
 def make_workload(ib, name: str):
     w = ib.workloads
     table = {"two_body_large": w.two_body_large, "cylinder_small": w.cylinder_small,
-             "four_cylinders": w.four_cylinders}
+             "four_cylinders": w.four_cylinders, "heaving_plate": w.heaving_plate}
     return table[name]()
+
+
+# ----------------------------------------------------------------------------------------------
+# moving bodies: the plain FP64 GPU path (the reference's algorithm: cg! from the previous Fb, no
+# preconditioner) against mixed precision + Schur-preconditioned CG + learned warm start
+# ----------------------------------------------------------------------------------------------
+def moving_arm(ib, wl, precision, pc, warm, n, timed_from, learn=None):
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = wl.initial_gamma()
+    s = ib.initsolver(prob, st, precision=precision)
+    s.set_cg_options(tol=1e-10, warm_start="extrapolate" if warm == "learned" else warm)
+    s.set_cg_preconditioner(pc)
+    s.vort2flux(st)
+    info = {}
+    if learn:
+        s.learn_init(hidden=256, layers=3, capacity=4096, seed=0)
+        s.learn_collect(True)
+    cd, cl = [], []
+    t0 = None
+    for i in range(n):
+        if learn and i == learn["train_at"]:
+            s.lib.ib_synchronize(s.handle)
+            a = time.perf_counter()
+            loss = s.learn_train(epochs=learn["epochs"], batch=64, lr=1e-3, seed=0)
+            blend, rel = s.learn_validation()
+            info = {"train_samples": s.learn_samples(), "train_loss": loss, "blend": blend,
+                    "held_out_rel_err_vs_extrapolation": rel, "train_s": time.perf_counter() - a}
+            s.set_cg_options(tol=1e-10, warm_start="learned")
+        if i == timed_from:
+            s.lib.ib_synchronize(s.handle)
+            t0 = time.perf_counter()
+        ib.advance_(st, s, i * wl.dt)
+        cd.append([b.CD for b in st.qty.stress])
+        cl.append([b.CL for b in st.qty.stress])
+    s.lib.ib_synchronize(s.handle)
+    sec = (time.perf_counter() - t0) / (n - timed_from)
+    it, res, r0 = s.cg_stats(n, start=True)
+    pcs = s.cg_preconditioner_stats()
+    s.close()
+    return dict(sec=sec, it=it, res=res, r0=r0, cd=np.array(cd), cl=np.array(cl), learn=info, pc=pcs)
+
+
+def run_moving_config(ib, wl, quick=False):
+    n_plain = 6 if quick else 12
+    plain = moving_arm(ib, wl, "fp64", "none", "previous", n_plain, 2)
+    n_train, n_eval = (60, 20) if quick else (300, 60)
+    ours = moving_arm(ib, wl, "mixed", "schur_ref", "learned", n_train + n_eval, n_train,
+                      learn={"train_at": n_train, "epochs": 200})
+    extrap = moving_arm(ib, wl, "mixed", "schur_ref", "extrapolate", n_train + n_eval, n_train)
+    m = min(n_plain, len(ours["cd"]))
+    err = float(max(np.max(np.abs(ours["cd"][:m] - plain["cd"][:m]) / np.maximum(1, np.abs(plain["cd"][:m]))),
+                    np.max(np.abs(ours["cl"][:m] - plain["cl"][:m]) / np.maximum(1, np.abs(plain["cl"][:m])))))
+    cells = wl.cells_per_step
+    ev = slice(n_train, n_train + n_eval)
+    return {
+        "workload": describe(wl) + " (moving: heave 0.5 sin(2 pi f t), pitch 30 deg, f=0.2)",
+        "value": cells / ours["sec"], "unit": "cell-steps/s", "ms_per_step": ours["sec"] * 1e3,
+        "arm": "mixed precision + Schur-preconditioned CG + learned warm start",
+        "plain_fp64": {"value": cells / plain["sec"], "ms_per_step": plain["sec"] * 1e3,
+                       "arm": "FP64, CG from the previous Fb, no preconditioner (the reference's algorithm)",
+                       "steps_timed": n_plain - 2},
+        "speedup_vs_plain_fp64": plain["sec"] / ours["sec"],
+        "cg_iterations_per_step": {"plain_fp64": float(np.mean(plain["it"][2:])),
+                                   "ours_learned": float(np.mean(ours["it"][ev])),
+                                   "ours_extrapolated": float(np.mean(extrap["it"][ev]))},
+        "cg_start_residual_mean": {"learned": float(np.mean(ours["r0"][ev])),
+                                   "extrapolated": float(np.mean(extrap["r0"][ev]))},
+        "cg_final_residual_max": float(max(ours["res"].max(), plain["res"].max())),
+        "max_cl_cd_err_vs_fp64": err,
+        "err_note": f"first {m} steps, |C - C_plain_fp64| / max(1, |C_plain_fp64|), both CG to 1e-10",
+        "learned": dict(ours["learn"], eval_steps=n_eval,
+                        note="trained on the run's own steps 2..%d, evaluated on the next %d; blend 0 means the "
+                             "validated network correction fell back to extrapolation" % (n_train - 1, n_eval)),
+        "preconditioner_assemblies": ours["pc"][0],
+        "timed_steps": n_eval,
+    }
+
+
+def run_static_config(ib, lib, L, wl, K, W, local, dist):
+    arm = run_arm(ib, lib, L, wl, "mixed", K, W, local, dist)
+    ref = run_arm(ib, lib, L, wl, "fp64", K, W, local, dist)
+    t, t64 = arm["dev_s"], ref["dev_s"]
+    err = max(float(np.max(np.abs(arm["cd"] - ref["cd"]) / np.maximum(1.0, np.abs(ref["cd"])))),
+              float(np.max(np.abs(arm["cl"] - ref["cl"]) / np.maximum(1.0, np.abs(ref["cl"])))))
+    out = {"workload": describe(wl), "value": wl.cells_per_step * K / t, "unit": "cell-steps/s",
+           "ms_per_step": t / K * 1e3, "plain_fp64": {"value": wl.cells_per_step * K / t64, "ms_per_step": t64 / K * 1e3},
+           "speedup_vs_plain_fp64": t64 / t, "max_cl_cd_err_vs_fp64": err, "steps": K}
+    arm["solver"].close()
+    ref["solver"].close()
+    return out
 
 
 def describe(wl) -> str:
@@ -341,6 +432,12 @@ def run_ours(args, rank, world, local):
                   "h2d_bytes_per_step": 8 * 2 * wl.nlevels,
                   "d2h_bytes_per_step": 4 * 3 + 8 * 2 * solver.nbodies + 8 * 2 * nb,
                   "api": "solve_(state, prob, (t0, tf); save=(each_timestep(C_D, C_L),)) per-step advance!"}
+    # the other benchmark configurations, one summary each (single-GPU runs; --no-configs skips)
+    if world == 1 and not args.no_configs:
+        out["configs"] = {
+            "four_cylinders": run_static_config(ib, lib, L, ib.workloads.four_cylinders(), 60, 3, local, dist),
+            "heaving_plate": run_moving_config(ib, ib.workloads.heaving_plate()),
+        }
     if rank == 0 and not args.no_cpu_baseline:
         v, sec, cores = cpu_reference(ib, wl, args.cpu_steps, 1)
         out["cpu_baseline"] = {"value": v, "unit": "cell-steps/s", "cores": cores, "kind": "port",
@@ -384,6 +481,8 @@ def main():
     ap.add_argument("--workload", default="two_body_large")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the per-configuration summaries (2048^2 four cylinders, moving plate)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
                     help="arithmetic of the timed arm (mixed: FP32 transforms + FP64 residual refinement)")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip timing the FP64 GPU path beside it")

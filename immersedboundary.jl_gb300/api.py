@@ -509,7 +509,7 @@ class Solver:
     def set_cg_preconditioner(self, mode: str = "schur_ref", refresh_steps: int = 0):
         """``"none"`` (plain CG, the reference's) or ``"schur_ref"``: PCG with the inverse Schur
         matrix of a reference configuration, re-assembled every ``refresh_steps`` steps or, with 0,
-        when the iterations have doubled since the last assembly."""
+        once the extra iterations since the last assembly have cost as much time as an assembly."""
         m = {"none": _lib.IB_PC_NONE, "schur_ref": _lib.IB_PC_SCHUR_REF}[mode]
         self._check(self.lib.ib_set_cg_preconditioner(self.handle, m, int(refresh_steps)))
 

@@ -44,7 +44,8 @@ __device__ __forceinline__ df64 two_prod(float a, float b) {
   return df64(p, fmaf(a, b, -p));
 }
 
-__device__ __forceinline__ df64 operator+(df64 a, df64 b) {
+// accurate sum (error relative to the result, also under cancellation)
+__device__ __forceinline__ df64 add_accurate(df64 a, df64 b) {
   df64 s = two_sum(a.hi, b.hi);
   const df64 t = two_sum(a.lo, b.lo);
   s.lo += t.hi;
@@ -52,23 +53,23 @@ __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
   s.lo += t.lo;
   return fast_two_sum(s.hi, s.lo);
 }
+// Dekker's add: error below 2 ulp of max(|a|, |b|) in the float-float sense, i.e. about 2^-46
+// relative to the larger operand (not to the sum); enough wherever the sum's absolute error
+// is what matters, which is every use in this library (the arithmetic operators use it).
+__device__ __forceinline__ df64 add_sloppy(df64 a, df64 b) {
+  df64 s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df64 operator+(df64 a, df64 b) { return add_sloppy(a, b); }
 __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
-__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
+__device__ __forceinline__ df64 operator-(df64 a, df64 b) { return add_sloppy(a, -b); }
 __device__ __forceinline__ df64 operator*(df64 a, df64 b) {
   df64 p = two_prod(a.hi, b.hi);
   p.lo = fmaf(a.hi, b.lo, p.lo);
   p.lo = fmaf(a.lo, b.hi, p.lo);
   return fast_two_sum(p.hi, p.lo);
 }
-// Dekker's add: error below 2 ulp of max(|a|, |b|) in the float-float sense, i.e. about 2^-46
-// relative to the larger operand (not to the sum); enough wherever the sum's absolute error
-// is what matters.
-__device__ __forceinline__ df64 add_sloppy(df64 a, df64 b) {
-  df64 s = two_sum(a.hi, b.hi);
-  s.lo += a.lo + b.lo;
-  return fast_two_sum(s.hi, s.lo);
-}
-
 // 4 c - (w + e + s + n) of five floats, to float-float accuracy: the neighbour sum is formed
 // with error-free sums (its three small parts add up in float with an error ~2^-48 of the
 // sum), the difference with the exactly scaled centre with one more error-free sum.

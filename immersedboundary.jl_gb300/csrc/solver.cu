@@ -103,6 +103,9 @@ struct ib_handle {
   int pc_base_iters = -1;                         // iterations of the first solve after an assembly
   int64_t pc_step = -1;                           // step of the last assembly
   int pc_assemblies = 0;
+  double pc_assembly_s = 0.0;                     // measured duration of the last assembly
+  double pc_excess_iters = 0.0;                   // iterations above the base since then
+  double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
   double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
   double* h_sc = nullptr;  // pinned CG scalars read back each iteration
   double cg_tol = 1e-10;
@@ -671,6 +674,7 @@ int cg_solve(ib_handle* h) {
   h->cg_res0.push_back(h->h_sc[3] > 0 ? rn / std::sqrt(h->h_sc[3]) : rn);
   int it = 0;
   bool conv = rn <= target;
+  const auto t_loop = std::chrono::steady_clock::now();
   while (!conv && it < h->cg_maxiter) {
     ++it;
     CK(schur_apply<S>(h, p, Ap));
@@ -691,6 +695,10 @@ int cg_solve(ib_handle* h) {
       }
       CK(cg_update_p(p, z, sc, nf, s));
     }
+  }
+  if (it > 0) {
+    const double per = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_loop).count() / it;
+    h->cg_iter_s = h->cg_iter_s > 0.0 ? 0.9 * h->cg_iter_s + 0.1 * per : per;
   }
   h->cg_iters.push_back(it);
   h->cg_res.push_back(h->h_sc[3] > 0 ? rn / std::sqrt(h->h_sc[3]) : rn);
@@ -736,15 +744,14 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
     default: break;
   }
   // preconditioner: the inverse Schur matrix of the current configuration, assembled at the first
-  // step and again every pc_refresh steps, or (pc_refresh = 0) when the iterations have grown to
-  // twice (and 10 more than) those right after the last assembly
+  // step and again every pc_refresh steps, or (pc_refresh = 0) once the iterations spent above
+  // those of the first solve after the last assembly have cost as much time as an assembly
   if (h->precond == IB_PC_SCHUR_REF) {
-    const int last_it = h->cg_iters.empty() ? 0 : h->cg_iters.back();
     const bool due = h->pc_step < 0 ||
                      (h->pc_refresh > 0 ? h->steps - h->pc_step >= h->pc_refresh
-                                        : (h->pc_base_iters >= 0 && last_it >= 2 * h->pc_base_iters &&
-                                           last_it >= h->pc_base_iters + 10));
+                                        : h->pc_excess_iters * h->cg_iter_s >= h->pc_assembly_s);
     if (due) {
+      const auto t_asm = std::chrono::steady_clock::now();
       if (!h->bmat) {
         const int64_t n2 = (int64_t)h->nf * h->nf;
         CK(h->alloc(&h->bmat, n2));
@@ -757,12 +764,20 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
       if (rc != IB_OK) return rc;
       h->pc_step = h->steps;
       h->pc_base_iters = -1;
+      h->pc_excess_iters = 0.0;
       h->pc_assemblies++;
+      h->pc_assembly_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_asm).count();
     }
   }
   rc = cg_solve<S>(h);
   if (rc != IB_OK) return rc;
-  if (h->precond == IB_PC_SCHUR_REF && h->pc_base_iters < 0) h->pc_base_iters = h->cg_iters.back();
+  if (h->precond == IB_PC_SCHUR_REF) {
+    // the first solve after an assembly starts at the previous Fb of a changed matrix; the
+    // second one sets the base
+    const int it_now = h->cg_iters.back();
+    if (h->pc_base_iters < 0 && h->steps > h->pc_step) h->pc_base_iters = it_now;
+    else if (h->pc_base_iters >= 0) h->pc_excess_iters += std::max(0, it_now - h->pc_base_iters);
+  }
   if (h->mlp && h->collect && hist2) CK(h->mlp->record(h->fb));
   CK(cudaMemcpyAsync(h->fb_prev, h->fb_last, fbytes, cudaMemcpyDeviceToDevice, s));
   CK(enqueue_stress(h));

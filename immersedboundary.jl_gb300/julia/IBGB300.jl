@@ -19,11 +19,18 @@ using ImmersedBoundary.StreamFcn
 using ImmersedBoundary.StreamFcn: StreamFcnGrid, BodyStress
 using ImmersedBoundary.Fluids: baselevel, nlevels, xycoords, gridstep
 using ImmersedBoundary.Bodies: npoints
+using ImmersedBoundary.Dynamics: GridFrame, RelativeFrame
 
 const libibgb300 = joinpath(@__DIR__, "..", "libibgb300.so")
 
 const IB_PREC_FP64 = Int32(0)
 const IB_PREC_MIXED = Int32(1)
+const IB_MOTION_STATIC = Int32(0)
+const IB_MOTION_PRESCRIBED = Int32(1)
+const IB_PC_SCHUR_REF = Int32(1)
+
+# bodies moving in the grid frame (RigidBody{RelativeFrame}) use ib_advance_kin
+moving(bodies) = any(b -> b.frame isa RelativeFrame, bodies)
 
 # mirrors `ib_problem` (natural C alignment; all fields isbits)
 struct IbProblem
@@ -65,11 +72,13 @@ mutable struct GB300Solver{P<:Problem} <: AbstractSolver
     prob::P
     handle::Ptr{Cvoid}
     sync::Symbol   # :all (copy state.qty back every step) or :stress (forces only)
+    moving::Bool
+    kin::Vector{Float64}
 end
 
 ImmersedBoundary.problemof(s::GB300Solver) = s.prob
 
-function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, sync=:all)
+function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, sync=:all, precondition=true)
     fluid = fluidof(prob)
     grid = discretize(fluid)
     base = baselevel(grid)
@@ -79,17 +88,22 @@ function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, syn
     xb = vcat((b.xb for b in bodies)...)          # nb x 2, column-major
     ds = vcat((b.ds for b in bodies)...)
     scheme = schemeof(prob)
+    mv = moving(bodies)
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve npts xb ds begin
         p = IbProblem(fluid.domain.nx, fluid.domain.ny, nlevels(grid), first(xs), first(ys),
                       gridstep(base), scheme.dt, scheme.β[1], scheme.β[2], fluid.Re,
-                      length(npts), pointer(npts), pointer(xb), pointer(ds), 0, precision,
-                      device, 4096, 0)
+                      length(npts), pointer(npts), pointer(xb), pointer(ds),
+                      mv ? IB_MOTION_PRESCRIBED : IB_MOTION_STATIC, precision, device, 4096, 0)
         st = ccall((:ib_create, libibgb300), Cint, (Ref{IbProblem}, Ref{Ptr{Cvoid}}), p, handle)
         check(st, C_NULL)
     end
-    s = GB300Solver(prob, handle[], sync)
+    s = GB300Solver(prob, handle[], sync, mv, zeros(6 * length(npts)))
     finalizer(x -> ccall((:ib_destroy, libibgb300), Cint, (Ptr{Cvoid},), x.handle), s)
+    if mv && precondition
+        check(ccall((:ib_set_cg_preconditioner, libibgb300), Cint, (Ptr{Cvoid}, Int32, Int32),
+                    s.handle, IB_PC_SCHUR_REF, 0), s.handle)
+    end
     push_state!(s, state)
     return s
 end
@@ -136,8 +150,19 @@ end
 "`advance!(state, solver, t)`: src/streamfcn/cnab/timestepping.jl:253-290 on the GPU."
 function ImmersedBoundary.advance!(state, solver::GB300Solver, t::Float64)
     u, v = fluidof(solver.prob).freestream(t)
-    st = ccall((:ib_advance, libibgb300), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble),
-               solver.handle, t, u, v)
+    st = if solver.moving
+        # update_bodies! (src/bodies/body-points.jl:52-68): the frame closures at t, per body
+        for (k, b) in enumerate(bodygroup(solver.prob))
+            f = b.frame
+            r, vel, θ, Ω = f isa RelativeFrame ? (f.r(t), f.v(t), f.θ(t), f.Ω(t)) : ((0.0, 0.0), (0.0, 0.0), 0.0, 0.0)
+            solver.kin[6k-5:6k] .= (r[1], r[2], vel[1], vel[2], θ, Ω)
+        end
+        ccall((:ib_advance_kin, libibgb300), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble, Ptr{Float64}),
+              solver.handle, t, u, v, solver.kin)
+    else
+        ccall((:ib_advance, libibgb300), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble),
+              solver.handle, t, u, v)
+    end
     check(st, solver.handle)
     solver.sync === :all && pull_state!(solver, state)
     pull_stress!(solver, state)

@@ -136,8 +136,9 @@ int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_st
  * IB_PC_SCHUR_REF uses the inverse Schur matrix B_ref^-1 of a reference configuration (FP64,
  * assembled on the device like the static Binv of cnab/ops.jl:79-96) as P in preconditioned CG.
  * It is assembled at the next step, then again every `refresh_steps` steps, or, with
- * refresh_steps = 0, whenever a solve needs twice (and at least 10 more) the iterations of the
- * first solve after the last assembly.  The stopping rule ||r|| <= tol ||rhs|| is unchanged. */
+ * refresh_steps = 0, once the CG iterations spent above those of the solve after the last
+ * assembly have taken as long as that assembly (both timed on the host).  The stopping rule
+ * ||r|| <= tol ||rhs|| is unchanged. */
 #define IB_PC_NONE 0
 #define IB_PC_SCHUR_REF 1
 int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps);

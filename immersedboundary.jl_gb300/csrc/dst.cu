@@ -22,6 +22,7 @@
 #include "fft_small.cuh"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -449,34 +450,44 @@ cudaError_t AxisTables<T>::build(int n) {
     post[k] = mk<V>((T)cosl(ang), (T)sinl(ang));
   }
   for (int j = 0; j <= n / 2; ++j) sn[j] = (T)sinl(pi * (long double)j / (long double)n);
-  // lane-ordered tables of the warp-per-line transforms
-  const int P = warp_p(n);
+  // lane-ordered tables of the line-parallel transforms: one warp per line.  Two warps per line
+  // (IBGB300_LINE_LANES=64; M = 64 P with P = 2..16 so the cross-lane stage stays inside a
+  // warp) halve each lane's work but measured slower on GB300 (1024^2 mixed step 1.53 vs
+  // 1.48 ms, 2048^2 6.46 vs 5.75 ms): the pair's named barriers cost more than they save.
+  int P = warp_p(n), NL = 32;
+  const char* lanes_env = std::getenv("IBGB300_LINE_LANES");
+  const bool two_warps = lanes_env && std::strcmp(lanes_env, "64") == 0;
+  if (P && two_warps && M % 64 == 0 && (M / 64 == 2 || M / 64 == 4 || M / 64 == 8 || M / 64 == 16)) {
+    NL = 64;
+    P = M / 64;
+  }
   d.wP = P;
-  const int G = !P ? 1 : (32 % P == 0 ? 32 / P : 32);
+  d.wNL = NL;
+  const int G = !P ? 1 : (NL % P == 0 ? NL / P : 32);
   int lg = 0;
   while ((1 << lg) < G) ++lg;
-  std::vector<V> w1((size_t)P * 32), w2((size_t)P * 32), w3((size_t)(lg > 0 ? lg : 1) * 32), ws((size_t)P * 32);
+  std::vector<V> w1((size_t)P * NL), w2((size_t)P * NL), w3((size_t)(lg > 0 ? lg : 1) * NL), ws((size_t)P * NL);
   auto cis = [&](long double num, long double den) {  // e^{-2 pi i num / den}
     const long double ang = -2.0L * pi * num / den;
     return mk<V>((T)cosl(ang), (T)sinl(ang));
   };
   for (int a = 0; a < P; ++a)
-    for (int l = 0; l < 32; ++l) {
-      w1[a * 32 + l] = cis((long double)(l * a), (long double)M);
-      w2[a * 32 + l] = cis((long double)((l % G) * a), 32.0L);
-      const int m = l + 32 * a;
-      ws[a * 32 + l] = mk<V>((T)sinl(pi * (long double)(2 * m) / (long double)n),
+    for (int l = 0; l < NL; ++l) {
+      w1[a * NL + l] = cis((long double)(l * a), (long double)M);
+      w2[a * NL + l] = cis((long double)((l % G) * a), (long double)NL);
+      const int m = l + NL * a;
+      ws[a * NL + l] = mk<V>((T)sinl(pi * (long double)(2 * m) / (long double)n),
                              (T)sinl(pi * (long double)(2 * m + 1) / (long double)n));
     }
   for (int s = 0; s < lg; ++s) {
     const int h = G >> (s + 1);
-    for (int l = 0; l < 32; ++l) {
+    for (int l = 0; l < NL; ++l) {
       const int j = (l % G) % (2 * h);
-      w3[s * 32 + l] = j >= h ? cis((long double)(j - h), (long double)(2 * h)) : mk<V>((T)1, (T)0);
+      w3[s * NL + l] = j >= h ? cis((long double)(j - h), (long double)(2 * h)) : mk<V>((T)1, (T)0);
     }
   }
   const size_t b_tw = tw.size() * sizeof(V), b_post = post.size() * sizeof(V), b_sn = sn.size() * sizeof(T);
-  const size_t b_w = (size_t)P * 32 * sizeof(V), b_w3 = w3.size() * sizeof(V);
+  const size_t b_w = (size_t)P * NL * sizeof(V), b_w3 = w3.size() * sizeof(V);
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t o_post = up(b_tw);
   const size_t o_sn = o_post + up(b_post);

@@ -27,7 +27,14 @@ namespace ib {
 namespace wdst {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kWarps = 4;  // lines (warps) per block
+constexpr int kLines = 4;  // lines per block
+
+// (lanes per line, values per lane) pairs with compiled passes: one warp per line, or two
+// (IBGB300_LINE_LANES=64, axes with M = 64 P, P = 2..16)
+#define IB_WDST_COMBOS(X) \
+  X(32, 1) X(32, 2) X(32, 3) X(32, 4) X(32, 6) X(32, 8) X(32, 12) X(32, 16) X(32, 24) X(32, 32) \
+  X(64, 2) X(64, 4) X(64, 8) X(64, 16)
+constexpr int kLB = 8;     // loads in flight per lane in the line copies
 
 // cos(2 pi t / 96) for t = 0..24 (a quarter period); the rest by symmetry.  96 = lcm of the
 // in-lane transform sizes 2^k and 3 2^k (k <= 5).
@@ -122,72 +129,88 @@ template <typename T> struct LaneDft<T, 24> {
 
 constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x / 2); }
 
-// Shared-memory shape of one line (in elements of T).
-template <typename T, int P>
+// Synchronisation of the NL threads of one line: the warp itself, or (two warps) a named
+// barrier of the line (ids 1.. kLines; 0 is __syncthreads).
+template <int NL>
+__device__ __forceinline__ void line_sync(int bar) {
+  if constexpr (NL == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(NL) : "memory");
+  }
+}
+
+// Shared-memory shape of one line of NL lanes (NL = 32: one warp, 64: two warps), in elements.
+template <typename T, int P, int NL>
 struct Shape {
-  // P dividing 32: transpose + G = 32 / P lanes per sub-transform.  P = 3 2^k: no transpose,
-  // the second factor is a 32-point transform across all lanes (G = 32, shuffles only).
-  static constexpr bool kShuffle = (32 % P) != 0;
-  static constexpr int M = 32 * P, N = 2 * M, G = kShuffle ? 32 : 32 / P, S = 32 + G, LG = ilog2(G);
-  // line / transpose / natural-order spectrum share one buffer: max(n + 1, 2 P S) = n + 64
-  static constexpr int kU = N + 64;
-  // prefix-sum workspace, chunk of P padded by one: index k + k / P
-  static constexpr int kD = M + 32;
-  // per-line stride: 16-byte aligned and 32 / kWarps (mod 32) words apart, so that the lines
+  // P dividing NL: transpose + G = NL / P lanes per sub-transform (G <= 32, inside a warp).
+  // P = 3 2^k (NL = 32 only): no transpose, the second factor is a 32-point transform across
+  // all lanes (shuffles only).
+  static constexpr bool kShuffle = (NL % P) != 0;
+  static_assert(!kShuffle || NL == 32, "3 2^k lines use one warp");
+  static constexpr int M = NL * P, N = 2 * M, G = kShuffle ? 32 : NL / P, S = NL + G, LG = ilog2(G);
+  static_assert(G <= 32, "cross-lane stage must stay inside a warp");
+  // line / transpose / natural-order spectrum share one buffer: max(n + 1, 2 P S) = n + 2 NL
+  static constexpr int kU = N + 2 * NL;
+  // prefix-sum workspace, chunk of P padded by one (index k + k / P), plus the warp-total slot
+  static constexpr int kD = M + NL + 4;
+  // per-line stride: 16-byte aligned and 32 / kLines (mod 32) words apart, so that the lines
   // of a block sit in different banks for the column-wise (transposing) copies
   static constexpr int words = (int)(sizeof(T) / 4);
   static constexpr int stride_from(int s) {
-    return ((s * words) % 32 == 32 / kWarps && (s * (int)sizeof(T)) % 16 == 0) ? s : stride_from(s + 1);
+    return ((s * words) % 32 == 32 / kLines && (s * (int)sizeof(T)) % 16 == 0) ? s : stride_from(s + 1);
   }
   static constexpr int kStride = stride_from(kU + kD);
 };
 
-// In-place DST-I (F convention) of U[1..n-1] by the 32 lanes of a warp; U[0] and U[n] are read
-// as zero.  U: Shape::kU elements, D: Shape::kD, both private to the warp.
-template <typename T, int P>
-__device__ __forceinline__ void warp_dst(T* U, T* D, const DstAxis<T>& ax, int lane) {
+// In-place DST-I (F convention) of U[1..n-1] by the NL threads of a line (lane = 0..NL-1, bar
+// = the line's barrier id); U[0] and U[n] are read as zero.  U: Shape::kU elements, D:
+// Shape::kD, both private to the line.
+template <typename T, int P, int NL>
+__device__ __forceinline__ void line_dst(T* U, T* D, const DstAxis<T>& ax, int lane, int bar) {
   using V = c2_t<T>;
-  using Sh = Shape<T, P>;
+  using Sh = Shape<T, P, NL>;
   constexpr int M = Sh::M, N = Sh::N, G = Sh::G, S = Sh::S;
+  const int wl = lane & 31;  // lane within its warp
   V z[P];
   // 1. u_j = sin(pi j/n)(y_j + y_{n-j}) + (y_j - y_{n-j})/2, paired into complex points
 #pragma unroll
   for (int r = 0; r < P; ++r) {
-    const int m = lane + 32 * r;
+    const int m = lane + NL * r;
     const int j0 = 2 * m, j1 = j0 + 1;
     const T a0 = j0 ? U[j0] : T(0);
     const T b0 = j0 ? U[N - j0] : T(0);
     const T a1 = U[j1], b1 = U[N - j1];
-    const V sn = __ldg(&ax.wsn[r * 32 + lane]);
+    const V sn = __ldg(&ax.wsn[r * NL + lane]);
     z[r] = mk<V>(fmaT(sn.x, a0 + b0, T(0.5) * (a0 - b0)), fmaT(sn.y, a1 + b1, T(0.5) * (a1 - b1)));
   }
-  __syncwarp();
+  line_sync<NL>(bar);
   // 2. DFT_P over r, twiddle, transpose
   LaneDft<T, P>::run(z);
 #pragma unroll
-  for (int a = 1; a < P; ++a) z[a] = cmul(z[a], __ldg(&ax.wtw1[a * 32 + lane]));
+  for (int a = 1; a < P; ++a) z[a] = cmul(z[a], __ldg(&ax.wtw1[a * NL + lane]));
   V* X = reinterpret_cast<V*>(U);
   // P = 3 2^k: the sub-transform index stays a = c, one group of 32 lanes
   const int ap = Sh::kShuffle ? 0 : lane / G, g = Sh::kShuffle ? lane : lane % G;
   if constexpr (!Sh::kShuffle) {
 #pragma unroll
     for (int a = 0; a < P; ++a) X[a * S + lane] = z[a];
-    __syncwarp();
+    line_sync<NL>(bar);
 #pragma unroll
     for (int i = 0; i < P; ++i) z[i] = X[ap * S + g + G * i];
     // 3. DFT_P over i, twiddle
     LaneDft<T, P>::run(z);
 #pragma unroll
     for (int c = 1; c < P; ++c)
-      if (G > 1) z[c] = cmul(z[c], __ldg(&ax.wtw2[c * 32 + lane]));
+      if (G > 1) z[c] = cmul(z[c], __ldg(&ax.wtw2[c * NL + lane]));
   }
-  // DFT_G across the group
+  // DFT_G across the group (its G lanes are consecutive inside one warp)
   if (G > 1) {
 #pragma unroll
     for (int s = 0; s < Sh::LG; ++s) {
       const int h = G >> (s + 1);
       const bool upper = (lane & h) != 0;
-      const V w = __ldg(&ax.wtw3[s * 32 + lane]);
+      const V w = __ldg(&ax.wtw3[s * NL + lane]);
 #pragma unroll
       for (int c = 0; c < P; ++c) {
         V p;
@@ -198,7 +221,7 @@ __device__ __forceinline__ void warp_dst(T* U, T* D, const DstAxis<T>& ax, int l
     }
   }
   const int d = (G > 1) ? (int)(__brev((unsigned)g) >> (32 - Sh::LG)) : 0;
-  __syncwarp();
+  line_sync<NL>(bar);
   // 4. natural order, real split (pairs k, M-k), prefix sum
   if constexpr (Sh::kShuffle) {
 #pragma unroll
@@ -207,12 +230,12 @@ __device__ __forceinline__ void warp_dst(T* U, T* D, const DstAxis<T>& ax, int l
 #pragma unroll
     for (int c = 0; c < P; ++c) X[ap + P * c + P * P * d] = z[c];
   }
-  __syncwarp();
+  line_sync<NL>(bar);
   T* L = U;
 #pragma unroll
   for (int t = 0; t < (P + 1) / 2; ++t) {
-    const int k = lane + 32 * t;
-    if (2 * k >= M) break;  // P == 1: lanes 16..31 have no pair
+    const int k = lane + NL * t;
+    if (2 * k >= M) break;  // P == 1: lanes NL/2.. have no pair
     const V zk = X[k];
     if (k == 0) {
       D[0] = T(0.5) * (zk.x + zk.y);  // D_0 / 2
@@ -233,9 +256,9 @@ __device__ __forceinline__ void warp_dst(T* U, T* D, const DstAxis<T>& ax, int l
     L[M] = zh.y;                      // F_M
     D[M / 2 + (M / 2) / P] = zh.x;
   }
-  __syncwarp();
+  line_sync<NL>(bar);
   // F_{2k+1} = D_0/2 + D_1 + ... + D_k: compensated chunk sums (chunk = P values per lane),
-  // scan of the chunk totals across the warp
+  // scan of the chunk totals across the warp (and across the pair of warps)
   T cs[P];
   T acc = T(0), comp = T(0);
 #pragma unroll
@@ -250,20 +273,29 @@ __device__ __forceinline__ void warp_dst(T* U, T* D, const DstAxis<T>& ax, int l
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
     const T v = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += v;
+    if (wl >= o) incl += v;
   }
   T excl = __shfl_up_sync(kFull, incl, 1);
-  if (lane == 0) excl = T(0);
+  if (wl == 0) excl = T(0);
+  if constexpr (NL == 64) {
+    T* wtot = D + Sh::kD - 2;
+    if (lane == 31) wtot[0] = incl;
+    line_sync<NL>(bar);
+    if (lane >= 32) excl += wtot[0];
+  }
 #pragma unroll
   for (int i = 0; i < P; ++i) D[lane * (P + 1) + i] = cs[i] + excl;
-  __syncwarp();
+  line_sync<NL>(bar);
 #pragma unroll
   for (int t = 0; t < P; ++t) {
-    const int k = lane + 32 * t;
+    const int k = lane + NL * t;
     L[2 * k + 1] = D[k + k / P];
   }
-  __syncwarp();
+  line_sync<NL>(bar);
 }
+
+// lanes per line for an axis with warp-per-line tables (the tables are built for this width)
+template <typename T> __host__ __device__ inline int line_lanes(const DstAxis<T>& ax) { return ax.wNL; }
 
 }  // namespace wdst
 }  // namespace ib

@@ -1,37 +1,42 @@
-// Warp-per-line x passes (see dstw.cuh): the first and last pass of every Poisson / CN solve
+// Line-parallel x passes (see dstw.cuh), kernels and launchers shared by dstw_xf.cu (forward
+// pass) and dstw_xi.cu (inverse pass): the first and last pass of every Poisson / CN solve
 // on grids whose axes have warp-per-line tables.
 //
 //   k_wxf: rows of the input -> prologue (load, apply_bc edges, refinement residual) -> S_x
 //          -> stored transposed (column by column) for the y pass
 //   k_wxi: transposed intermediate -> S_x -> epilogue (store, subtract, add the FP32 base
 //          iterate) into row-major output
-// A block owns kWarps consecutive rows; the transposing copies go through the rows' shared
+// A block owns kLines consecutive rows; the transposing copies go through the rows' shared
 // buffers so that both the row-major and the column-major side are contiguous in memory.
+#pragma once
+
 #include "dstw.cuh"
 
 namespace ib {
 namespace {
 
-using wdst::kWarps;
+using wdst::kLB;
+using wdst::kLines;
 using wdst::Shape;
-using wdst::warp_dst;
+using wdst::line_dst;
+using wdst::line_sync;
 
-template <typename T, typename Tin, int P, int PRO, bool kBC>
-__global__ void __launch_bounds__(kWarps * 32)
+template <typename T, typename Tin, int P, int NL, int PRO, bool kBC>
+__global__ void __launch_bounds__(kLines * NL)
 k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
   // exact arithmetic of the prologue: FP64, or float-float when the input is float-float
   using A = typename std::conditional<is_df64<Tin>::value, df64, double>::type;
-  using Sh = Shape<T, P>;
+  using Sh = Shape<T, P, NL>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = threadIdx.x / NL, lane = threadIdx.x % NL;
   T* U = sm + w * Sh::kStride;
   T* D = U + Sh::kU;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int total = a.batch * nrow;
   const Tin* in = static_cast<const Tin*>(a.in);
   T* out = static_cast<T*>(a.out);
-  for (int base = blockIdx.x * kWarps; base < total; base += gridDim.x * kWarps) {
+  for (int base = blockIdx.x * kLines; base < total; base += gridDim.x * kLines) {
     const int row = base + w;
     if (row < total) {
       const int b = row / nrow, J = row - b * nrow;
@@ -56,12 +61,12 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* yn = (x1 && J < nrow - 1) ? x1 + ncol : nullptr;
         // eight elements per lane per round, every load of a round issued before any use
         constexpr int R = 8;
-        for (int I0 = lane; I0 < ncol; I0 += 32 * R) {
+        for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float c0[R], w0[R], e0[R], s0[R], n0[R];
           df64 v[R];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
-            const int I = I0 + 32 * u;
+            const int I = I0 + NL * u;
             const bool ok = I < ncol;
             c0[u] = ok ? x0[I] : 0.0f;
             w0[u] = (ok && I > 0) ? x0[I - 1] : 0.0f;
@@ -79,7 +84,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           if (x1) {
 #pragma unroll
             for (int u = 0; u < R; ++u) {
-              const int I = I0 + 32 * u;
+              const int I = I0 + NL * u;
               const bool ok = I < ncol;
               c0[u] = ok ? x1[I] : 0.0f;
               w0[u] = (ok && I > 0) ? x1[I - 1] : 0.0f;
@@ -95,7 +100,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           }
 #pragma unroll
           for (int u = 0; u < R; ++u) {
-            const int I = I0 + 32 * u;
+            const int I = I0 + NL * u;
             if (I >= ncol) break;
             df64 mx = ma * lap[u];
             if (mcd == 1.0) mx = add_sloppy(mx, xv[u]);
@@ -113,13 +118,13 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           }
         }
       } else if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
-        for (int I0 = lane; I0 < ncol; I0 += 8 * 32) {
-          T v[8];
+        for (int I0 = lane; I0 < ncol; I0 += kLB * NL) {
+          T v[kLB];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = (I0 + 32 * u < ncol) ? (T)src[I0 + 32 * u] : T(0);
+          for (int u = 0; u < kLB; ++u) v[u] = (I0 + NL * u < ncol) ? (T)src[I0 + NL * u] : T(0);
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
-            if (I0 + 32 * u < ncol) U[I0 + 32 * u + 1] = v[u];
+          for (int u = 0; u < kLB; ++u)
+            if (I0 + NL * u < ncol) U[I0 + NL * u + 1] = v[u];
         }
       } else {
         const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
@@ -129,7 +134,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const A mc = (PRO == kProResid) ? A(a.mc[b * a.mstep]) : A(0.0);
         const A ma = (PRO == kProResid) ? A(a.ma[b * a.mstep]) : A(0.0);
 #pragma unroll 4
-        for (int I = lane; I < ncol; I += 32) {
+        for (int I = lane; I < ncol; I += NL) {
           A v = A(src[I]);
           if (kBC) {
             if (J == 0) v = v + fac * bc[g.B + 1 + I];
@@ -150,61 +155,61 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           U[I + 1] = (T)v;
         }
       }
-      __syncwarp();
-      warp_dst<T, P>(U, D, ax, lane);
+      line_sync<NL>(w + 1);
+      line_dst<T, P, NL>(U, D, ax, lane, w + 1);
     }
     __syncthreads();
-    // transposed store: thread (ww = tid mod kWarps) copies row base + ww, kWarps consecutive
+    // transposed store: thread (ww = tid mod kLines) copies row base + ww, kLines consecutive
     // threads write the block's rows of one column I next to each other
     {
-      const int ww = threadIdx.x & (kWarps - 1);
+      const int ww = threadIdx.x & (kLines - 1);
       const int rr = base + ww;
       if (rr < total) {
         const int b = rr / nrow, J = rr - b * nrow;
         T* o = out + (int64_t)b * a.stride + J;
         const T* srow = sm + ww * Sh::kStride + 1;
-        constexpr int step = kWarps * 32 / kWarps;
+        constexpr int step = NL;
 #pragma unroll 8
-        for (int I = threadIdx.x / kWarps; I < ncol; I += step) o[(int64_t)I * nrow] = srow[I];
+        for (int I = threadIdx.x / kLines; I < ncol; I += step) o[(int64_t)I * nrow] = srow[I];
       }
     }
     __syncthreads();
   }
 }
 
-template <typename T, typename Tout, int P, int EPI>
-__global__ void __launch_bounds__(kWarps * 32)
+template <typename T, typename Tout, int P, int NL, int EPI>
+__global__ void __launch_bounds__(kLines * NL)
 k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
   using A = typename std::conditional<is_df64<Tout>::value, df64, double>::type;
-  using Sh = Shape<T, P>;
+  using Sh = Shape<T, P, NL>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = threadIdx.x / NL, lane = threadIdx.x % NL;
   T* U = sm + w * Sh::kStride;
   T* D = U + Sh::kU;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int total = a.batch * nrow;
   const T* in = static_cast<const T*>(a.in);
   Tout* out = static_cast<Tout*>(a.out);
-  for (int base = blockIdx.x * kWarps; base < total; base += gridDim.x * kWarps) {
+  for (int base = blockIdx.x * kLines; base < total; base += gridDim.x * kLines) {
     // transposed load (the mirror of k_wxf's store), eight loads in flight per thread
     {
-      const int ww = threadIdx.x & (kWarps - 1);
+      const int ww = threadIdx.x & (kLines - 1);
       const int rr = base + ww;
       if (rr < total) {
         const int b = rr / nrow, J = rr - b * nrow;
         const T* src = in + (int64_t)b * a.stride + J;
         T* drow = sm + ww * Sh::kStride + 1;
-        constexpr int step = kWarps * 32 / kWarps;
-        for (int I0 = threadIdx.x / kWarps; I0 < ncol; I0 += 8 * step) {
-          T v[8];
+        constexpr int step = NL;
+        for (int I0 = threadIdx.x / kLines; I0 < ncol; I0 += kLB * step) {
+          T v[kLB];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < kLB; ++u) {
             const int I = I0 + u * step;
             v[u] = I < ncol ? src[(int64_t)I * nrow] : T(0);
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < kLB; ++u) {
             const int I = I0 + u * step;
             if (I < ncol) drow[I] = v[u];
           }
@@ -216,15 +221,15 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
     if (row < total) {
       const int b = row / nrow, J = row - b * nrow;
       const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
-      warp_dst<T, P>(U, D, ax, lane);
+      line_dst<T, P, NL>(U, D, ax, lane, w + 1);
       Tout* dst = out + off;
       if (EPI == kEpiStore) {
 #pragma unroll 8
-        for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)U[I + 1];
+        for (int I = lane; I < ncol; I += NL) dst[I] = (Tout)U[I + 1];
       } else if (EPI == kEpiSub) {
         const A* sf = static_cast<const A*>(a.sub_from) + off;
 #pragma unroll 4
-        for (int I = lane; I < ncol; I += 32) dst[I] = (Tout)(sf[I] - A(U[I + 1]));
+        for (int I = lane; I < ncol; I += NL) dst[I] = (Tout)(sf[I] - A(U[I + 1]));
       } else if constexpr (is_df64<Tout>::value) {
         // x = x0 [+ x1] + d: the FP32 parts summed error-free, the (small) correction added
         // to the low part
@@ -232,12 +237,12 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
         const df64* sf = (EPI == kEpiSubAddBase) ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         constexpr int R = 8;
-        for (int I0 = lane; I0 < ncol; I0 += 32 * R) {
+        for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
           df64 f[R];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
-            const int I = I0 + 32 * u;
+            const int I = I0 + NL * u;
             const bool ok = I < ncol;
             b0[u] = ok ? bs[I] : 0.0f;
             b1[u] = (ok && bs2) ? bs2[I] : 0.0f;
@@ -245,7 +250,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
           }
 #pragma unroll
           for (int u = 0; u < R; ++u) {
-            const int I = I0 + 32 * u;
+            const int I = I0 + NL * u;
             if (I >= ncol) break;
             const df64 x01 = two_sum(b0[u], b1[u]);
             const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
@@ -257,7 +262,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
         const A* sf = (EPI == kEpiSubAddBase) ? static_cast<const A*>(a.sub_from) + off : nullptr;
 #pragma unroll 4
-        for (int I = lane; I < ncol; I += 32) {
+        for (int I = lane; I < ncol; I += NL) {
           A xv = A(bs[I]);
           if (bs2) xv = xv + A(bs2[I]);
           xv = xv + A(U[I + 1]);
@@ -269,115 +274,66 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
   }
 }
 
-template <typename T, int P>
+template <typename T, int P, int NL>
 size_t smem_bytes() {
-  return (size_t)kWarps * Shape<T, P>::kStride * sizeof(T);
+  return (size_t)kLines * Shape<T, P, NL>::kStride * sizeof(T);
 }
 
-template <typename T, typename Tin, int P, int PRO, bool kBC>
+template <typename T, typename Tin, int P, int NL, int PRO, bool kBC>
 cudaError_t launch_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
-  auto k = k_wxf<T, Tin, P, PRO, kBC>;
-  const size_t smem = smem_bytes<T, P>();
+  auto k = k_wxf<T, Tin, P, NL, PRO, kBC>;
+  const size_t smem = smem_bytes<T, P, NL>();
   cudaError_t e = set_smem_limit((const void*)k, smem);
   if (e != cudaSuccess) return e;
   const int total = a.batch * (g.ny - 1);
-  k<<<(total + kWarps - 1) / kWarps, kWarps * 32, smem, s>>>(g, ax, a);
+  k<<<(total + kLines - 1) / kLines, kLines * NL, smem, s>>>(g, ax, a);
   return cudaGetLastError();
 }
 
-template <typename T, typename Tin, int P>
+template <typename T, typename Tin, int P, int NL>
 cudaError_t fwd_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
   const bool bc = a.bc != nullptr;
   if (a.pro == kProResid) {
     // the refinement residual belongs to the mixed path (float-float input)
     if constexpr (is_df64<Tin>::value) {
       if (!a.base || !a.mc || !a.ma) return cudaErrorInvalidValue;
-      return bc ? launch_fwd<T, Tin, P, kProResid, true>(g, ax, a, s)
-                : launch_fwd<T, Tin, P, kProResid, false>(g, ax, a, s);
+      return bc ? launch_fwd<T, Tin, P, NL, kProResid, true>(g, ax, a, s)
+                : launch_fwd<T, Tin, P, NL, kProResid, false>(g, ax, a, s);
     }
     return cudaErrorInvalidValue;
   }
-  return bc ? launch_fwd<T, Tin, P, kProLoad, true>(g, ax, a, s) : launch_fwd<T, Tin, P, kProLoad, false>(g, ax, a, s);
+  return bc ? launch_fwd<T, Tin, P, NL, kProLoad, true>(g, ax, a, s) : launch_fwd<T, Tin, P, NL, kProLoad, false>(g, ax, a, s);
 }
 
-template <typename T, typename Tout, int P, int EPI>
+template <typename T, typename Tout, int P, int NL, int EPI>
 cudaError_t launch_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
-  auto k = k_wxi<T, Tout, P, EPI>;
-  const size_t smem = smem_bytes<T, P>();
+  auto k = k_wxi<T, Tout, P, NL, EPI>;
+  const size_t smem = smem_bytes<T, P, NL>();
   cudaError_t e = set_smem_limit((const void*)k, smem);
   if (e != cudaSuccess) return e;
   const int total = a.batch * (g.ny - 1);
-  k<<<(total + kWarps - 1) / kWarps, kWarps * 32, smem, s>>>(g, ax, a);
+  k<<<(total + kLines - 1) / kLines, kLines * NL, smem, s>>>(g, ax, a);
   return cudaGetLastError();
 }
 
 // epilogues per output type: FP64 path store / subtract; mixed path FP32 store of the iterate
 // and float-float sums with the base iterate
-template <typename T, typename Tout, int P>
+template <typename T, typename Tout, int P, int NL>
 cudaError_t inv_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
   if (a.bc) return cudaErrorInvalidValue;
   if constexpr (std::is_same<Tout, T>::value) {
-    if (a.epi == kEpiStore) return launch_inv<T, Tout, P, kEpiStore>(g, ax, a, s);
+    if (a.epi == kEpiStore) return launch_inv<T, Tout, P, NL, kEpiStore>(g, ax, a, s);
     if constexpr (std::is_same<T, double>::value) {
-      if (a.epi == kEpiSub) return launch_inv<T, Tout, P, kEpiSub>(g, ax, a, s);
+      if (a.epi == kEpiSub) return launch_inv<T, Tout, P, NL, kEpiSub>(g, ax, a, s);
     }
     return cudaErrorInvalidValue;
   } else {
     if (!a.base) return cudaErrorInvalidValue;
-    if (a.epi == kEpiAddBase) return launch_inv<T, Tout, P, kEpiAddBase>(g, ax, a, s);
-    if (a.epi == kEpiSubAddBase) return launch_inv<T, Tout, P, kEpiSubAddBase>(g, ax, a, s);
+    if (a.epi == kEpiAddBase) return launch_inv<T, Tout, P, NL, kEpiAddBase>(g, ax, a, s);
+    if (a.epi == kEpiSubAddBase) return launch_inv<T, Tout, P, NL, kEpiSubAddBase>(g, ax, a, s);
     return cudaErrorInvalidValue;
   }
 }
 
 }  // namespace
-
-template <typename T, typename Tin>
-cudaError_t wx_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
-  if (ax.n != g.nx || !ax.wP) return cudaErrorInvalidValue;
-  if (a.batch <= 0) return cudaSuccess;
-  ProfScope prof(kClassXPass, s);
-  switch (ax.wP) {
-    case 1: return fwd_p<T, Tin, 1>(g, ax, a, s);
-    case 2: return fwd_p<T, Tin, 2>(g, ax, a, s);
-    case 3: return fwd_p<T, Tin, 3>(g, ax, a, s);
-    case 4: return fwd_p<T, Tin, 4>(g, ax, a, s);
-    case 6: return fwd_p<T, Tin, 6>(g, ax, a, s);
-    case 8: return fwd_p<T, Tin, 8>(g, ax, a, s);
-    case 12: return fwd_p<T, Tin, 12>(g, ax, a, s);
-    case 16: return fwd_p<T, Tin, 16>(g, ax, a, s);
-    case 24: return fwd_p<T, Tin, 24>(g, ax, a, s);
-    case 32: return fwd_p<T, Tin, 32>(g, ax, a, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-template <typename T, typename Tout>
-cudaError_t wx_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
-  if (ax.n != g.nx || !ax.wP) return cudaErrorInvalidValue;
-  if (a.batch <= 0) return cudaSuccess;
-  ProfScope prof(kClassXPass, s);
-  switch (ax.wP) {
-    case 1: return inv_p<T, Tout, 1>(g, ax, a, s);
-    case 2: return inv_p<T, Tout, 2>(g, ax, a, s);
-    case 3: return inv_p<T, Tout, 3>(g, ax, a, s);
-    case 4: return inv_p<T, Tout, 4>(g, ax, a, s);
-    case 6: return inv_p<T, Tout, 6>(g, ax, a, s);
-    case 8: return inv_p<T, Tout, 8>(g, ax, a, s);
-    case 12: return inv_p<T, Tout, 12>(g, ax, a, s);
-    case 16: return inv_p<T, Tout, 16>(g, ax, a, s);
-    case 24: return inv_p<T, Tout, 24>(g, ax, a, s);
-    case 32: return inv_p<T, Tout, 32>(g, ax, a, s);
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-// FP64 path: double in and out.  Mixed path: FP32 transforms fed from float-float inputs,
-// FP32 iterates, float-float results.
-template cudaError_t wx_fwd<double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
-template cudaError_t wx_fwd<float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
-template cudaError_t wx_inv<double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
-template cudaError_t wx_inv<float, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
-template cudaError_t wx_inv<float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
-
 }  // namespace ib

@@ -1,0 +1,25 @@
+// Line-parallel inverse x pass: transposed load, S_x, epilogue (kernels in dstw_x.cuh).
+#include "dstw_x.cuh"
+
+namespace ib {
+
+template <typename T, typename Tout>
+cudaError_t wx_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaStream_t s) {
+  if (ax.n != g.nx || !ax.wP) return cudaErrorInvalidValue;
+  if (a.batch <= 0) return cudaSuccess;
+  ProfScope prof(kClassXPass, s);
+  switch (ax.wNL * 100 + ax.wP) {
+#define IB_WCASE(NL, P) \
+  case NL * 100 + P: return inv_p<T, Tout, P, NL>(g, ax, a, s);
+    IB_WDST_COMBOS(IB_WCASE)
+#undef IB_WCASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// FP64 path: double out.  Mixed path: FP32 iterates and float-float results.
+template cudaError_t wx_inv<double, double>(const Geometry&, const DstAxis<double>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_inv<float, float>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+template cudaError_t wx_inv<float, df64>(const Geometry&, const DstAxis<float>&, const XArgs&, cudaStream_t);
+
+}  // namespace ib

@@ -49,13 +49,14 @@ template <typename T> struct DstAxis {
   const c2_t<T>* tw;        // [M]      e^{-2 pi i p / M}
   const T* sintab;          // [n/2+1]  sin(pi j / n)
   const c2_t<T>* post;      // [M/2+1]  e^{-2 pi i k / n}
-  // warp-per-line transforms (dstw.cuh), axes with M = 32 wP, wP in {1,2,4,8,16,32}; 0 otherwise.
-  // Tables in lane order (entry [s][lane] at s*32 + lane), G = 32 / wP:
-  int wP;
-  const c2_t<T>* wtw1;      // [wP][32]     e^{-2 pi i lane a / M}
-  const c2_t<T>* wtw2;      // [wP][32]     e^{-2 pi i (lane mod G) c / 32}
-  const c2_t<T>* wtw3;      // [log2 G][32] radix-2 twiddles of the cross-lane stages
-  const c2_t<T>* wsn;       // [wP][32]     (sin(pi 2m/n), sin(pi (2m+1)/n)), m = lane + 32 r
+  // line-parallel transforms (dstw.cuh): M = wNL wP, wNL = 32 (one warp per line) or 64 (two);
+  // wP = 0 for axes without them.  Tables in lane order (entry [s][lane] at s*wNL + lane),
+  // G = wNL / wP (or 32 when wP does not divide wNL):
+  int wP, wNL;
+  const c2_t<T>* wtw1;      // [wP][wNL]     e^{-2 pi i lane a / M}
+  const c2_t<T>* wtw2;      // [wP][wNL]     e^{-2 pi i (lane mod G) c / wNL}
+  const c2_t<T>* wtw3;      // [log2 G][wNL] radix-2 twiddles of the cross-lane stages
+  const c2_t<T>* wsn;       // [wP][wNL]     (sin(pi 2m/n), sin(pi (2m+1)/n)), m = lane + wNL r
 };
 
 struct Geometry {

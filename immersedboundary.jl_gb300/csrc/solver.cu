@@ -47,6 +47,8 @@ constexpr int kQ0Slots = 1024;  // pinned staging slots of per-step base flux
 struct ib_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;            // forked branch of a step (curl of finished levels)
+  std::vector<cudaEvent_t> fork_ev;       // one per level, plus the join
   Geometry g{};
   double dt = 0, re = 0, beta0 = 1.5, beta1 = -0.5;
   int nbodies = 0, nb = 0, nf = 0;
@@ -331,24 +333,39 @@ S* view(double* p) {
 
 // Vort2Flux (src/streamfcn/fluid-ops.jl:438-472) on one L-level set.  If q is null only the
 // level-1 flux is formed, into q1.  gam is coarsened in place like the reference.
+//
+// With q given, the curl of each finished level runs on the side stream while the finer levels
+// are solved (it reads only that level's psi and ring); the branch joins before returning.
 template <typename S>
 cudaError_t vort2flux(ib_handle* h, S* gam, S* psi, S* q, S* q1, S* rings) {
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t nG = g.nG;
-  for (int l = 1; l < L; ++l) CE(coarsify<S>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, h->stream));
+  cudaStream_t s = h->stream;
+  const bool fork = q && h->side && L > 1;
+  auto curl_level = [&](int l, const S* ring) -> cudaError_t {
+    if (!fork) return curl<S>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, s);
+    CE(cudaEventRecord(h->fork_ev[l], s));
+    CE(cudaStreamWaitEvent(h->side, h->fork_ev[l], 0));
+    return curl<S>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->side);
+  };
+  for (int l = 1; l < L; ++l) CE(coarsify<S>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, s));
   // mixed precision: the coarse levels only feed the finer levels' boundary rings
   const int coarse = std::min(h->refine, h->refine_coarse);
   CE(solve(h, gam + (L - 1) * nG, psi + (L - 1) * nG, 1, nullptr, op_lap(h), nullptr,
            L - 1 >= h->coarse_from ? coarse : 0));
-  if (q) CE(curl<S>(g, psi + (L - 1) * nG, nullptr, q + (int64_t)(L - 1) * g.nq, 1, h->stream));
-  else if (L == 1) CE(curl<S>(g, psi, nullptr, q1, 1, h->stream));
+  if (q) CE(curl_level(L - 1, nullptr));
+  else if (L == 1) CE(curl<S>(g, psi, nullptr, q1, 1, s));
   for (int l = L - 2; l >= 0; --l) {
     S* ring = rings + (int64_t)l * g.nbc;
-    CE(get_bc<S>(g, psi + (l + 1) * nG, ring, 1, S(1.0), h->stream));
+    CE(get_bc<S>(g, psi + (l + 1) * nG, ring, 1, S(1.0), s));
     CE(solve(h, gam + l * nG, psi + l * nG, 1, ring, op_lap(h), nullptr, l >= h->coarse_from ? coarse : 0));
-    if (q) CE(curl<S>(g, psi + l * nG, ring, q + (int64_t)l * g.nq, 1, h->stream));
-    else if (l == 0) CE(curl<S>(g, psi, ring, q1, 1, h->stream));
+    if (q) CE(l > 0 ? curl_level(l, ring) : curl<S>(g, psi, ring, q, 1, s));
+    else if (l == 0) CE(curl<S>(g, psi, ring, q1, 1, s));
+  }
+  if (fork) {
+    CE(cudaEventRecord(h->fork_ev[L], h->side));
+    CE(cudaStreamWaitEvent(s, h->fork_ev[L], 0));
   }
   return cudaSuccess;
 }
@@ -618,6 +635,9 @@ void destroy_handle(ib_handle* h) {
   h->axy.release();
   h->axx32.release();
   h->axy32.release();
+  for (auto ev : h->fork_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
@@ -883,6 +903,16 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     return rc;
   };
   h->g = make_geometry(p->nx, p->ny, p->nlevels, p->h, p->x0, p->y0);
+  if ((e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking)) != cudaSuccess) {
+    h->side = nullptr;
+    return bail(fail(h, IB_ERR_CUDA, "cudaStreamCreate", e));
+  }
+  h->fork_ev.assign(p->nlevels + 1, nullptr);
+  for (auto& ev : h->fork_ev)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      ev = nullptr;
+      return bail(fail(h, IB_ERR_CUDA, "cudaEventCreate", e));
+    }
   h->dt = p->dt;
   h->re = p->re;
   h->beta0 = p->beta0;

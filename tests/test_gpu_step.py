@@ -187,3 +187,22 @@ def test_warp_and_stockham_transforms_agree(ib, monkeypatch, precision, tol):
         s.close()
     assert rel(out["warp"][0], out["stockham"][0]) < tol
     assert np.max(np.abs(out["warp"][1] - out["stockham"][1])) < tol * 100
+
+
+def test_two_warp_lines_agree_with_one_warp_lines(ib, monkeypatch):
+    """Lines transformed by two warps (IBGB300_LINE_LANES=64) and by one warp give the same
+    mixed-precision steps to round-off."""
+    wl = ib.workloads.scaled(ib.workloads.two_body_large(), 256, 256, nlevels=3)
+    out = {}
+    for lanes in ("32", "64"):
+        monkeypatch.setenv("IBGB300_LINE_LANES", lanes)
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision="mixed")
+        s.vort2flux(st)
+        for i in range(10):
+            ib.advance_(st, s, i * wl.dt)
+        out[lanes] = st.qty.gamma.copy()
+        s.close()
+    assert rel(out["64"], out["32"]) < 1e-9

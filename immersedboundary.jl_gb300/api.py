@@ -44,7 +44,7 @@ __all__ = [
     "StreamFcnFluid", "RigidBody", "BodyGroup", "circle", "npoints", "SchemeCNAB", "SchemeRKC",
     "Problem", "State", "StreamFcnQuantities", "BodyStress", "Solver", "initstate", "initsolver",
     "advance_", "solve", "solve_", "each_timestep", "at_times", "at_indices", "StopIteration",
-    "StateResult", "timestep", "gridstep",
+    "StateResult", "timestep", "gridstep", "Ensemble",
 ]
 
 
@@ -445,6 +445,7 @@ class Solver:
         self.handle = h
         self._set_state(state)
         state._solver = self
+        self._bound_state = state
 
     def close(self):
         if getattr(self, "handle", None):
@@ -602,6 +603,12 @@ class Solver:
         state.t = float(t)
         state._stale = True
 
+    def _after_ensemble(self, t, state: State | None):
+        st = state if state is not None else getattr(self, "_bound_state", None)
+        if st is not None and t is not None:
+            st.t = t
+            st._stale = True
+
     def vort2flux(self, state: State):
         """``solver.vort2flux!(state.qty)`` (fluid-ops.jl:438): psi and q from Gamma, on the GPU."""
         self._check(self.lib.ib_vort2flux(self.handle))
@@ -631,6 +638,56 @@ def initsolver(prob: Problem, state: State, **kw) -> Solver:
 def advance_(state: State, solver: Solver, t: float):
     """``advance!(state, solver, t)`` (cnab/timestepping.jl:253-290)."""
     solver.advance(state, t)
+
+
+class Ensemble:
+    """Independent static-body simulations advanced together by one graph launch per step
+    (include/ibgb300_ensemble.h; no reference counterpart).  Members keep their own state;
+    ``state`` objects are refreshed lazily like after ``advance_``."""
+
+    def __init__(self, solvers: Sequence[Solver]):
+        self.solvers = list(solvers)
+        self.lib = self.solvers[0].lib
+        arr = (C.c_void_p * len(self.solvers))(*[s.handle for s in self.solvers])
+        h = C.c_void_p()
+        st = self.lib.ib_ensemble_create(arr, len(self.solvers), C.byref(h))
+        if st != _lib.IB_OK:
+            raise _lib.IBError(st, (self.lib.ib_ensemble_last_error(None) or b"").decode())
+        self.handle = h
+
+    def _check(self, st):
+        if st != _lib.IB_OK:
+            raise _lib.IBError(st, (self.lib.ib_ensemble_last_error(self.handle) or b"").decode())
+
+    def info(self):
+        n, k = C.c_int32(), C.c_int32()
+        self._check(self.lib.ib_ensemble_info(self.handle, C.byref(n), C.byref(k)))
+        return n.value, k.value
+
+    def advance_n(self, ts, uv=None, states: Sequence[State] | None = None) -> float:
+        """Advance every member through the times ``ts`` (freestream per member and step in
+        ``uv`` [len(ts)][members][2], default each member's problem freestream); returns the
+        device milliseconds."""
+        ts = np.ascontiguousarray(ts, dtype=np.float64)
+        if uv is None:
+            uv = np.array([[s.prob.fluid.freestream(float(t)) for s in self.solvers] for t in ts], dtype=np.float64)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        ms = C.c_double()
+        self._check(self.lib.ib_ensemble_advance_n(self.handle, len(ts), _lib.dptr(ts), _lib.dptr(uv), C.byref(ms)))
+        for k, s in enumerate(self.solvers):
+            s._after_ensemble(float(ts[-1]) if len(ts) else None, states[k] if states else None)
+        return ms.value
+
+    def close(self):
+        if self.handle:
+            self.lib.ib_ensemble_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------------------------

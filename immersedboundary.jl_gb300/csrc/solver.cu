@@ -15,6 +15,7 @@
 #include "mlp.cuh"
 #include "ibgb300.h"
 #include "ibgb300_learn.h"
+#include "ibgb300_ensemble.h"
 #include "ibgb300_ops.h"
 #include "ibgb300_diag.h"
 
@@ -1652,6 +1653,239 @@ int ib_get_cg_start_residuals(ib_handle* h, int32_t count, double* r0) {
   for (int i = 0; i < count; ++i)
     if (r0) r0[i] = h->cg_res0[off + i];
   return IB_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// ensembles (include/ibgb300_ensemble.h)
+// ------------------------------------------------------------------------------------------------
+}  // extern "C"
+
+struct ib_ensemble {
+  int device = 0;
+  std::vector<ib_handle*> m;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t start = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  double* h_q0 = nullptr;            // pinned [2][slot_len]: base flux of every member and level
+  std::vector<int64_t> q0_off;
+  int64_t slot_len = 0;
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  bool launched[2] = {false, false};
+  int parity = 0;
+  int kernels_per_step = 0;
+  std::string err;
+};
+
+namespace {
+
+int efail(ib_ensemble* e, int code, const std::string& what, cudaError_t ce = cudaSuccess) {
+  std::string msg = what;
+  if (ce != cudaSuccess) {
+    msg += ": ";
+    msg += cudaGetErrorString(ce);
+  }
+  if (e) e->err = msg;
+  else {
+    std::lock_guard<std::mutex> lock(g_err_mu);
+    g_create_err = msg;
+  }
+  return code;
+}
+
+#define EK(x)                                                              \
+  do {                                                                     \
+    cudaError_t e_ = (x);                                                  \
+    if (e_ != cudaSuccess) return efail(e, IB_ERR_CUDA, #x, e_);           \
+  } while (0)
+
+void destroy_ensemble(ib_ensemble* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  for (auto& g : e->gexec)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto ev : e->join)
+    if (ev) cudaEventDestroy(ev);
+  for (auto ev : e->done)
+    if (ev) cudaEventDestroy(ev);
+  if (e->start) cudaEventDestroy(e->start);
+  if (e->h_q0) cudaFreeHost(e->h_q0);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+// capture one ensemble step for buffer parity offset p (member i runs its parity base_i ^ p)
+int capture_ensemble(ib_ensemble* e, int p) {
+  cudaGraph_t graph = nullptr;
+  EK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaEventRecord(e->start, e->stream);
+  for (size_t i = 0; i < e->m.size() && ce == cudaSuccess; ++i) {
+    ib_handle* h = e->m[i];
+    ce = cudaStreamWaitEvent(h->stream, e->start, 0);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(h->d_q0, e->h_q0 + p * e->slot_len + e->q0_off[i], sizeof(double) * 2 * h->g.nlev,
+                           cudaMemcpyHostToDevice, h->stream);
+    if (ce == cudaSuccess) ce = enqueue_step_mode(h, h->parity ^ p);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e->join[i], h->stream);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->join[i], 0);
+  }
+  cudaError_t ce2 = cudaStreamEndCapture(e->stream, &graph);
+  if (ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return efail(e, IB_ERR_CUDA, "ensemble capture", ce);
+  }
+  if (ce2 != cudaSuccess) return efail(e, IB_ERR_CUDA, "ensemble capture", ce2);
+  size_t nn = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nn) == cudaSuccess && nn > 0) {
+    std::vector<cudaGraphNode_t> nodes(nn);
+    cudaGraphGetNodes(graph, nodes.data(), &nn);
+    int k = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType ty;
+      if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++k;
+    }
+    e->kernels_per_step = k;
+  }
+  ce = cudaGraphInstantiate(&e->gexec[p], graph, 0);
+  cudaGraphDestroy(graph);
+  if (ce != cudaSuccess) return efail(e, IB_ERR_CUDA, "ensemble graph instantiate", ce);
+  return IB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) {
+  if (!members || n < 1 || !out) return efail(nullptr, IB_ERR_INVALID, "ensemble: no members");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    const ib_handle* h = members[i];
+    if (!h) return efail(nullptr, IB_ERR_INVALID, "ensemble: null member");
+    if (h->motion != IB_MOTION_STATIC)
+      return efail(nullptr, IB_ERR_UNSUPPORTED, "ensemble members must have bodies fixed in the grid");
+    if (h->device != members[0]->device || h->steps != members[0]->steps)
+      return efail(nullptr, IB_ERR_INVALID, "ensemble members must share the device and the step count");
+    for (int j = 0; j < i; ++j)
+      if (members[j] == h) return efail(nullptr, IB_ERR_INVALID, "ensemble member given twice");
+  }
+  ib_ensemble* e = new ib_ensemble();
+  e->device = members[0]->device;
+  e->m.assign(members, members + n);
+  cudaError_t ce = cudaSetDevice(e->device);
+  auto bail = [&](int rc) {
+    {
+      std::lock_guard<std::mutex> lock(g_err_mu);
+      g_create_err = e->err;
+    }
+    destroy_ensemble(e);
+    return rc;
+  };
+  if (ce != cudaSuccess) return bail(efail(e, IB_ERR_CUDA, "cudaSetDevice", ce));
+  for (ib_handle* h : e->m) {
+    e->q0_off.push_back(e->slot_len);
+    e->slot_len += 2 * h->g.nlev;
+    if ((ce = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(efail(e, IB_ERR_CUDA, "member sync", ce));
+  }
+  if ((ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    e->stream = nullptr;
+    return bail(efail(e, IB_ERR_CUDA, "cudaStreamCreate", ce));
+  }
+  if ((ce = cudaEventCreateWithFlags(&e->start, cudaEventDisableTiming)) != cudaSuccess) {
+    e->start = nullptr;
+    return bail(efail(e, IB_ERR_CUDA, "cudaEventCreate", ce));
+  }
+  e->join.assign(n, nullptr);
+  for (auto& ev : e->join)
+    if ((ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      ev = nullptr;
+      return bail(efail(e, IB_ERR_CUDA, "cudaEventCreate", ce));
+    }
+  for (auto& ev : e->done)
+    if ((ce = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      ev = nullptr;
+      return bail(efail(e, IB_ERR_CUDA, "cudaEventCreate", ce));
+    }
+  if ((ce = cudaMallocHost(&e->h_q0, sizeof(double) * 2 * (size_t)e->slot_len)) != cudaSuccess) {
+    e->h_q0 = nullptr;
+    return bail(efail(e, IB_ERR_CUDA, "pinned staging", ce));
+  }
+  for (int p = 0; p < 2; ++p) {
+    int rc = capture_ensemble(e, p);
+    if (rc != IB_OK) return bail(rc);
+  }
+  *out = e;
+  return IB_OK;
+}
+
+int ib_ensemble_destroy(ib_ensemble* e) {
+  destroy_ensemble(e);
+  return IB_OK;
+}
+
+int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, double* device_ms) {
+  if (!e || nsteps < 0 || (nsteps > 0 && (!t || !uv))) return IB_ERR_INVALID;
+  EK(cudaSetDevice(e->device));
+  const int n = (int)e->m.size();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (device_ms) {
+    EK(cudaEventCreate(&e0));
+    EK(cudaEventCreate(&e1));
+    EK(cudaEventRecord(e0, e->stream));
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    const int p = e->parity;
+    // the launch that read this slot two steps ago must be done before the slot is rewritten
+    if (e->launched[p]) EK(cudaEventSynchronize(e->done[p]));
+    double* slot = e->h_q0 + (size_t)p * e->slot_len;
+    for (int i = 0; i < n; ++i) {
+      const ib_handle* h = e->m[i];
+      const double u = uv[((size_t)s * n + i) * 2], v = uv[((size_t)s * n + i) * 2 + 1];
+      for (int l = 0; l < h->g.nlev; ++l) {
+        const double hc = h->g.h * std::ldexp(1.0, l);  // base_flux!, fluid-ops.jl:414-415
+        slot[e->q0_off[i] + 2 * l] = u * hc;
+        slot[e->q0_off[i] + 2 * l + 1] = v * hc;
+      }
+    }
+    EK(cudaGraphLaunch(e->gexec[p], e->stream));
+    EK(cudaEventRecord(e->done[p], e->stream));
+    e->launched[p] = true;
+    e->parity ^= 1;
+    for (ib_handle* h : e->m) {
+      h->parity ^= 1;
+      h->steps++;
+      h->t = t[s];
+    }
+  }
+  if (device_ms) {
+    EK(cudaEventRecord(e1, e->stream));
+    EK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    EK(cudaEventElapsedTime(&ms, e0, e1));
+    *device_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  EK(cudaStreamSynchronize(e->stream));
+  for (int i = 0; i < n; ++i) {
+    int rc = check_status(e->m[i]);
+    if (rc != IB_OK) return efail(e, rc, "member " + std::to_string(i) + ": " + e->m[i]->err);
+  }
+  return IB_OK;
+}
+
+int ib_ensemble_info(ib_ensemble* e, int32_t* members, int32_t* kernels_per_step) {
+  if (!e) return IB_ERR_INVALID;
+  if (members) *members = (int32_t)e->m.size();
+  if (kernels_per_step) *kernels_per_step = e->kernels_per_step;
+  return IB_OK;
+}
+
+const char* ib_ensemble_last_error(const ib_ensemble* e) {
+  if (e) return e->err.c_str();
+  std::lock_guard<std::mutex> lock(g_err_mu);
+  return g_create_err.c_str();
 }
 
 }  // extern "C"

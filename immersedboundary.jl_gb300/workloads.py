@@ -14,6 +14,10 @@ seeded initial vorticity noise (NumPy PCG64), identical for the GPU path and the
                        y = 0.5 sin(2 pi f t) and pitching 30 deg sin(2 pi f t + pi/2) about its
                        quarter chord, f = 0.2, Re=1000, dt=0.0005 (at dt=0.001 the explicit
                        advection of the CNAB step grows by ~4x per step from step 5)
+* ``ensemble``         independent members: finest grid drawn from {128x128, 256x256,
+                       384x256, 512x512}, h = 4/nx, 3-5 levels, an ellipse of chord 1 with aspect
+                       ratio U[0.1, 1] at U[0, 40] deg (points ~h apart), Re log-uniform in
+                       [50, 500], dt = 0.2 h (bodies fixed in the grid)
 * ``scaled(...)``      the same bodies on coarser grids, for tests
 """
 from __future__ import annotations
@@ -102,6 +106,38 @@ def four_cylinders(nsteps: int = 2000, seed: int = 0) -> Workload:
     cyl = [cylinder((x, y), 0.5, 629) for y in (-0.75, 0.75) for x in (-0.75, 0.75)]
     return Workload("four_cylinders", 0.0025, (-2.0, 3.12), (-2.56, 2.56), 5, 150.0, 0.0005, nsteps, cyl,
                     seed=seed)
+
+
+def ellipse(center, chord: float, aspect: float, angle_deg: float, h: float, frame=None) -> RigidBody:
+    """Points ~h apart (equal arc length) on an ellipse of major axis `chord` and minor axis
+    aspect*chord, rotated by angle_deg (leading edge up for positive angles)."""
+    a, b = chord / 2, aspect * chord / 2
+    th = np.linspace(0, 2 * math.pi, 4097)
+    x, y = a * np.cos(th), b * np.sin(th)
+    s = np.concatenate([[0.0], np.cumsum(np.hypot(np.diff(x), np.diff(y)))])
+    n = max(8, int(round(s[-1] / h)))
+    sk = np.arange(n) * s[-1] / n
+    xs, ys = np.interp(sk, s, x), np.interp(sk, s, y)
+    c, sn = math.cos(math.radians(angle_deg)), math.sin(math.radians(angle_deg))
+    xb = np.stack([center[0] + c * xs + sn * ys, center[1] - sn * xs + c * ys], axis=1)
+    return RigidBody(frame or GridFrame(), xb, np.full(n, s[-1] / n))
+
+
+def ensemble(n: int = 96, nsteps: int = 1000, seed: int = 0) -> list[Workload]:
+    rng = np.random.default_rng(seed)
+    grids = [(128, 128), (256, 256), (384, 256), (512, 512)]
+    out = []
+    for k in range(n):
+        nx, ny = grids[rng.integers(len(grids))]
+        h = 4.0 / nx
+        L = int(rng.integers(3, 6))
+        aspect = float(rng.uniform(0.1, 1.0))
+        angle = float(rng.uniform(0.0, 40.0))
+        re = float(np.exp(rng.uniform(np.log(50.0), np.log(500.0))))
+        body = ellipse((0.0, 0.0), 1.0, aspect, angle, h)
+        out.append(Workload(f"member{k}", h, (-1.5, 2.5), (-ny * h / 2, ny * h / 2), L, re, 0.2 * h, nsteps,
+                            [body], seed=seed + k))
+    return out
 
 
 def heave_pitch_frame(f: float = 0.2, heave: float = 0.5, pitch_deg: float = 30.0) -> RelativeFrame:

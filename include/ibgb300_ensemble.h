@@ -1,0 +1,39 @@
+/* libibgb300: ensembles of independent simulations stepped by one graph launch.
+ *
+ * No reference counterpart (the reference advances one problem per solve! call).  An ensemble
+ * groups handles created by ib_create (any grid sizes, levels, bodies and precisions; bodies
+ * fixed in the grid; same device; same step count) and captures their advance! steps as
+ * parallel branches of one CUDA graph, so that one launch advances every member by one step
+ * and their kernels share the GPU.  Each member's freestream value enters through a captured
+ * host-to-device copy from a pinned slot (two slots, one per buffer parity).  The members'
+ * own state, history and error reporting work as for single handles; a member must not be
+ * advanced on its own while it belongs to an ensemble.
+ */
+#ifndef IBGB300_ENSEMBLE_H
+#define IBGB300_ENSEMBLE_H
+
+#include "ibgb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ib_ensemble ib_ensemble;
+
+int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out);
+int ib_ensemble_destroy(ib_ensemble* e);
+
+/* nsteps steps of every member: t[nsteps] (common times), uv[nsteps][n][2] (freestream per
+ * member and step); device_ms (optional) receives the device time of the steps */
+int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, double* device_ms);
+
+/* kernel launches per ensemble step (graph kernel nodes over all members) */
+int ib_ensemble_info(ib_ensemble* e, int32_t* members, int32_t* kernels_per_step);
+
+const char* ib_ensemble_last_error(const ib_ensemble* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

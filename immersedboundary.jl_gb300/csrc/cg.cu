@@ -72,7 +72,59 @@ __global__ void k_cg_roll(double* s) {
 
 inline int blocks(int n) { return (n + 255) / 256 < 1 ? 1 : (n + 255) / 256; }
 
+// Device-side control of the CG loop in a captured step (a while-conditional graph node).
+// sc: [0] r.z, [1] p.Ap, [2] new r.z, [3] rhs.rhs, [4] r.r, [5] target, [6] |rhs|;
+// ctl: [0] iterations (as double), out: [0] iterations, [1] final and [2] initial relative
+// residual, [3] 1 when the cap was reached
+__global__ void k_cg_start(double* __restrict__ sc, double* __restrict__ ctl, double tol, int* __restrict__ status,
+                           double* __restrict__ out, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x != 0) return;
+  const double bn = sqrt(sc[3]), rn = sqrt(sc[4]);
+  sc[5] = tol * bn;
+  sc[6] = bn;
+  ctl[0] = 0.0;
+  out[2] = bn > 0.0 ? rn / bn : rn;
+  const bool finite = isfinite(rn);
+  if (!finite) status[1] = 1;
+  cudaGraphSetConditional(cond, (finite && rn > sc[5]) ? 1u : 0u);
+}
+
+__global__ void k_cg_check(const double* __restrict__ sc, double* __restrict__ ctl, int maxiter, int* __restrict__ status,
+                           cudaGraphConditionalHandle cond) {
+  if (threadIdx.x != 0) return;
+  ctl[0] += 1.0;
+  const double rn = sqrt(sc[4]);
+  const bool finite = isfinite(rn);
+  if (!finite) status[1] = 1;
+  cudaGraphSetConditional(cond, (finite && rn > sc[5] && ctl[0] < (double)maxiter) ? 1u : 0u);
+}
+
+__global__ void k_cg_finish(const double* __restrict__ sc, const double* __restrict__ ctl, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  const double rn = sqrt(sc[4]), bn = sc[6];
+  out[0] = ctl[0];
+  out[1] = bn > 0.0 ? rn / bn : rn;
+  out[3] = (isfinite(rn) && rn > sc[5]) ? 1.0 : 0.0;
+}
+
 }  // namespace
+
+cudaError_t cg_start(double* sc, double* ctl, double tol, int* status, double* out, cudaGraphConditionalHandle cond,
+                     cudaStream_t s) {
+  k_cg_start<<<1, 32, 0, s>>>(sc, ctl, tol, status, out, cond);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_check(const double* sc, double* ctl, int maxiter, int* status, cudaGraphConditionalHandle cond,
+                     cudaStream_t s) {
+  k_cg_check<<<1, 32, 0, s>>>(sc, ctl, maxiter, status, cond);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_finish(const double* sc, const double* ctl, double* out, cudaStream_t s) {
+  k_cg_finish<<<1, 32, 0, s>>>(sc, ctl, out);
+  return cudaGetLastError();
+}
 
 cudaError_t body_points(const double* xb_body, const double* kin, const int* body_of, int nb, double* xb, double* vb,
                         cudaStream_t s) {

@@ -252,6 +252,12 @@ cudaError_t vec_dot(const double* a, const double* b, int n, double* out, cudaSt
 cudaError_t cg_update_xr(double* x, double* r, const double* p, const double* Ap, const double* sc, int n,
                          cudaStream_t s);
 cudaError_t cg_update_p(double* p, const double* r, double* sc, int n, cudaStream_t s);
+// device-side loop control of a captured CG (see cg.cu)
+cudaError_t cg_start(double* sc, double* ctl, double tol, int* status, double* out, cudaGraphConditionalHandle cond,
+                     cudaStream_t s);
+cudaError_t cg_check(const double* sc, double* ctl, int maxiter, int* status, cudaGraphConditionalHandle cond,
+                     cudaStream_t s);
+cudaError_t cg_finish(const double* sc, const double* ctl, double* out, cudaStream_t s);
 
 // ----------------------------------------------------------------------------------------------
 // dense linear algebra (linalg.cu)

@@ -161,13 +161,19 @@ __global__ void k_features(const double* __restrict__ kin, int nkin, const doubl
   }
 }
 
-// sample slot <- (raw features, F_n)
+// ring slot *next <- (raw features, F_n), then *next advances (one block; capturable, the slot
+// index lives on the device)
 __global__ void k_record(const float* __restrict__ x, int din, const double* __restrict__ fn, int nf,
-                         float* __restrict__ xs, float* __restrict__ ys) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < din + nf; i += gridDim.x * blockDim.x) {
+                         float* __restrict__ xs_all, float* __restrict__ ys_all, int* __restrict__ next, int cap) {
+  const int slot = *next;
+  float* xs = xs_all + (int64_t)slot * din;
+  float* ys = ys_all + (int64_t)slot * nf;
+  for (int i = threadIdx.x; i < din + nf; i += blockDim.x) {
     if (i < din) xs[i] = x[i];
     else ys[i - din] = (float)fn[i - din];
   }
+  __syncthreads();
+  if (threadIdx.x == 0) *next = (slot + 1) % cap;
 }
 
 // per-column mean and standard deviation over `count` rows (fixed order, one thread per column);
@@ -330,6 +336,7 @@ cudaError_t Mlp::init(int din_, int dout_, int hidden, int nhidden, int capacity
   A_(sd_y, sizeof(float) * dout_);
   A_(loss, sizeof(double) * 4);
   A_(idx, sizeof(int) * (size_t)cap);
+  A_(d_next, sizeof(int));
   act.assign(nl + 1, nullptr);
   dact.assign(nl + 1, nullptr);
   for (int l = 0; l <= nl; ++l) {
@@ -426,14 +433,21 @@ cudaError_t Mlp::features(const double* kin, int nkin, const double* f1, const d
   return cudaGetLastError();
 }
 
-cudaError_t Mlp::record(const double* fn) {
+cudaError_t Mlp::record_enqueue(const double* fn) {
   const int din = dims[0], nf = dims[nl];
-  const int slot = next;
+  k_record<<<1, 256, 0, stream>>>(feat, din, fn, nf, xs, ys, d_next, cap);
+  return cudaGetLastError();
+}
+
+void Mlp::record_commit() {
   next = (next + 1) % cap;
   count = std::min(count + 1, cap);
-  k_record<<<blocks_for(din + nf), 256, 0, stream>>>(feat, din, fn, nf, xs + (int64_t)slot * din,
-                                                     ys + (int64_t)slot * nf);
-  return cudaGetLastError();
+}
+
+cudaError_t Mlp::record(const double* fn) {
+  cudaError_t e = record_enqueue(fn);
+  if (e == cudaSuccess) record_commit();
+  return e;
 }
 
 cudaError_t Mlp::predict(const double* f1, const double* f2, double* fb) {

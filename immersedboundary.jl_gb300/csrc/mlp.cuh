@@ -32,6 +32,7 @@ struct Mlp {
   float *mu_x = nullptr, *sd_x = nullptr, *mu_y = nullptr, *sd_y = nullptr;
   double* loss = nullptr;
   int* idx = nullptr;
+  int* d_next = nullptr;  // device copy of next (the recording kernel advances it)
   bool trained = false;
   double blend = 1.0;    // weight of the network's correction (validated at training)
   double val_rel = -1;   // held-out squared error relative to plain extrapolation's (-1: none)
@@ -48,7 +49,9 @@ struct Mlp {
   cudaError_t adam_step(float lr);
   // per step: raw features from device kinematics and force history; record F_n; prediction
   cudaError_t features(const double* kin, int nkin, const double* f1, const double* f2, int nf);
-  cudaError_t record(const double* fn);
+  cudaError_t record(const double* fn);         // record_enqueue + record_commit
+  cudaError_t record_enqueue(const double* fn); // the device side (slot index on the device)
+  void record_commit();                         // the host mirror of count / next
   cudaError_t predict(const double* f1, const double* f2, double* fb);
   cudaError_t train(int epochs, int batch, float lr, uint64_t seed, double* final_loss);
   // loss and parameter gradients of the raw network on host rows (normalised inputs/targets)

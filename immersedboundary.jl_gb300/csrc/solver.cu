@@ -99,6 +99,14 @@ struct ib_handle {
   double *fb_prev = nullptr, *fb_last = nullptr;  // F_{n-2}, F_{n-1} at the start of a step
   double* cg_z = nullptr;                         // preconditioned residual
   learn::Mlp* mlp = nullptr;                      // learned warm start (ib_learn_init)
+  // the moving step as captured graphs (one per buffer parity), from the third step on
+  bool use_moving_graph = true;
+  cudaGraphExec_t mgexec[2] = {nullptr, nullptr};
+  uint64_t mg_key = 0;
+  cudaStream_t loop_stream = nullptr;             // capture stream of the CG loop body
+  double* h_mslot = nullptr;                      // pinned: base flux [2L] and kinematics [6 nbodies]
+  double* h_cgout = nullptr;                      // pinned: CG statistics of the last captured step
+  double *d_cgctl = nullptr, *d_cgout = nullptr;
   bool collect = false;                           // record (features, F_n) every moving step
   std::vector<double> cg_res0;                    // initial relative residual of each CG solve
   int precond = IB_PC_NONE;                       // moving-body CG preconditioner
@@ -628,6 +636,11 @@ void destroy_handle(ib_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& ge : h->gexec)
     if (ge) cudaGraphExecDestroy(ge);
+  for (auto& ge : h->mgexec)
+    if (ge) cudaGraphExecDestroy(ge);
+  if (h->h_mslot) cudaFreeHost(h->h_mslot);
+  if (h->h_cgout) cudaFreeHost(h->h_cgout);
+  if (h->loop_stream) cudaStreamDestroy(h->loop_stream);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_q0) cudaFreeHost(h->h_q0);
   if (h->h_sc) cudaFreeHost(h->h_sc);
@@ -727,6 +740,66 @@ int cg_solve(ib_handle* h) {
   return IB_OK;
 }
 
+// warm start (h->fb holds F_{n-1}, h->fb_prev F_{n-2}): the previous Fb (the reference's cg! on
+// qty.Fb), its linear extrapolation, zero, or the learned prediction (extrapolation until a
+// network is trained); keeps F_{n-1} in h->fb_last and the network's features
+cudaError_t enqueue_warm_start(ib_handle* h, bool hist2) {
+  cudaStream_t s = h->stream;
+  const size_t fbytes = sizeof(double) * h->nf;
+  CE(cudaMemcpyAsync(h->fb_last, h->fb, fbytes, cudaMemcpyDeviceToDevice, s));
+  const bool use_mlp = h->mlp && (h->collect || h->warm_start == IB_WARM_LEARNED);
+  if (use_mlp) CE(h->mlp->features(h->d_kin, 6 * h->nbodies, h->fb_last, h->fb_prev, h->nf));
+  switch (h->warm_start) {
+    case IB_WARM_ZERO: CE(cudaMemsetAsync(h->fb, 0, fbytes, s)); break;
+    case IB_WARM_EXTRAPOLATE:
+      if (hist2) CE(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
+      break;
+    case IB_WARM_LEARNED:
+      if (hist2 && h->mlp && h->mlp->trained) CE(h->mlp->predict(h->fb_last, h->fb_prev, h->fb));
+      else if (hist2) CE(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
+      break;
+    default: break;
+  }
+  return cudaSuccess;
+}
+
+// preconditioner: the inverse Schur matrix of the current configuration, assembled at the first
+// step and again every pc_refresh steps, or (pc_refresh = 0) once the iterations spent above
+// those of the first solve after the last assembly have cost as much time as an assembly
+int pc_maybe_assemble(ib_handle* h) {
+  if (h->precond != IB_PC_SCHUR_REF) return IB_OK;
+  const bool due = h->pc_step < 0 ||
+                   (h->pc_refresh > 0 ? h->steps - h->pc_step >= h->pc_refresh
+                                      : h->pc_excess_iters * h->cg_iter_s >= h->pc_assembly_s);
+  if (!due) return IB_OK;
+  const auto t_asm = std::chrono::steady_clock::now();
+  if (!h->bmat) {
+    const int64_t n2 = (int64_t)h->nf * h->nf;
+    CK(h->alloc(&h->bmat, n2));
+    CK(h->alloc(&h->binv_cm, n2));
+    CK(h->alloc(&h->binv_rm, n2));
+  }
+  int rc = assemble_schur(h);
+  if (rc != IB_OK) return rc;
+  rc = check_status(h);
+  if (rc != IB_OK) return rc;
+  h->pc_step = h->steps;
+  h->pc_base_iters = -1;
+  h->pc_excess_iters = 0.0;
+  h->pc_assemblies++;
+  h->pc_assembly_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_asm).count();
+  return IB_OK;
+}
+
+// the first solve after an assembly starts at the previous Fb of a changed matrix; the second
+// one (solve_step > pc_step) sets the base for the extra-iteration count
+void pc_account(ib_handle* h, int64_t solve_step) {
+  if (h->precond != IB_PC_SCHUR_REF || h->cg_iters.empty()) return;
+  const int it_now = h->cg_iters.back();
+  if (h->pc_base_iters < 0 && solve_step > h->pc_step) h->pc_base_iters = it_now;
+  else if (h->pc_base_iters >= 0) h->pc_excess_iters += std::max(0, it_now - h->pc_base_iters);
+}
+
 // advance! for rigidly moving bodies (corrected reference branch): points and weights from the
 // step's kinematics, the trial state, Fb by CG, stress, projection and Vort2Flux.
 template <typename S>
@@ -745,62 +818,15 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
   CK(vec_axpy(h->ftmp, h->vb, -g.h, h->nf, s));
   rc = check_status(h);
   if (rc != IB_OK) return rc;
-  // warm start (h->fb holds F_{n-1}, h->fb_prev F_{n-2}): the previous Fb (the reference's cg!
-  // on qty.Fb), its linear extrapolation, zero, or the learned prediction (extrapolation until a
-  // network is trained)
-  const size_t fbytes = sizeof(double) * h->nf;
   const bool hist2 = h->steps >= 2;
-  CK(cudaMemcpyAsync(h->fb_last, h->fb, fbytes, cudaMemcpyDeviceToDevice, s));
-  const bool use_mlp = h->mlp && (h->collect || h->warm_start == IB_WARM_LEARNED);
-  if (use_mlp) CK(h->mlp->features(h->d_kin, 6 * h->nbodies, h->fb_last, h->fb_prev, h->nf));
-  switch (h->warm_start) {
-    case IB_WARM_ZERO: CK(cudaMemsetAsync(h->fb, 0, fbytes, s)); break;
-    case IB_WARM_EXTRAPOLATE:
-      if (hist2) CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
-      break;
-    case IB_WARM_LEARNED:
-      if (hist2 && h->mlp && h->mlp->trained) CK(h->mlp->predict(h->fb_last, h->fb_prev, h->fb));
-      else if (hist2) CK(axpby<double>(h->fb, h->fb_prev, -1.0, 2.0, h->nf, s));
-      break;
-    default: break;
-  }
-  // preconditioner: the inverse Schur matrix of the current configuration, assembled at the first
-  // step and again every pc_refresh steps, or (pc_refresh = 0) once the iterations spent above
-  // those of the first solve after the last assembly have cost as much time as an assembly
-  if (h->precond == IB_PC_SCHUR_REF) {
-    const bool due = h->pc_step < 0 ||
-                     (h->pc_refresh > 0 ? h->steps - h->pc_step >= h->pc_refresh
-                                        : h->pc_excess_iters * h->cg_iter_s >= h->pc_assembly_s);
-    if (due) {
-      const auto t_asm = std::chrono::steady_clock::now();
-      if (!h->bmat) {
-        const int64_t n2 = (int64_t)h->nf * h->nf;
-        CK(h->alloc(&h->bmat, n2));
-        CK(h->alloc(&h->binv_cm, n2));
-        CK(h->alloc(&h->binv_rm, n2));
-      }
-      rc = assemble_schur(h);
-      if (rc != IB_OK) return rc;
-      rc = check_status(h);
-      if (rc != IB_OK) return rc;
-      h->pc_step = h->steps;
-      h->pc_base_iters = -1;
-      h->pc_excess_iters = 0.0;
-      h->pc_assemblies++;
-      h->pc_assembly_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_asm).count();
-    }
-  }
+  CK(enqueue_warm_start(h, hist2));
+  rc = pc_maybe_assemble(h);
+  if (rc != IB_OK) return rc;
   rc = cg_solve<S>(h);
   if (rc != IB_OK) return rc;
-  if (h->precond == IB_PC_SCHUR_REF) {
-    // the first solve after an assembly starts at the previous Fb of a changed matrix; the
-    // second one sets the base
-    const int it_now = h->cg_iters.back();
-    if (h->pc_base_iters < 0 && h->steps > h->pc_step) h->pc_base_iters = it_now;
-    else if (h->pc_base_iters >= 0) h->pc_excess_iters += std::max(0, it_now - h->pc_base_iters);
-  }
+  pc_account(h, h->steps);
   if (h->mlp && h->collect && hist2) CK(h->mlp->record(h->fb));
-  CK(cudaMemcpyAsync(h->fb_prev, h->fb_last, fbytes, cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(h->fb_prev, h->fb_last, sizeof(double) * h->nf, cudaMemcpyDeviceToDevice, s));
   CK(enqueue_stress(h));
   CK(enqueue_project<S>(h, p));
   h->parity ^= 1;
@@ -809,8 +835,165 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
   return check_status(h);
 }
 
+// ---- the moving step as a captured graph (steps >= 2) -------------------------------------------
+// Per parity one graph: staging copies of the base flux and kinematics from a pinned slot, the
+// body update, trial state, forcing, warm start, CG with a device-side convergence test (a
+// while-conditional node), stress, projection and Vort2Flux, and copies of the CG statistics and
+// status flags to pinned memory.  The host launches it, waits, and keeps the statistics, the
+// preconditioner policy and the error reporting of the eager step.
+
+template <typename S>
+int capture_moving(ib_handle* h, int p) {
+  const Geometry& g = h->g;
+  cudaStream_t s = h->stream;
+  const int L = g.nlev;
+  const size_t fbytes = sizeof(double) * h->nf;
+  const bool pc = h->precond == IB_PC_SCHUR_REF && h->binv_rm;
+  double *x = h->fb, *r = h->cg_r, *pv = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
+  double* z = pc ? h->cg_z : r;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  auto body = [&]() -> cudaError_t {
+    CE(cudaMemcpyAsync(h->d_q0, h->h_mslot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, s));
+    CE(cudaMemcpyAsync(h->d_kin, h->h_mslot + 2 * L, sizeof(double) * 6 * h->nbodies, cudaMemcpyHostToDevice, s));
+    CE(body_points(h->xb_body, h->d_kin, h->body_of, h->nb, h->xb, h->vb, s));
+    CE(reg_update(g, h->xb, h->nb, h->body_idx, h->weight, h->status, s));
+    CE(enqueue_trial<S>(h, p));
+    CE(reg_gather<S>(g, view<S>(h->qs1), h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, g.nq, h->nf, s));
+    CE(vec_axpy(h->ftmp, h->vb, -g.h, h->nf, s));
+    CE(enqueue_warm_start(h, true));
+    // CG start (as cg_solve)
+    CE(schur_apply<S>(h, x, Ap));
+    CE(cudaMemcpyAsync(r, h->ftmp, fbytes, cudaMemcpyDeviceToDevice, s));
+    CE(vec_axpy(r, Ap, -1.0, h->nf, s));
+    CE(vec_dot(r, r, h->nf, sc + 4, s));
+    CE(vec_dot(h->ftmp, h->ftmp, h->nf, sc + 3, s));
+    if (pc) CE(gemv_rowmajor(h->binv_rm, r, z, h->nf, s));
+    CE(vec_dot(r, z, h->nf, sc + 0, s));
+    CE(cudaMemcpyAsync(pv, z, fbytes, cudaMemcpyDeviceToDevice, s));
+    // while-conditional node: the loop body is captured on the side stream into its graph
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t ndeps = 0;
+    CE(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, &edges, &ndeps));
+    cudaGraphConditionalHandle cond;
+    CE(cudaGraphConditionalHandleCreate(&cond, cg, 0, cudaGraphCondAssignDefault));
+    CE(cg_start(sc, h->d_cgctl, h->cg_tol, h->status, h->d_cgout, cond, s));
+    CE(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, &edges, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CE(cudaGraphAddNode(&node, cg, deps, edges, ndeps, &cp));
+    cudaGraph_t loop = cp.conditional.phGraph_out[0];
+    CE(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaStream_t ls = h->loop_stream;
+    CE(cudaStreamBeginCaptureToGraph(ls, loop, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    h->stream = ls;
+    cudaError_t le = [&]() -> cudaError_t {
+      CE(schur_apply<S>(h, pv, Ap));
+      CE(vec_dot(pv, Ap, h->nf, sc + 1, ls));
+      CE(cg_update_xr(x, r, pv, Ap, sc, h->nf, ls));
+      CE(vec_dot(r, r, h->nf, sc + 4, ls));
+      if (pc) CE(gemv_rowmajor(h->binv_rm, r, z, h->nf, ls));
+      CE(vec_dot(r, z, h->nf, sc + 2, ls));
+      CE(cg_update_p(pv, z, sc, h->nf, ls));
+      return cg_check(sc, h->d_cgctl, h->cg_maxiter, h->status, cond, ls);
+    }();
+    h->stream = s;
+    cudaGraph_t loop_out = nullptr;
+    cudaError_t le2 = cudaStreamEndCapture(ls, &loop_out);
+    CE(le);
+    CE(le2);
+    CE(cg_finish(sc, h->d_cgctl, h->d_cgout, s));
+    if (h->mlp && h->collect) CE(h->mlp->record_enqueue(h->fb));
+    CE(cudaMemcpyAsync(h->fb_prev, h->fb_last, fbytes, cudaMemcpyDeviceToDevice, s));
+    CE(enqueue_stress(h));
+    CE(enqueue_project<S>(h, p));
+    CE(cudaMemcpyAsync(h->h_cgout, h->d_cgout, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+    return cudaSuccess;
+  };
+  cudaError_t e = body();
+  h->stream = s;
+  cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+  if (e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return fail(h, IB_ERR_CUDA, "moving-step capture", e);
+  }
+  if (e2 != cudaSuccess) return fail(h, IB_ERR_CUDA, "moving-step capture", e2);
+  if (h->mgexec[p]) {
+    cudaGraphExecDestroy(h->mgexec[p]);
+    h->mgexec[p] = nullptr;
+  }
+  e = cudaGraphInstantiate(&h->mgexec[p], graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "moving-step graph instantiate", e);
+  return IB_OK;
+}
+
+// what the captured moving step depends on besides the device buffers
+uint64_t moving_graph_key(const ib_handle* h) {
+  uint64_t k = (uint64_t)h->warm_start;
+  k = k * 31 + (uint64_t)h->precond;
+  k = k * 31 + (uint64_t)(h->binv_rm != nullptr);
+  k = k * 31 + (uint64_t)(h->mlp != nullptr);
+  k = k * 31 + (uint64_t)h->collect;
+  k = k * 31 + (uint64_t)(h->mlp && h->mlp->trained);
+  k = k * 31 + (uint64_t)h->cg_maxiter;
+  uint64_t tb;
+  std::memcpy(&tb, &h->cg_tol, sizeof(tb));
+  k = k * 31 + tb;
+  return k;
+}
+
+template <typename S>
+int moving_step_graph(ib_handle* h, double t, double u, double v, const double* kin) {
+  const Geometry& g = h->g;
+  // base flux and kinematics of this step into the pinned slot the graphs copy from (the
+  // previous launch is complete: every step ends with a synchronisation)
+  for (int l = 0; l < g.nlev; ++l) {
+    const double hc = g.h * std::ldexp(1.0, l);  // base_flux!, fluid-ops.jl:414-415
+    h->h_mslot[2 * l] = u * hc;
+    h->h_mslot[2 * l + 1] = v * hc;
+  }
+  std::memcpy(h->h_mslot + 2 * g.nlev, kin, sizeof(double) * 6 * h->nbodies);
+  int rc = pc_maybe_assemble(h);
+  if (rc != IB_OK) return rc;
+  const uint64_t key = moving_graph_key(h);
+  if (!h->mgexec[0] || key != h->mg_key) {
+    for (int p = 0; p < 2; ++p) {
+      rc = capture_moving<S>(h, p);
+      if (rc != IB_OK) return rc;
+    }
+    h->mg_key = key;
+  }
+  CK(cudaGraphLaunch(h->mgexec[h->parity], h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  const double* o = h->h_cgout;
+  h->cg_iters.push_back((int)o[0]);
+  h->cg_res.push_back(o[1]);
+  h->cg_res0.push_back(o[2]);
+  if (h->mlp && h->collect) h->mlp->record_commit();
+  pc_account(h, h->steps);
+  h->parity ^= 1;
+  h->steps++;
+  h->t = t;
+  rc = check_status(h);
+  if (rc != IB_OK) return rc;
+  if (o[3] != 0.0) return fail(h, IB_ERR_CG_MAXITER, "Schur CG reached its iteration cap");
+  return IB_OK;
+}
+
 int moving_step_mode(ib_handle* h, double t, double u, double v, const double* kin) {
-  return h->precision == IB_PREC_MIXED ? moving_step<df64>(h, t, u, v, kin) : moving_step<double>(h, t, u, v, kin);
+  // the first two steps (no force history yet, first preconditioner) run eagerly
+  const bool graph = h->use_moving_graph && h->steps >= 2 && (h->precond != IB_PC_SCHUR_REF || h->pc_step >= 0);
+  if (h->precision == IB_PREC_MIXED)
+    return graph ? moving_step_graph<df64>(h, t, u, v, kin) : moving_step<df64>(h, t, u, v, kin);
+  return graph ? moving_step_graph<double>(h, t, u, v, kin) : moving_step<double>(h, t, u, v, kin);
 }
 
 int one_step(ib_handle* h, double t, double u, double v) {
@@ -1025,7 +1208,19 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     } else {
       AL(h->xb_body, 2 * nb); AL(h->vb, 2 * nb); AL(h->d_kin, 6 * h->nbodies); AL(h->body_of, nb);
       AL(h->cg_r, h->nf); AL(h->cg_p, h->nf); AL(h->cg_Ap, h->nf); AL(h->cg_sc, 8); AL(h->fb_prev, h->nf);
-      AL(h->fb_last, h->nf); AL(h->cg_z, h->nf);
+      AL(h->fb_last, h->nf); AL(h->cg_z, h->nf); AL(h->d_cgctl, 4); AL(h->d_cgout, 4);
+      if ((e = cudaMallocHost(&h->h_mslot, sizeof(double) * (2 * L + 6 * h->nbodies))) != cudaSuccess) {
+        h->h_mslot = nullptr;
+        return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
+      }
+      if ((e = cudaMallocHost(&h->h_cgout, sizeof(double) * 4)) != cudaSuccess) {
+        h->h_cgout = nullptr;
+        return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
+      }
+      if ((e = cudaStreamCreateWithFlags(&h->loop_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        h->loop_stream = nullptr;
+        return bail(fail(h, IB_ERR_CUDA, "cudaStreamCreate", e));
+      }
       AL(h->Gw, L * nG); AL(h->Pw, L * nG); AL(h->qw, g.nq); AL(h->rings_w, (int64_t)L * g.nbc);
       if ((e = cudaMallocHost(&h->h_sc, sizeof(double) * 8)) != cudaSuccess) {
         h->h_sc = nullptr;
@@ -1062,7 +1257,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     rc = check_status(h);
     if (rc != IB_OK) return bail(rc);
   }
-  if (h->motion == IB_MOTION_PRESCRIBED) h->use_graph = false;
+  if (h->motion == IB_MOTION_PRESCRIBED) {
+    h->use_moving_graph = h->use_graph;  // IBGB300_NO_GRAPH=1 keeps every moving step eager
+    h->use_graph = false;
+  }
   if (h->use_graph) {
     int rc = capture_graphs(h);
     if (rc != IB_OK) return bail(rc);

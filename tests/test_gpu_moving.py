@@ -110,3 +110,36 @@ def test_schur_preconditioned_cg_same_answer_fewer_iterations(ib, precision):
     assert rel(out["schur_ref"][1], out["none"][1]) < 1e-7
     assert out["schur_ref"][3][0] >= 1
     assert out["schur_ref"][2] < 0.5 * out["none"][2], (out["schur_ref"][2], out["none"][2])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_captured_moving_step_equals_eager(ib, monkeypatch, precision):
+    """From the third step on a moving step runs as a captured graph with the CG loop driven
+    on the device; it gives the eager step's iterates (IBGB300_NO_GRAPH=1) exactly."""
+    wl = small_heaving(ib, nsteps=10)
+    wl.dt = 0.005
+    out = {}
+    for mode in ("graph", "eager"):
+        if mode == "eager":
+            monkeypatch.setenv("IBGB300_NO_GRAPH", "1")
+        else:
+            monkeypatch.delenv("IBGB300_NO_GRAPH", raising=False)
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision=precision)
+        s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+        s.set_cg_preconditioner("schur_ref")
+        s.vort2flux(st)
+        for i in range(wl.nsteps):
+            ib.advance_(st, s, i * wl.dt)
+        it, res, r0 = s.cg_stats(wl.nsteps, start=True)
+        out[mode] = (st.qty.gamma.copy(), st.qty.Fb.copy(), it, res, r0)
+        s.close()
+    g1, f1, it1, res1, r01 = out["graph"]
+    g2, f2, it2, res2, r02 = out["eager"]
+    np.testing.assert_array_equal(it1, it2)
+    np.testing.assert_array_equal(g1, g2)
+    np.testing.assert_array_equal(f1, f2)
+    np.testing.assert_array_equal(res1, res2)
+    assert np.all(res1 <= 1e-10)

@@ -165,60 +165,88 @@ def run_moving_config(ib, wl, quick=False):
     }
 
 
-def run_ensemble_config(ib, lib, n=96, K=20, W=3):
-    """n independent members (mixed precision) advanced by one graph launch per step, against
-    the plain FP64 GPU path stepping the same members one at a time."""
-    ws = ib.workloads.ensemble(n)
+def ensemble_member(ib, w, precision, plain=False):
+    prob = w.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = w.initial_gamma()
+    s = ib.initsolver(prob, st, precision=precision)
+    if s.moving:
+        if plain:
+            s.set_cg_options(tol=1e-10, warm_start="previous")   # the reference's cg! on qty.Fb
+        else:
+            s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+            s.set_cg_preconditioner("schur_ref")
+    s.vort2flux(st)
+    return st, s
+
+
+def run_ensemble_config(ib, lib, n=96, K=20, W=3, moving=True):
+    """n independent members (with `moving`, every other one pitching) advanced by one graph
+    launch per step in mixed precision, against the plain FP64 GPU path stepping the same
+    members one at a time (moving ones with the reference's CG: no preconditioner, previous-Fb
+    start)."""
+    ws = ib.workloads.ensemble(n, moving=moving)
     cells = sum(w.cells_per_step for w in ws)
     a = time.perf_counter()
-    runs = []
-    for w in ws:
-        prob = w.problem()
-        st = ib.initstate(prob)
-        st._gamma[:] = w.initial_gamma()
-        s = ib.initsolver(prob, st, precision="mixed")
-        s.vort2flux(st)
-        runs.append(s)
+    runs = [ensemble_member(ib, w, "mixed") for w in ws]
+    # moving members take their first two steps on their own (force history, preconditioner);
+    # every member does, so that all share the step count
+    for w, (st, s) in zip(ws, runs):
+        for k in range(2):
+            ib.advance_(st, s, k * w.dt)
     setup = time.perf_counter() - a
-    ens = ib.Ensemble(runs)
+    ens = ib.Ensemble([s for _, s in runs])
     members, kernels = ens.info()
-    ts = np.arange(W + K) * 1e-3
-    ens.advance_n(ts[:W])
-    ms = ens.advance_n(ts[W:]) / K
+    times = np.array([[(2 + k) * w.dt for w in ws] for k in range(W + K)])
+    ens.advance_n(times[:W], states=[st for st, _ in runs])
+    ms = ens.advance_n(times[W:], states=[st for st, _ in runs]) / K
     ens.close()
-    for s in runs:
+    iters = [float(np.mean(s.cg_stats(K)[0])) for (st, s) in runs if s.moving]
+    iters_max = [int(np.max(s.cg_stats(K)[0])) for (st, s) in runs if s.moving]
+    for _, s in runs:
         s.close()
-    # plain FP64 GPU path, one member at a time (device time of each member's own graph replays)
+    # plain FP64 GPU path, one member at a time
     t64 = 0.0
+    plain_iters = []
     for w in ws:
-        prob = w.problem()
-        st = ib.initstate(prob)
-        st._gamma[:] = w.initial_gamma()
-        s = ib.initsolver(prob, st, precision="fp64")
-        s.vort2flux(st)
-        m = 8
-        tt = np.ascontiguousarray(np.arange(m + 2) * 1e-3)
-        uv = np.ascontiguousarray(np.tile(np.array(w.freestream, dtype=np.float64), m + 2))
-        dp = C.POINTER(C.c_double)
-        s._check(lib.ib_advance_n(s.handle, 2, tt.ctypes.data_as(dp), uv.ctypes.data_as(dp)))
-        dms = C.c_double()
-        s._check(lib.ib_advance_n_timed(s.handle, m, tt[2:].ctypes.data_as(dp), uv[4:].ctypes.data_as(dp),
-                                        C.byref(dms)))
-        t64 += dms.value / m
+        st, s = ensemble_member(ib, w, "fp64", plain=True)
+        m = 4 if s.moving else 8
+        for k in range(2):
+            ib.advance_(st, s, k * w.dt)
+        lib.ib_synchronize(s.handle)
+        a = time.perf_counter()
+        if s.moving:
+            for k in range(m):
+                ib.advance_(st, s, (2 + k) * w.dt)
+            lib.ib_synchronize(s.handle)
+            t64 += (time.perf_counter() - a) * 1e3 / m
+            plain_iters.append(float(np.mean(s.cg_stats(m)[0])))
+        else:
+            tt = np.ascontiguousarray((2 + np.arange(m)) * w.dt)
+            uv = np.ascontiguousarray(np.tile(np.array(w.freestream, dtype=np.float64), m))
+            dp = C.POINTER(C.c_double)
+            dms = C.c_double()
+            s._check(lib.ib_advance_n_timed(s.handle, m, tt.ctypes.data_as(dp), uv.ctypes.data_as(dp),
+                                            C.byref(dms)))
+            t64 += dms.value / m
         s.close()
     from collections import Counter
     grids = Counter(f"{w.nx}x{w.ny}" for w in ws)
     return {
-        "workload": f"ensemble of {members} static members: grids {dict(grids)}, 3-5 levels, ellipses "
-                    "(aspect U[0.1,1], angle U[0,40] deg, points ~h), Re log-uniform [50,500], dt=0.2h",
+        "workload": f"ensemble of {members} members ({len(iters)} pitching 15 deg about mid-chord at f=U[0.1,0.3]): "
+                    f"grids {dict(grids)}, 3-5 levels, ellipses (aspect U[0.1,1], angle U[0,40] deg, points ~h), "
+                    "Re log-uniform [50,500], dt=0.2h",
         "value": cells / (ms / 1e3), "unit": "cell-steps/s", "ms_per_step": ms,
-        "arm": "mixed precision, all members in one CUDA graph launch per step",
+        "arm": "mixed precision, all members in one CUDA graph launch per step (moving members: "
+               "Schur-preconditioned CG loop inside the graph)",
         "kernels_per_launch": kernels, "setup_s": setup,
+        "cg_iterations_per_step_moving": float(np.mean(iters)) if iters else None,
+        "cg_iterations_max_member": max(iters_max) if iters_max else None,
+        "note": "members step in lockstep: a step lasts as long as its slowest member's CG",
         "plain_fp64": {"value": cells / (t64 / 1e3), "ms_per_step": t64,
-                       "arm": "FP64, one member at a time (each its own graph)"},
+                       "arm": "FP64, one member at a time (moving: plain CG from the previous Fb)",
+                       "cg_iterations_per_step_moving": float(np.mean(plain_iters)) if plain_iters else None},
         "speedup_vs_plain_fp64": t64 / ms, "steps": K,
-        "note": "the pitching half of the proposed ensemble is not in the graph: moving bodies "
-                "use the host-checked CG loop",
     }
 
 
@@ -502,6 +530,7 @@ def run_ours(args, rank, world, local):
             "four_cylinders": run_static_config(ib, lib, L, ib.workloads.four_cylinders(), 60, 3, local, dist),
             "heaving_plate": run_moving_config(ib, ib.workloads.heaving_plate()),
             "ensemble": run_ensemble_config(ib, lib),
+            "ensemble_static": run_ensemble_config(ib, lib, moving=False),
         }
     if rank == 0 and not args.no_cpu_baseline:
         v, sec, cores = cpu_reference(ib, wl, args.cpu_steps, 1)

@@ -641,9 +641,10 @@ def advance_(state: State, solver: Solver, t: float):
 
 
 class Ensemble:
-    """Independent static-body simulations advanced together by one graph launch per step
-    (include/ibgb300_ensemble.h; no reference counterpart).  Members keep their own state;
-    ``state`` objects are refreshed lazily like after ``advance_``."""
+    """Independent simulations advanced together by one graph launch per step
+    (include/ibgb300_ensemble.h; no reference counterpart).  Moving members join after their
+    first two steps.  Members keep their own state; ``state`` objects are refreshed lazily like
+    after ``advance_``."""
 
     def __init__(self, solvers: Sequence[Solver]):
         self.solvers = list(solvers)
@@ -665,17 +666,32 @@ class Ensemble:
         return n.value, k.value
 
     def advance_n(self, ts, uv=None, states: Sequence[State] | None = None) -> float:
-        """Advance every member through the times ``ts`` (freestream per member and step in
-        ``uv`` [len(ts)][members][2], default each member's problem freestream); returns the
-        device milliseconds."""
-        ts = np.ascontiguousarray(ts, dtype=np.float64)
+        """Advance every member through the times ``ts``: [nsteps] (the same times for every
+        member) or [nsteps][members] (each member's own times, e.g. t0 + k dt of its scheme);
+        freestream per member and step in ``uv`` [nsteps][members][2] (default: each member's
+        problem freestream at its time).  Returns the device milliseconds."""
+        ts = np.asarray(ts, dtype=np.float64)
+        n = len(self.solvers)
+        if ts.ndim == 1:
+            ts = np.repeat(ts[:, None], n, axis=1)
+        ts = np.ascontiguousarray(ts)
         if uv is None:
-            uv = np.array([[s.prob.fluid.freestream(float(t)) for s in self.solvers] for t in ts], dtype=np.float64)
+            uv = np.array([[s.prob.fluid.freestream(float(ts[k, i])) for i, s in enumerate(self.solvers)]
+                           for k in range(ts.shape[0])], dtype=np.float64)
         uv = np.ascontiguousarray(uv, dtype=np.float64)
         ms = C.c_double()
-        self._check(self.lib.ib_ensemble_advance_n(self.handle, len(ts), _lib.dptr(ts), _lib.dptr(uv), C.byref(ms)))
+        movers = [i for i, s in enumerate(self.solvers) if s.moving]
+        if movers:
+            kin = np.ascontiguousarray(np.concatenate(
+                [np.concatenate([self.solvers[i].kinematics(float(ts[k, i])).reshape(-1) for i in movers])
+                 for k in range(ts.shape[0])]))
+            self._check(self.lib.ib_ensemble_advance_n_kin(self.handle, len(ts), _lib.dptr(ts), _lib.dptr(uv),
+                                                           _lib.dptr(kin), C.byref(ms)))
+        else:
+            self._check(self.lib.ib_ensemble_advance_n(self.handle, len(ts), _lib.dptr(ts), _lib.dptr(uv),
+                                                       C.byref(ms)))
         for k, s in enumerate(self.solvers):
-            s._after_ensemble(float(ts[-1]) if len(ts) else None, states[k] if states else None)
+            s._after_ensemble(float(ts[-1, k]) if len(ts) else None, states[k] if states else None)
         return ms.value
 
     def close(self):

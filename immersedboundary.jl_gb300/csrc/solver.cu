@@ -842,8 +842,10 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
 // status flags to pinned memory.  The host launches it, waits, and keeps the statistics, the
 // preconditioner policy and the error reporting of the eager step.
 
+// Records the moving step for buffer parity p into the capture h->stream belongs to (its own,
+// or an ensemble's that it joined).
 template <typename S>
-int capture_moving(ib_handle* h, int p) {
+cudaError_t enqueue_moving_captured(ib_handle* h, int p) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   const int L = g.nlev;
@@ -851,8 +853,6 @@ int capture_moving(ib_handle* h, int p) {
   const bool pc = h->precond == IB_PC_SCHUR_REF && h->binv_rm;
   double *x = h->fb, *r = h->cg_r, *pv = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
   double* z = pc ? h->cg_z : r;
-  cudaGraph_t graph = nullptr;
-  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   auto body = [&]() -> cudaError_t {
     CE(cudaMemcpyAsync(h->d_q0, h->h_mslot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, s));
     CE(cudaMemcpyAsync(h->d_kin, h->h_mslot + 2 * L, sizeof(double) * 6 * h->nbodies, cudaMemcpyHostToDevice, s));
@@ -919,6 +919,15 @@ int capture_moving(ib_handle* h, int p) {
   };
   cudaError_t e = body();
   h->stream = s;
+  return e;
+}
+
+template <typename S>
+int capture_moving(ib_handle* h, int p) {
+  cudaStream_t s = h->stream;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = enqueue_moving_captured<S>(h, p);
   cudaError_t e2 = cudaStreamEndCapture(s, &graph);
   if (e != cudaSuccess) {
     if (graph) cudaGraphDestroy(graph);
@@ -1872,6 +1881,8 @@ struct ib_ensemble {
   bool launched[2] = {false, false};
   int parity = 0;
   int kernels_per_step = 0;
+  bool any_moving = false;
+  std::vector<uint64_t> keys;        // moving members' capture keys at capture time
   std::string err;
 };
 
@@ -1921,10 +1932,17 @@ int capture_ensemble(ib_ensemble* e, int p) {
   for (size_t i = 0; i < e->m.size() && ce == cudaSuccess; ++i) {
     ib_handle* h = e->m[i];
     ce = cudaStreamWaitEvent(h->stream, e->start, 0);
-    if (ce == cudaSuccess)
-      ce = cudaMemcpyAsync(h->d_q0, e->h_q0 + p * e->slot_len + e->q0_off[i], sizeof(double) * 2 * h->g.nlev,
-                           cudaMemcpyHostToDevice, h->stream);
-    if (ce == cudaSuccess) ce = enqueue_step_mode(h, h->parity ^ p);
+    if (h->motion == IB_MOTION_PRESCRIBED) {
+      // the member's own staging slot holds this step's base flux and kinematics
+      if (ce == cudaSuccess)
+        ce = h->precision == IB_PREC_MIXED ? enqueue_moving_captured<df64>(h, h->parity ^ p)
+                                           : enqueue_moving_captured<double>(h, h->parity ^ p);
+    } else {
+      if (ce == cudaSuccess)
+        ce = cudaMemcpyAsync(h->d_q0, e->h_q0 + p * e->slot_len + e->q0_off[i], sizeof(double) * 2 * h->g.nlev,
+                             cudaMemcpyHostToDevice, h->stream);
+      if (ce == cudaSuccess) ce = enqueue_step_mode(h, h->parity ^ p);
+    }
     if (ce == cudaSuccess) ce = cudaEventRecord(e->join[i], h->stream);
     if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->join[i], 0);
   }
@@ -1961,8 +1979,10 @@ int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) 
   for (int i = 0; i < n; ++i) {
     const ib_handle* h = members[i];
     if (!h) return efail(nullptr, IB_ERR_INVALID, "ensemble: null member");
-    if (h->motion != IB_MOTION_STATIC)
-      return efail(nullptr, IB_ERR_UNSUPPORTED, "ensemble members must have bodies fixed in the grid");
+    if (h->motion == IB_MOTION_PRESCRIBED &&
+        (!h->use_moving_graph || h->steps < 2 || (h->precond == IB_PC_SCHUR_REF && h->pc_step < 0)))
+      return efail(nullptr, IB_ERR_UNSUPPORTED,
+                   "a moving member joins after its first two steps (and first preconditioner), with graphs enabled");
     if (h->device != members[0]->device || h->steps != members[0]->steps)
       return efail(nullptr, IB_ERR_INVALID, "ensemble members must share the device and the step count");
     for (int j = 0; j < i; ++j)
@@ -1982,6 +2002,12 @@ int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) 
   };
   if (ce != cudaSuccess) return bail(efail(e, IB_ERR_CUDA, "cudaSetDevice", ce));
   for (ib_handle* h : e->m) {
+    if (h->motion == IB_MOTION_PRESCRIBED) {
+      e->any_moving = true;
+      e->keys.push_back(moving_graph_key(h));
+    } else {
+      e->keys.push_back(0);
+    }
     e->q0_off.push_back(e->slot_len);
     e->slot_len += 2 * h->g.nlev;
     if ((ce = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(efail(e, IB_ERR_CUDA, "member sync", ce));
@@ -2023,8 +2049,18 @@ int ib_ensemble_destroy(ib_ensemble* e) {
 }
 
 int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, double* device_ms) {
+  if (e && e->any_moving) return efail(e, IB_ERR_INVALID, "moving members need kinematics (ib_ensemble_advance_n_kin)");
+  return ib_ensemble_advance_n_kin(e, nsteps, t, uv, nullptr, device_ms);
+}
+
+int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, const double* kin,
+                              double* device_ms) {
   if (!e || nsteps < 0 || (nsteps > 0 && (!t || !uv))) return IB_ERR_INVALID;
+  if (e->any_moving && nsteps > 0 && !kin) return efail(e, IB_ERR_INVALID, "moving members need kinematics");
   EK(cudaSetDevice(e->device));
+  int kin_per_step = 0;
+  for (ib_handle* h : e->m)
+    if (h->motion == IB_MOTION_PRESCRIBED) kin_per_step += 6 * h->nbodies;
   const int n = (int)e->m.size();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (device_ms) {
@@ -2037,23 +2073,50 @@ int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const
     // the launch that read this slot two steps ago must be done before the slot is rewritten
     if (e->launched[p]) EK(cudaEventSynchronize(e->done[p]));
     double* slot = e->h_q0 + (size_t)p * e->slot_len;
+    const double* ks = kin ? kin + (size_t)s * kin_per_step : nullptr;
     for (int i = 0; i < n; ++i) {
-      const ib_handle* h = e->m[i];
+      ib_handle* h = e->m[i];
       const double u = uv[((size_t)s * n + i) * 2], v = uv[((size_t)s * n + i) * 2 + 1];
+      double* dst = h->motion == IB_MOTION_PRESCRIBED ? h->h_mslot : slot + e->q0_off[i];
       for (int l = 0; l < h->g.nlev; ++l) {
         const double hc = h->g.h * std::ldexp(1.0, l);  // base_flux!, fluid-ops.jl:414-415
-        slot[e->q0_off[i] + 2 * l] = u * hc;
-        slot[e->q0_off[i] + 2 * l + 1] = v * hc;
+        dst[2 * l] = u * hc;
+        dst[2 * l + 1] = v * hc;
+      }
+      if (h->motion == IB_MOTION_PRESCRIBED) {
+        std::memcpy(h->h_mslot + 2 * h->g.nlev, ks, sizeof(double) * 6 * h->nbodies);
+        ks += 6 * h->nbodies;
+        // preconditioner re-assembly between launches, on the member's own stream
+        int rc = pc_maybe_assemble(h);
+        if (rc != IB_OK) return efail(e, rc, "member " + std::to_string(i) + ": " + h->err);
+        if (moving_graph_key(h) != e->keys[i])
+          return efail(e, IB_ERR_INVALID, "member " + std::to_string(i) + " changed its CG options inside the ensemble");
       }
     }
     EK(cudaGraphLaunch(e->gexec[p], e->stream));
     EK(cudaEventRecord(e->done[p], e->stream));
     e->launched[p] = true;
     e->parity ^= 1;
-    for (ib_handle* h : e->m) {
+    if (e->any_moving) {
+      // moving members: the step's CG statistics came back through pinned memory
+      EK(cudaStreamSynchronize(e->stream));
+      for (int i = 0; i < n; ++i) {
+        ib_handle* h = e->m[i];
+        if (h->motion != IB_MOTION_PRESCRIBED) continue;
+        const double* o = h->h_cgout;
+        h->cg_iters.push_back((int)o[0]);
+        h->cg_res.push_back(o[1]);
+        h->cg_res0.push_back(o[2]);
+        if (h->mlp && h->collect) h->mlp->record_commit();
+        pc_account(h, h->steps);
+        if (o[3] != 0.0) return efail(e, IB_ERR_CG_MAXITER, "member " + std::to_string(i) + ": Schur CG iteration cap");
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      ib_handle* h = e->m[i];
       h->parity ^= 1;
       h->steps++;
-      h->t = t[s];
+      h->t = t[(size_t)s * n + i];
     }
   }
   if (device_ms) {

@@ -17,7 +17,8 @@ seeded initial vorticity noise (NumPy PCG64), identical for the GPU path and the
 * ``ensemble``         independent members: finest grid drawn from {128x128, 256x256,
                        384x256, 512x512}, h = 4/nx, 3-5 levels, an ellipse of chord 1 with aspect
                        ratio U[0.1, 1] at U[0, 40] deg (points ~h apart), Re log-uniform in
-                       [50, 500], dt = 0.2 h (bodies fixed in the grid)
+                       [50, 500], dt = 0.2 h; every other member pitches about mid-chord at
+                       15 deg amplitude and frequency U[0.1, 0.3] (moving=True)
 * ``scaled(...)``      the same bodies on coarser grids, for tests
 """
 from __future__ import annotations
@@ -123,7 +124,15 @@ def ellipse(center, chord: float, aspect: float, angle_deg: float, h: float, fra
     return RigidBody(frame or GridFrame(), xb, np.full(n, s[-1] / n))
 
 
-def ensemble(n: int = 96, nsteps: int = 1000, seed: int = 0) -> list[Workload]:
+def pitch_frame(f: float, amp_deg: float = 15.0) -> RelativeFrame:
+    """Pitching about the frame origin: theta = A sin(2 pi f t)."""
+    w = 2 * math.pi * f
+    a = math.radians(amp_deg)
+    return RelativeFrame(GridFrame(), r=lambda t: (0.0, 0.0), v=lambda t: (0.0, 0.0),
+                         theta=lambda t: a * math.sin(w * t), omega=lambda t: a * w * math.cos(w * t))
+
+
+def ensemble(n: int = 96, nsteps: int = 1000, seed: int = 0, moving: bool = False) -> list[Workload]:
     rng = np.random.default_rng(seed)
     grids = [(128, 128), (256, 256), (384, 256), (512, 512)]
     out = []
@@ -134,7 +143,9 @@ def ensemble(n: int = 96, nsteps: int = 1000, seed: int = 0) -> list[Workload]:
         aspect = float(rng.uniform(0.1, 1.0))
         angle = float(rng.uniform(0.0, 40.0))
         re = float(np.exp(rng.uniform(np.log(50.0), np.log(500.0))))
-        body = ellipse((0.0, 0.0), 1.0, aspect, angle, h)
+        f = float(rng.uniform(0.1, 0.3))
+        frame = pitch_frame(f) if (moving and k % 2 == 1) else None
+        body = ellipse((0.0, 0.0), 1.0, aspect, angle, h, frame=frame)
         out.append(Workload(f"member{k}", h, (-1.5, 2.5), (-ny * h / 2, ny * h / 2), L, re, 0.2 * h, nsteps,
                             [body], seed=seed + k))
     return out

@@ -1,13 +1,16 @@
 /* libibgb300: ensembles of independent simulations stepped by one graph launch.
  *
  * No reference counterpart (the reference advances one problem per solve! call).  An ensemble
- * groups handles created by ib_create (any grid sizes, levels, bodies and precisions; bodies
- * fixed in the grid; same device; same step count) and captures their advance! steps as
- * parallel branches of one CUDA graph, so that one launch advances every member by one step
- * and their kernels share the GPU.  Each member's freestream value enters through a captured
- * host-to-device copy from a pinned slot (two slots, one per buffer parity).  The members'
- * own state, history and error reporting work as for single handles; a member must not be
- * advanced on its own while it belongs to an ensemble.
+ * groups handles created by ib_create (any grid sizes, levels, bodies and precisions; same
+ * device; same step count) and captures their advance! steps as parallel branches of one CUDA
+ * graph, so that one launch advances every member by one step and their kernels share the GPU.
+ * Each member's freestream value (and, for moving bodies, kinematics) enters through captured
+ * host-to-device copies from pinned slots.  Moving members run their CG loop inside the graph
+ * (a device-side convergence test), join after their first two steps (and first preconditioner
+ * assembly) and keep their CG options while in the ensemble; the host reads their CG statistics
+ * after every step and re-assembles preconditioners between launches.  The members' own state,
+ * history and error reporting work as for single handles; a member must not be advanced on its
+ * own while it belongs to an ensemble.
  */
 #ifndef IBGB300_ENSEMBLE_H
 #define IBGB300_ENSEMBLE_H
@@ -23,9 +26,15 @@ typedef struct ib_ensemble ib_ensemble;
 int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out);
 int ib_ensemble_destroy(ib_ensemble* e);
 
-/* nsteps steps of every member: t[nsteps] (common times), uv[nsteps][n][2] (freestream per
- * member and step); device_ms (optional) receives the device time of the steps */
+/* nsteps steps of every member: t[nsteps][n] (each member's time of the step; members may have
+ * different time steps), uv[nsteps][n][2] (freestream per member and step); device_ms
+ * (optional) receives the device time of the steps */
 int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, double* device_ms);
+
+/* the same with moving members: kin[nsteps][6 per body of each moving member, in member
+ * order] = r0x, r0y, v0x, v0y, theta, Omega (as ib_advance_kin) */
+int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, const double* kin,
+                              double* device_ms);
 
 /* kernel launches per ensemble step (graph kernel nodes over all members) */
 int ib_ensemble_info(ib_ensemble* e, int32_t* members, int32_t* kernels_per_step);

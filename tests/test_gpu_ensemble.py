@@ -56,11 +56,56 @@ def test_ensemble_steps_equal_single_steps(ib):
         r[2].close()
 
 
-def test_ensemble_rejects_moving_members(ib):
-    wl = ib.workloads.scaled(ib.workloads.heaving_plate(nsteps=2), 128, 96, nlevels=2)
+def heaving(ib, f):
+    W = ib.workloads
+    frame = W.heave_pitch_frame(f=f, heave=0.25, pitch_deg=15.0)
+    base = W.Workload("heave", 0.005, (-1.0, 2.84), (-1.28, 1.28), 2, 200.0, 0.005, 10,
+                      [W.moving_plate(201, frame=frame)])
+    wl = W.scaled(base, 128, 96, nlevels=2, nsteps=10)
+    wl.Re, wl.dt = 200.0, 0.005
+    return wl
+
+
+def start_moving(ib, wl, precision):
     prob = wl.problem()
     st = ib.initstate(prob)
-    s = ib.initsolver(prob, st)
-    with pytest.raises(ib.IBError):
-        ib.Ensemble([s])
-    s.close()
+    st._gamma[:] = wl.initial_gamma()
+    s = ib.initsolver(prob, st, precision=precision)
+    s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+    s.set_cg_preconditioner("schur_ref")
+    s.vort2flux(st)
+    return prob, st, s
+
+
+def test_ensemble_with_moving_members_equals_single_steps(ib):
+    """Static and moving members (their CG loops inside the ensemble graph) give exactly the
+    steps they give alone; moving members join after two steps of their own."""
+    n = 10
+    cases = [("static", members(ib)[0]), ("static", members(ib)[1]),
+             ("moving", (heaving(ib, 0.5), "fp64")), ("moving", (heaving(ib, 0.4), "mixed"))]
+    alone = []
+    for kind, (wl, prec) in cases:
+        prob, st, s = (start_moving if kind == "moving" else start)(ib, wl, prec)
+        for i in range(n):
+            ib.advance_(st, s, i * wl.dt)
+        alone.append((st.qty.gamma.copy(), s.force_history(n), s.cg_stats(n - 2)[0] if kind == "moving" else None))
+        s.close()
+    runs = []
+    for kind, (wl, prec) in cases:
+        prob, st, s = (start_moving if kind == "moving" else start)(ib, wl, prec)
+        for i in range(2):
+            ib.advance_(st, s, i * wl.dt)
+        runs.append((kind, wl, st, s))
+    dt = cases[2][1][0].dt
+    assert all(r[1].dt == dt for r in runs if r[0] == "moving")
+    ens = ib.Ensemble([r[3] for r in runs])
+    ts = np.arange(2, n) * dt
+    ens.advance_n(ts, states=[r[2] for r in runs])
+    ens.close()
+    for (kind, wl, st, s), (g1, (cd1, cl1), it1) in zip(runs, alone):
+        np.testing.assert_array_equal(st.qty.gamma, g1)
+        cd, cl = s.force_history(n)
+        np.testing.assert_array_equal(cd, cd1)
+        if kind == "moving":
+            np.testing.assert_array_equal(s.cg_stats(n - 2)[0], it1)
+        s.close()

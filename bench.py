@@ -210,7 +210,7 @@ def run_ensemble_config(ib, lib, n=96, K=20, W=3, moving=True):
     plain_iters = []
     for w in ws:
         st, s = ensemble_member(ib, w, "fp64", plain=True)
-        m = 4 if s.moving else 8
+        m = 2 if s.moving else 8
         for k in range(2):
             ib.advance_(st, s, k * w.dt)
         lib.ib_synchronize(s.handle)
@@ -529,8 +529,8 @@ def run_ours(args, rank, world, local):
         out["configs"] = {
             "four_cylinders": run_static_config(ib, lib, L, ib.workloads.four_cylinders(), 60, 3, local, dist),
             "heaving_plate": run_moving_config(ib, ib.workloads.heaving_plate()),
-            "ensemble": run_ensemble_config(ib, lib),
-            "ensemble_static": run_ensemble_config(ib, lib, moving=False),
+            "ensemble": run_ensemble_config(ib, lib, K=10, W=2),
+            "ensemble_static": run_ensemble_config(ib, lib, K=20, W=3, moving=False),
         }
     if rank == 0 and not args.no_cpu_baseline:
         v, sec, cores = cpu_reference(ib, wl, args.cpu_steps, 1)

@@ -77,7 +77,7 @@ SIGNATURES = {
     "ib_set_cg_options": (C.c_int, [_vp, C.c_double, C.c_int32, C.c_int32]),
     "ib_get_cg_stats": (C.c_int, [_vp, C.c_int32, _ip, _dp]),
     "ib_set_cg_preconditioner": (C.c_int, [_vp, C.c_int32, C.c_int32]),
-    "ib_get_cg_preconditioner_stats": (C.c_int, [_vp, _ip, C.POINTER(C.c_int64)]),
+    "ib_get_cg_preconditioner_stats": (C.c_int, [_vp, _ip, C.POINTER(C.c_int64), _dp]),
     "ib_get_body_points": (C.c_int, [_vp, _dp, _dp]),
     "ib_get_stress": (C.c_int, [_vp, _dp, _dp, _dp]),
     "ib_get_force_history": (C.c_int, [_vp, C.c_int32, _dp, _dp]),

@@ -514,10 +514,11 @@ class Solver:
         m = {"none": _lib.IB_PC_NONE, "schur_ref": _lib.IB_PC_SCHUR_REF}[mode]
         self._check(self.lib.ib_set_cg_preconditioner(self.handle, m, int(refresh_steps)))
 
-    def cg_preconditioner_stats(self):
-        n, last = C.c_int32(), C.c_int64()
-        self._check(self.lib.ib_get_cg_preconditioner_stats(self.handle, C.byref(n), C.byref(last)))
-        return n.value, last.value
+    def cg_preconditioner_stats(self, seconds: bool = False):
+        """(assemblies, step of the last one[, its duration in seconds])."""
+        n, last, sec = C.c_int32(), C.c_int64(), C.c_double()
+        self._check(self.lib.ib_get_cg_preconditioner_stats(self.handle, C.byref(n), C.byref(last), C.byref(sec)))
+        return (n.value, last.value, sec.value) if seconds else (n.value, last.value)
 
     def cg_stats(self, count: int, start: bool = False):
         """Iterations and final relative residuals of the last `count` CG solves (and, with

@@ -233,7 +233,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
       } else if constexpr (is_df64<Tout>::value) {
         // x = x0 [+ x1] + d: the FP32 parts summed error-free, the (small) correction added
         // to the low part
-        const float* bs = a.base + off;
+        const float* bs = a.base ? a.base + off : nullptr;
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
         const df64* sf = (EPI == kEpiSubAddBase) ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         constexpr int R = 8;
@@ -244,7 +244,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
           for (int u = 0; u < R; ++u) {
             const int I = I0 + NL * u;
             const bool ok = I < ncol;
-            b0[u] = ok ? bs[I] : 0.0f;
+            b0[u] = (ok && bs) ? bs[I] : 0.0f;
             b1[u] = (ok && bs2) ? bs2[I] : 0.0f;
             if (EPI == kEpiSubAddBase) f[u] = ok ? sf[I] : df64(0.0f);
           }
@@ -328,7 +328,8 @@ cudaError_t inv_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaS
     }
     return cudaErrorInvalidValue;
   } else {
-    if (!a.base) return cudaErrorInvalidValue;
+    // a float-float result needs no base (a transform-only solve); a double one does
+    if (!a.base && (a.base2 || !is_df64<Tout>::value)) return cudaErrorInvalidValue;
     if (a.epi == kEpiAddBase) return launch_inv<T, Tout, P, NL, kEpiAddBase>(g, ax, a, s);
     if (a.epi == kEpiSubAddBase) return launch_inv<T, Tout, P, NL, kEpiSubAddBase>(g, ax, a, s);
     return cudaErrorInvalidValue;

@@ -115,6 +115,11 @@ struct ib_handle {
   int64_t pc_step = -1;                           // step of the last assembly
   int pc_assemblies = 0;
   double pc_assembly_s = 0.0;                     // measured duration of the last assembly
+  // Schur assembly work buffers, kept between the re-assemblies of a moving handle
+  double *asm_G = nullptr, *asm_P = nullptr, *asm_Wa = nullptr, *asm_Wb = nullptr, *asm_Q = nullptr,
+         *asm_R = nullptr, *asm_work = nullptr;
+  int asm_nc = 0;
+  bool asm_fp64 = false;  // assemble a moving handle's preconditioner in FP64 even in mixed mode
   double pc_excess_iters = 0.0;                   // iterations above the base since then
   double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
   double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
@@ -246,7 +251,8 @@ cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, co
 //   sweep 2 (optional): r = b - M (x0 + d1) with x0 + d1 an exact FP32 pair;  d2 = F32 solve(r)
 //   x = x0 + d1 [+ d2] summed in df64 (optionally subtracted from sub_from)
 // b, the result and the residual arithmetic are float-float (df64.cuh), so the whole solve runs
-// on the FP32 pipe; w32 / x032 / x132: FP32 work of batch arrays.
+// on the FP32 pipe; w32 / x032 / x132: FP32 work of batch arrays.  sweeps = 0 (warp passes
+// only) is the transform-only solve x = x0, FP32-accurate, and needs w32 alone.
 cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
                           const df64* sub_from, float* w32, float* x032, float* x132, int sweeps) {
   const Geometry& g = h->g;
@@ -268,6 +274,11 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
     a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
     CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
     CE(wypass<float>(g, h->axy32.d, ya, s));
+    if (sweeps <= 0) {
+      a.in = w32; a.out = out; a.bc = nullptr; a.sub_from = sub_from; a.base = nullptr; a.base2 = nullptr;
+      a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
+      return wx_inv<float, df64>(g, h->axx32.d, a, s);
+    }
     a.in = w32; a.out = x032; a.bc = nullptr;
     CE((wx_inv<float, float>(g, h->axx32.d, a, s)));
     const bool two = sweeps >= 2 && x132;
@@ -525,8 +536,44 @@ void build_multipliers(const ib_handle* h, std::vector<double>& lap, std::vector
     }
 }
 
+// Columns c0 .. c0+n-1 of B (B_Times, cnab/ops.jl:125-143 on unit vectors) into h->bmat.  S =
+// double: FP64 solves; S = df64: transform-only FP32 solves (sweeps 0 on the warp passes, one
+// sweep otherwise), B to FP32 accuracy.  Buffers hold n arrays per level (Gb, Pb: L n), Wb is
+// the solves' work (n FP64 arrays, or 2n FP32 ones).
+template <typename S>
+cudaError_t schur_columns(ib_handle* h, int c0, int n, double* Wa, double* Gb, double* Pb, double* Wb, double* Qb,
+                          double* Rb) {
+  const Geometry& g = h->g;
+  const int L = g.nlev, nf = h->nf;
+  const int64_t nG = g.nG;
+  cudaStream_t s = h->stream;
+  auto psolve = [&](const S* in, S* out, const S* bc, const SolveOp& op) -> cudaError_t {
+    if constexpr (std::is_same<S, double>::value) {
+      return poisson64(h, in, out, n, bc, op, nullptr, Wb);
+    } else {
+      float* w = reinterpret_cast<float*>(Wb);
+      return poisson_mixed(h, in, out, n, bc, op, nullptr, w, w + (int64_t)n * nG, nullptr, h->wdst ? 0 : 1);
+    }
+  };
+  S *A = view<S>(Wa), *G = view<S>(Gb), *P = view<S>(Pb), *Q = view<S>(Qb), *R = view<S>(Rb);
+  CE(unit_scatter_rot<S>(g, h->body_idx, h->weight, h->nb, c0, n, A, s));
+  CE(psolve(A, G, nullptr, op_cn1(h)));
+  if (L > 1) CE(cudaMemsetAsync(G + (int64_t)n * nG, 0, sizeof(S) * (L - 1) * n * nG, s));
+  for (int l = 1; l < L; ++l) CE(coarsify<S>(g, G + (int64_t)l * n * nG, G + (int64_t)(l - 1) * n * nG, n, nG, s));
+  CE(psolve(G + (int64_t)(L - 1) * n * nG, P + (int64_t)(L - 1) * n * nG, nullptr, op_lap(h)));
+  for (int l = L - 2; l >= 0; --l) {
+    CE(get_bc<S>(g, P + (int64_t)(l + 1) * n * nG, R, n, S(1.0), s));
+    CE(psolve(G + (int64_t)l * n * nG, P + (int64_t)l * n * nG, R, op_lap(h)));
+  }
+  CE(curl<S>(g, P, L > 1 ? R : nullptr, Q, n, s));
+  return reg_gather<S>(g, Q, nullptr, h->body_idx, h->weight, h->nb, h->bmat + (int64_t)c0 * nf, n, g.nq, nf, s);
+}
+
 // Schur matrix assembly (cnab/ops.jl:79-94 with B_Times, ops.jl:125-143), `nc` columns per
 // batch of device solves; then inverse (ops.jl:96) and a row-major copy for the step's gemv.
+// The B of bodies fixed in the grid is the direct solve and is assembled in FP64; for moving
+// bodies B^-1 only preconditions CG on the exact operator, and a mixed-precision handle
+// assembles it with FP32 transforms.
 int assemble_schur(ib_handle* h) {
   const Geometry& g = h->g;
   const int L = g.nlev, nf = h->nf;
@@ -540,48 +587,52 @@ int assemble_schur(ib_handle* h) {
   if (nc > 64) nc = 64;
   if (nc > nf) nc = nf;
   if (nc < 1) return fail(h, IB_ERR_CUDA, "not enough device memory for the Schur assembly");
-  double *Gb, *Pb, *Wa, *Wb, *Qb, *Rb;
-  CK(cudaMalloc(&Gb, sizeof(double) * L * nc * nG));
-  CK(cudaMalloc(&Pb, sizeof(double) * L * nc * nG));
-  CK(cudaMalloc(&Wa, sizeof(double) * nc * nG));
-  CK(cudaMalloc(&Wb, sizeof(double) * nc * nG));
-  CK(cudaMalloc(&Qb, sizeof(double) * nc * g.nq));
-  CK(cudaMalloc(&Rb, sizeof(double) * nc * g.nbc));
+  // a moving handle keeps its buffers for the next re-assembly; a static one frees them
+  const bool keep = h->motion == IB_MOTION_PRESCRIBED;
+  if (keep && h->asm_G) nc = h->asm_nc;
+  double *Gb = h->asm_G, *Pb = h->asm_P, *Wa = h->asm_Wa, *Wb = h->asm_Wb, *Qb = h->asm_Q, *Rb = h->asm_R;
+  double* work = h->asm_work;
+  if (!(keep && h->asm_G)) {
+    CK(cudaMalloc(&Gb, sizeof(double) * L * nc * nG));
+    CK(cudaMalloc(&Pb, sizeof(double) * L * nc * nG));
+    CK(cudaMalloc(&Wa, sizeof(double) * nc * nG));
+    CK(cudaMalloc(&Wb, sizeof(double) * nc * nG));
+    CK(cudaMalloc(&Qb, sizeof(double) * nc * g.nq));
+    CK(cudaMalloc(&Rb, sizeof(double) * nc * g.nbc));
+    CK(cudaMalloc(&work, invert_workspace_bytes(nf)));
+    if (keep) {
+      h->asm_G = Gb; h->asm_P = Pb; h->asm_Wa = Wa; h->asm_Wb = Wb; h->asm_Q = Qb; h->asm_R = Rb;
+      h->asm_work = work;
+      h->asm_nc = nc;
+    }
+  }
+  auto release = [&]() {
+    if (keep) return;
+    cudaFree(Gb); cudaFree(Pb); cudaFree(Wa); cudaFree(Wb); cudaFree(Qb); cudaFree(Rb); cudaFree(work);
+  };
   cudaStream_t s = h->stream;
+  const bool fp32 = keep && h->precision == IB_PREC_MIXED && !h->asm_fp64;
   int rc = IB_OK;
   for (int c0 = 0; c0 < nf && rc == IB_OK; c0 += nc) {
     const int n = (nf - c0 < nc) ? nf - c0 : nc;
-    auto run = [&]() -> cudaError_t {
-      CE(unit_scatter_rot<double>(g, h->body_idx, h->weight, h->nb, c0, n, Wa, s));
-      CE(poisson64(h, Wa, Gb, n, nullptr, op_cn1(h), nullptr, Wb));
-      if (L > 1) CE(cudaMemsetAsync(Gb + (int64_t)n * nG, 0, sizeof(double) * (L - 1) * n * nG, s));
-      for (int l = 1; l < L; ++l)
-        CE(coarsify<double>(g, Gb + (int64_t)l * n * nG, Gb + (int64_t)(l - 1) * n * nG, n, nG, s));
-      CE(poisson64(h, Gb + (int64_t)(L - 1) * n * nG, Pb + (int64_t)(L - 1) * n * nG, n, nullptr, op_lap(h), nullptr, Wb));
-      for (int l = L - 2; l >= 0; --l) {
-        CE(get_bc<double>(g, Pb + (int64_t)(l + 1) * n * nG, Rb, n, 1.0, s));
-        CE(poisson64(h, Gb + (int64_t)l * n * nG, Pb + (int64_t)l * n * nG, n, Rb, op_lap(h), nullptr, Wb));
-      }
-      CE(curl<double>(g, Pb, L > 1 ? Rb : nullptr, Qb, n, s));
-      CE(reg_gather<double>(g, Qb, nullptr, h->body_idx, h->weight, h->nb, h->bmat + (int64_t)c0 * nf, n, g.nq, nf, s));
-      return cudaSuccess;
-    };
-    cudaError_t e = run();
+    cudaError_t e = fp32 ? schur_columns<df64>(h, c0, n, Wa, Gb, Pb, Wb, Qb, Rb)
+                         : schur_columns<double>(h, c0, n, Wa, Gb, Pb, Wb, Qb, Rb);
     if (e != cudaSuccess) rc = fail(h, IB_ERR_CUDA, "Schur assembly", e);
   }
-  cudaStreamSynchronize(s);
-  cudaFree(Gb); cudaFree(Pb); cudaFree(Wa); cudaFree(Wb); cudaFree(Qb); cudaFree(Rb);
-  if (rc != IB_OK) return rc;
+  if (rc != IB_OK) {
+    cudaStreamSynchronize(s);
+    release();
+    return rc;
+  }
   // inverse (column-major), then the row-major copy
-  CK(cudaMemcpyAsync(h->binv_cm, h->bmat, sizeof(double) * (size_t)nf * nf, cudaMemcpyDeviceToDevice, s));
-  double* work = nullptr;
-  CK(cudaMalloc(&work, invert_workspace_bytes(nf)));
-  cudaError_t e = invert_inplace(h->binv_cm, nf, work, h->status + 2, s);
-  if (e != cudaSuccess) { cudaFree(work); return fail(h, IB_ERR_CUDA, "Schur inverse", e); }
+  cudaError_t e = cudaMemcpyAsync(h->binv_cm, h->bmat, sizeof(double) * (size_t)nf * nf, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = invert_inplace(h->binv_cm, nf, work, h->status + 2, s);
   // column-major (nf x nf) read as row-major is the transpose: transpose it back
-  CK(transpose(h->binv_cm, h->binv_rm, nf, nf, s));
-  CK(cudaStreamSynchronize(s));
-  cudaFree(work);
+  if (e == cudaSuccess) e = transpose(h->binv_cm, h->binv_rm, nf, nf, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  release();
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "Schur inverse", e);
+  if (e2 != cudaSuccess) return fail(h, IB_ERR_CUDA, "Schur assembly", e2);
   return IB_OK;
 }
 
@@ -639,6 +690,8 @@ void destroy_handle(ib_handle* h) {
   for (auto& ge : h->mgexec)
     if (ge) cudaGraphExecDestroy(ge);
   if (h->h_mslot) cudaFreeHost(h->h_mslot);
+  for (double* b : {h->asm_G, h->asm_P, h->asm_Wa, h->asm_Wb, h->asm_Q, h->asm_R, h->asm_work})
+    if (b) cudaFree(b);
   if (h->h_cgout) cudaFreeHost(h->h_cgout);
   if (h->loop_stream) cudaStreamDestroy(h->loop_stream);
   for (void* p : h->allocs) cudaFree(p);
@@ -1129,6 +1182,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     if (v >= 1) h->coarse_from = v;
   }
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
+  if (const char* env = std::getenv("IBGB300_PC_ASSEMBLY")) h->asm_fp64 = std::strcmp(env, "fp64") == 0;
   // transform kernels, by measurement on GB300: FP32 (mixed) transforms run faster one warp
   // per line where both axes allow it; FP64 transforms are FP64-pipe bound and the shared-memory
   // Stockham passes, with fewer twiddle multiplies and no transposing copies, are faster up to
@@ -1406,10 +1460,11 @@ int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps) 
   return IB_OK;
 }
 
-int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step) {
+int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step, double* last_seconds) {
   if (!h) return IB_ERR_INVALID;
   if (assemblies) *assemblies = h->pc_assemblies;
   if (last_step) *last_step = h->pc_step;
+  if (last_seconds) *last_seconds = h->pc_assembly_s;
   return IB_OK;
 }
 

@@ -143,8 +143,9 @@ int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_st
 #define IB_PC_SCHUR_REF 1
 int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps);
 
-/* number of preconditioner assemblies so far and the step of the last one (-1: none) */
-int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step);
+/* number of preconditioner assemblies so far, the step of the last one (-1: none) and its
+ * host-timed duration in seconds */
+int ib_get_cg_preconditioner_stats(ib_handle* h, int32_t* assemblies, int64_t* last_step, double* last_seconds);
 
 /* CG iterations and final relative residuals of the last `count` moving-body steps */
 int ib_get_cg_stats(ib_handle* h, int32_t count, int32_t* iterations, double* residuals);

@@ -42,44 +42,71 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
       const int b = row / nrow, J = row - b * nrow;
       const int64_t off = (int64_t)b * a.stride + (int64_t)J * ncol;
       const Tin* src = in + off;
-      if constexpr (PRO == kProResid && is_df64<Tin>::value) {
-        // refinement residual r = b [+ apply_bc] - M x, x = x0 [+ x1] (FP32 parts), with
-        // M x = mc x + ma (4 x - neighbours) to float-float accuracy.  Only float(r) is kept
-        // (it feeds an FP32 transform), so the final difference needs no more than float
-        // arithmetic on the float-float parts.
-        const float* x0 = a.base + off;
-        const float* x1 = a.base2 ? a.base2 + off : nullptr;
+      if constexpr ((PRO == kProResid || PRO == kProResidD) && is_df64<Tin>::value) {
+        // refinement residual r = b [+ apply_bc] - M x, x = x0 [+ x1] (FP32 parts, or the two
+        // parts of a float-float x0), with M x = mc x + ma (4 x - neighbours) to float-float
+        // accuracy.  float(r) feeds the FP32 transform; r itself can be kept (resid_out).
+        constexpr bool kD = PRO == kProResidD;
+        const float* x0 = kD ? nullptr : a.base + off;
+        const float* x1 = (!kD && a.base2) ? a.base2 + off : nullptr;
+        const df64* xd = kD ? a.based + off : nullptr;
         const double mcd = a.mc[b * a.mstep];
         const df64 mc = df64(mcd), ma = df64(a.ma[b * a.mstep]);
         const A* bc = kBC ? static_cast<const A*>(a.bc) + (int64_t)b * g.nbc : nullptr;
         const bool fac1 = a.bcfac == 1.0;
         const df64 fac = df64(a.bcfac);
         df64* rout = a.resid_out ? static_cast<df64*>(a.resid_out) + off : nullptr;
-        const float* xs = J > 0 ? x0 - ncol : nullptr;
-        const float* xn = J < nrow - 1 ? x0 + ncol : nullptr;
+        const float* xs = (!kD && J > 0) ? x0 - ncol : nullptr;
+        const float* xn = (!kD && J < nrow - 1) ? x0 + ncol : nullptr;
         const float* ys = (x1 && J > 0) ? x1 - ncol : nullptr;
         const float* yn = (x1 && J < nrow - 1) ? x1 + ncol : nullptr;
+        const df64* ds = (kD && J > 0) ? xd - ncol : nullptr;
+        const df64* dn = (kD && J < nrow - 1) ? xd + ncol : nullptr;
+        // ring terms of this row: the whole row at the bottom / top edge, one element at the
+        // left / right edge
+        const A* bcrow = (kBC && J == 0) ? bc + g.B + 1 : ((kBC && J == nrow - 1) ? bc + g.T + 1 : nullptr);
         // eight elements per lane per round, every load of a round issued before any use
         constexpr int R = 8;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float c0[R], w0[R], e0[R], s0[R], n0[R];
+          float c1[kD ? R : 1], w1[kD ? R : 1], e1[kD ? R : 1], s1[kD ? R : 1], n1[kD ? R : 1];
           df64 v[R];
+          df64 br[kBC ? R : 1], bs[kBC ? R : 1];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             const int I = I0 + NL * u;
             const bool ok = I < ncol;
-            c0[u] = ok ? x0[I] : 0.0f;
-            w0[u] = (ok && I > 0) ? x0[I - 1] : 0.0f;
-            e0[u] = (I < ncol - 1) ? x0[I + 1] : 0.0f;
-            s0[u] = (ok && xs) ? xs[I] : 0.0f;
-            n0[u] = (ok && xn) ? xn[I] : 0.0f;
+            if constexpr (kD) {
+              const df64 z(0.0f);
+              const df64 c = ok ? xd[I] : z, ww = (ok && I > 0) ? xd[I - 1] : z, e = (I < ncol - 1) ? xd[I + 1] : z;
+              const df64 ss = (ok && ds) ? ds[I] : z, nn = (ok && dn) ? dn[I] : z;
+              c0[u] = c.hi; w0[u] = ww.hi; e0[u] = e.hi; s0[u] = ss.hi; n0[u] = nn.hi;
+              c1[u] = c.lo; w1[u] = ww.lo; e1[u] = e.lo; s1[u] = ss.lo; n1[u] = nn.lo;
+            } else {
+              c0[u] = ok ? x0[I] : 0.0f;
+              w0[u] = (ok && I > 0) ? x0[I - 1] : 0.0f;
+              e0[u] = (I < ncol - 1) ? x0[I + 1] : 0.0f;
+              s0[u] = (ok && xs) ? xs[I] : 0.0f;
+              n0[u] = (ok && xn) ? xn[I] : 0.0f;
+            }
             v[u] = ok ? src[I] : df64(0.0f);
+            if constexpr (kBC) {
+              br[u] = (ok && bcrow) ? bcrow[I] : df64(0.0f);
+              bs[u] = (ok && I == 0) ? bc[g.L + 1 + J] : ((ok && I == ncol - 1) ? bc[g.R + 1 + J] : df64(0.0f));
+            }
           }
           df64 lap[R], xv[R];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             lap[u] = lap5_exact(c0[u], w0[u], e0[u], s0[u], n0[u]);
             xv[u] = df64(c0[u]);
+          }
+          if constexpr (kD) {
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+              lap[u] = add_sloppy(lap[u], lap5_exact(c1[u], w1[u], e1[u], s1[u], n1[u]));
+              xv[u] = two_sum(c0[u], c1[u]);
+            }
           }
           if (x1) {
 #pragma unroll
@@ -106,12 +133,10 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
             if (mcd == 1.0) mx = add_sloppy(mx, xv[u]);
             else if (mcd != 0.0) mx = add_sloppy(mx, mc * xv[u]);
             df64 vv = v[u];
-            if (kBC) {
+            if constexpr (kBC) {
               auto addbc = [&](df64 q) { vv = add_sloppy(vv, fac1 ? q : fac * q); };
-              if (J == 0) addbc(bc[g.B + 1 + I]);
-              if (J == nrow - 1) addbc(bc[g.T + 1 + I]);
-              if (I == 0) addbc(bc[g.L + 1 + J]);
-              if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
+              if (bcrow) addbc(br[u]);
+              if (I == 0 || I == ncol - 1) addbc(bs[u]);
             }
             U[I + 1] = (T)((vv.hi - mx.hi) + (vv.lo - mx.lo));
             if (rout) rout[I] = add_sloppy(vv, -mx);
@@ -133,6 +158,11 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* x1 = (PRO == kProResid && a.base2) ? a.base2 + off : nullptr;
         const A mc = (PRO == kProResid) ? A(a.mc[b * a.mstep]) : A(0.0);
         const A ma = (PRO == kProResid) ? A(a.ma[b * a.mstep]) : A(0.0);
+        // float-float load with a ring: the formed row can be kept (the next residual's b)
+        A* rout = nullptr;
+        if constexpr (PRO == kProLoad && is_df64<Tin>::value) {
+          if (a.resid_out) rout = static_cast<A*>(a.resid_out) + off;
+        }
 #pragma unroll 4
         for (int I = lane; I < ncol; I += NL) {
           A v = A(src[I]);
@@ -152,6 +182,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
             if (J < nrow - 1) lap = lap - X(I + ncol);
             v = v - (mc * xc + ma * lap);
           }
+          if (rout) rout[I] = v;
           U[I + 1] = (T)v;
         }
       }
@@ -235,7 +266,8 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         // to the low part
         const float* bs = a.base ? a.base + off : nullptr;
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
-        const df64* sf = (EPI == kEpiSubAddBase) ? static_cast<const df64*>(a.sub_from) + off : nullptr;
+        constexpr bool kF = EPI == kEpiSubAddBase || EPI == kEpiAddTo;
+        const df64* sf = kF ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         constexpr int R = 8;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
@@ -246,7 +278,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
             const bool ok = I < ncol;
             b0[u] = (ok && bs) ? bs[I] : 0.0f;
             b1[u] = (ok && bs2) ? bs2[I] : 0.0f;
-            if (EPI == kEpiSubAddBase) f[u] = ok ? sf[I] : df64(0.0f);
+            if (kF) f[u] = ok ? sf[I] : df64(0.0f);
           }
 #pragma unroll
           for (int u = 0; u < R; ++u) {
@@ -254,7 +286,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
             if (I >= ncol) break;
             const df64 x01 = two_sum(b0[u], b1[u]);
             const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
-            dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(f[u], -xv) : xv;
+            dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(f[u], -xv) : (EPI == kEpiAddTo) ? add_sloppy(f[u], xv) : xv;
           }
         }
       } else {
@@ -302,6 +334,14 @@ cudaError_t fwd_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaS
     }
     return cudaErrorInvalidValue;
   }
+  if (a.pro == kProResidD) {
+    if constexpr (is_df64<Tin>::value) {
+      if (!a.based || !a.mc || !a.ma) return cudaErrorInvalidValue;
+      return bc ? launch_fwd<T, Tin, P, NL, kProResidD, true>(g, ax, a, s)
+                : launch_fwd<T, Tin, P, NL, kProResidD, false>(g, ax, a, s);
+    }
+    return cudaErrorInvalidValue;
+  }
   return bc ? launch_fwd<T, Tin, P, NL, kProLoad, true>(g, ax, a, s) : launch_fwd<T, Tin, P, NL, kProLoad, false>(g, ax, a, s);
 }
 
@@ -332,6 +372,9 @@ cudaError_t inv_p(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cudaS
     if (!a.base && (a.base2 || !is_df64<Tout>::value)) return cudaErrorInvalidValue;
     if (a.epi == kEpiAddBase) return launch_inv<T, Tout, P, NL, kEpiAddBase>(g, ax, a, s);
     if (a.epi == kEpiSubAddBase) return launch_inv<T, Tout, P, NL, kEpiSubAddBase>(g, ax, a, s);
+    if constexpr (is_df64<Tout>::value) {
+      if (a.epi == kEpiAddTo) return launch_inv<T, Tout, P, NL, kEpiAddTo>(g, ax, a, s);
+    }
     return cudaErrorInvalidValue;
   }
 }

@@ -108,14 +108,16 @@ enum class SpecOp : int {
 //   kProLoad   row = in                                  (in: Tin)
 //   kProResid  row = in - M x0, M x = mc*x + ma*rot(curl(x)), formed in FP64
 //              (x0 = base, or base + base2 when base2 is given: an exact FP32 pair)
+//   kProResidD the same with a float-float x0 (based; warp passes, float-float input)
 // either optionally plus fac * apply_bc(bc) on the edges (bc != nullptr)
 // epilogue (what is stored):
 //   kEpiStore       out = row                              (out: Tout)
 //   kEpiSub         out = sub_from - row
 //   kEpiAddBase     out = base [+ base2] + row             (FP64 sum)
 //   kEpiSubAddBase  out = sub_from - (base [+ base2] + row)
-enum XPro : int { kProLoad = 0, kProResid = 1 };
-enum XEpi : int { kEpiStore = 0, kEpiSub = 1, kEpiAddBase = 2, kEpiSubAddBase = 3 };
+//   kEpiAddTo       out = sub_from + (base [+ base2] + row)  (float-float output; out may be sub_from)
+enum XPro : int { kProLoad = 0, kProResid = 1, kProResidD = 2 };
+enum XEpi : int { kEpiStore = 0, kEpiSub = 1, kEpiAddBase = 2, kEpiSubAddBase = 3, kEpiAddTo = 4 };
 
 struct XArgs {
   const void* in;           // Tin
@@ -127,11 +129,13 @@ struct XArgs {
   const void* sub_from;     // kEpiSub / kEpiSubAddBase (same element type as bc)
   const float* base;        // x0 of the refinement (kProResid, kEpiAddBase)
   const float* base2;       // optional second FP32 part of x0 (second refinement sweep)
+  const df64* based;        // float-float x0 (kProResidD)
   const double* mc;         // residual operator per slot (stride mstep)
   const double* ma;
   int mstep;
   int pro, epi;
   void* resid_out;          // optional (warp passes, float-float input): the residual itself, float-float
+                            // (kProResid), or the formed row in + bc (kProLoad with a ring)
 };
 
 template <typename T, typename Tin, typename Tout>
@@ -274,6 +278,31 @@ cudaError_t transpose(const double* in, double* out, int rows, int cols, cudaStr
 // launch profiling: when a Prof is installed for the calling thread, launches of the selected
 // kernel class are bracketed by CUDA events on their stream (used by ib_profile_steps)
 // ----------------------------------------------------------------------------------------------
+// Multilevel Vort2Flux with the levels solved together (v2f.cu; mixed precision, one-warp line
+// passes on both axes).  Tables of the ring transfer and the work of the ring chain.
+struct RingPlan {
+  int Kx = 0, Ky = 0, nK = 0, nchunk = 0;  // sine modes kept per bottom/top (left/right) side
+  int64_t qls = 0;                          // quarter-line values per level: 2 rows, 2 columns
+  double* St = nullptr;                     // [Kx][nx-1] 2 sin(pi (k+1)(I+1)/nx), [Ky][ny-1] (y)
+  double* Aring = nullptr;                  // [nbc][nK] ring entry per harmonic coefficient
+  int4* pts = nullptr;                      // [nbc] {x0 index, quarter-line index} x (1 or 2)
+  float *vrow = nullptr, *ucolp = nullptr, *ucol = nullptr, *qline = nullptr, *sidex = nullptr, *sidey = nullptr;
+  double *ringd = nullptr, *coef = nullptr;  // change of each level's ring (FP64), its coefficients
+  double* dring = nullptr;                   // the change as float-float (df64 pairs)
+  cudaError_t build(const Geometry& g);
+  void release();
+};
+cudaError_t v2f_yspec(const Geometry& g, const DstAxis<float>& ax, float* w, const float* m, int batch, float* vrow,
+                      cudaStream_t s);
+cudaError_t v2f_yring(const Geometry& g, const DstAxis<float>& axy, const DstAxis<float>& axx, float* w,
+                      const float* m, int batch, const float* sidex, const float* sidey, cudaStream_t s);
+cudaError_t v2f_colsum(const Geometry& g, const RingPlan& rp, const float* w, int batch, cudaStream_t s);
+cudaError_t v2f_lines(const DstAxis<float>& ax, const float* in, int64_t in_b, int64_t in_s, float* out,
+                      int64_t out_b, int64_t out_s, int nlines, cudaStream_t s);
+cudaError_t v2f_ring_eval(const Geometry& g, const RingPlan& rp, int l, const df64* xp_up, const float* x0_up,
+                          df64* ring_l, cudaStream_t s);
+cudaError_t v2f_ring_coef(const Geometry& g, const RingPlan& rp, int l, cudaStream_t s);
+
 enum KClass : int { kClassXPass = 0, kClassYPass = 1, kClassNonlin = 2, kClassCount = 3 };
 struct Prof {
   int cls = -1;

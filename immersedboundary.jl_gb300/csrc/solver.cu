@@ -120,6 +120,9 @@ struct ib_handle {
          *asm_R = nullptr, *asm_work = nullptr;
   int asm_nc = 0;
   bool asm_fp64 = false;  // assemble a moving handle's preconditioner in FP64 even in mixed mode
+  // mixed precision: Vort2Flux with the rings found first and the levels solved in one batch
+  bool v2f_levels = false;
+  RingPlan rplan;
   double pc_excess_iters = 0.0;                   // iterations above the base since then
   double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
   double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
@@ -356,8 +359,94 @@ S* view(double* p) {
 //
 // With q given, the curl of each finished level runs on the side stream while the finer levels
 // are solved (it reads only that level's psi and ring); the branch joins before returning.
+// Mixed-precision Vort2Flux of all levels in one batch (v2f.cu has the ring transfer).  psi and
+// rings hold the previous call's results (zero after a state upload without psi), used as
+// predictors: the FP32 sweeps then carry only the change since that call.
+//   r0 = Gamma + apply_bc(ring_old) - L psi_p (float-float);  d0 = F32 solve(r0)
+//   r1 = r0 - L d0; its spectrum; psi_o = psi_p + d0 + S^-1 spec on the quarter lines
+//   rings coarse to fine: ring_l = get_bc(psi_o_{l+1}) + harmonic part of the change of
+//   ring_{l+1}   (FP64)
+//   sweep 1: d1 = F32 inverse of (spec + spectrum of apply_bc(ring - ring_old))
+//   sweep 2: r2 = r1 + apply_bc(ring - ring_old) - L d1;  psi = psi_p + d0 + d1 + F32 solve(r2)
+// Only level 0 is finished when only its fluxes are asked for (q == nullptr); the other levels
+// keep their previous psi.
+cudaError_t vort2flux_levels(ib_handle* h, df64* gam, df64* psi, df64* q, df64* q1, df64* rings) {
+  const Geometry& g = h->g;
+  const int L = g.nlev, ncol = g.nx - 1, nrow = g.ny - 1;
+  const int64_t nG = g.nG;
+  cudaStream_t s = h->stream;
+  const RingPlan& rp = h->rplan;
+  const DstAxis<float>& ax = h->axx32.d;
+  const DstAxis<float>& ay = h->axy32.d;
+  const SolveOp op = op_lap(h);
+  const int nf = q ? L : 1;
+  df64* r1 = reinterpret_cast<df64*>(h->r1);
+  // x and y line transforms side by side (side stream) where there is one
+  auto lines2 = [&](const float* inx, int64_t inx_b, float* outx, int64_t outx_b, const float* iny, int64_t iny_b,
+                    float* outy, int64_t outy_b, int nl) -> cudaError_t {
+    cudaStream_t sy = s;
+    if (h->side) {
+      CE(cudaEventRecord(h->fork_ev[0], s));
+      CE(cudaStreamWaitEvent(h->side, h->fork_ev[0], 0));
+      sy = h->side;
+    }
+    CE(v2f_lines(ax, inx, inx_b, ncol, outx, outx_b, ncol, nl, s));
+    CE(v2f_lines(ay, iny, iny_b, nrow, outy, outy_b, nrow, nl, sy));
+    if (h->side) {
+      CE(cudaEventRecord(h->fork_ev[1], h->side));
+      CE(cudaStreamWaitEvent(s, h->fork_ev[1], 0));
+    }
+    return cudaSuccess;
+  };
+  for (int l = 1; l < L; ++l) CE(coarsify<df64>(g, gam + l * nG, gam + (l - 1) * nG, 1, nG, s));
+  XArgs a{};
+  a.batch = L; a.stride = nG; a.bcfac = 1.0;
+  a.in = gam; a.out = h->w32; a.bc = rings; a.pro = kProResidD; a.based = psi; a.epi = kEpiStore;
+  a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep; a.resid_out = r1;
+  CE((wx_fwd<float, df64>(g, ax, a, s)));
+  YPassArgs<float> ya{};
+  ya.in1 = h->w32; ya.out = h->w32; ya.batch = L; ya.stride = nG; ya.m1 = op.m32; ya.mstride = op.mstride;
+  ya.op = SpecOp::kScale;
+  CE(wypass<float>(g, ay, ya, s));
+  a = XArgs{};
+  a.batch = L; a.stride = nG; a.bcfac = 1.0;
+  a.in = h->w32; a.out = h->x032; a.pro = kProLoad; a.epi = kEpiStore;
+  CE((wx_inv<float, float>(g, ax, a, s)));
+  a.in = r1; a.out = h->w32; a.pro = kProResid; a.base = h->x032; a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+  a.resid_out = r1;
+  CE((wx_fwd<float, df64>(g, ax, a, s)));
+  CE(v2f_yspec(g, ay, h->w32, op.m32, L, rp.vrow, s));
+  CE(v2f_colsum(g, rp, h->w32, L, s));
+  CE(lines2(rp.vrow, 2 * ncol, rp.qline, rp.qls, rp.ucol, 2 * nrow, rp.qline + 2 * ncol, rp.qls, 2 * L));
+  for (int l = L - 2; l >= 0; --l) {
+    CE(v2f_ring_eval(g, rp, l, psi + (l + 1) * nG, h->x032 + (l + 1) * nG, rings + (int64_t)l * g.nbc, s));
+    if (l > 0) CE(v2f_ring_coef(g, rp, l, s));
+  }
+  const int ns = std::min(nf, L - 1);  // finished levels with a ring
+  CE(lines2(rp.sidex, 2 * ncol, rp.sidex, 2 * ncol, rp.sidey, 2 * nrow, rp.sidey, 2 * nrow, 2 * ns));
+  CE(v2f_yring(g, ay, ax, h->w32, op.m32, nf, rp.sidex, rp.sidey, s));
+  a = XArgs{};
+  a.batch = nf; a.stride = nG; a.bcfac = 1.0;
+  a.in = h->w32; a.out = h->x132; a.pro = kProLoad; a.epi = kEpiStore;
+  CE((wx_inv<float, float>(g, ax, a, s)));
+  if (ns > 0) CE(apply_bc<df64>(g, r1, reinterpret_cast<const df64*>(rp.dring), df64(1.0f), ns, s));
+  a.in = r1; a.out = h->w32; a.pro = kProResid; a.base = h->x132; a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep;
+  CE((wx_fwd<float, df64>(g, ax, a, s)));
+  ya.batch = nf;
+  CE(wypass<float>(g, ay, ya, s));
+  a = XArgs{};
+  a.batch = nf; a.stride = nG; a.bcfac = 1.0;
+  a.in = h->w32; a.out = psi; a.sub_from = psi; a.pro = kProLoad; a.base = h->x032; a.base2 = h->x132;
+  a.epi = kEpiAddTo;
+  CE((wx_inv<float, df64>(g, ax, a, s)));
+  return q ? curl<df64>(g, psi, rings, q, L, s) : curl<df64>(g, psi, rings, q1, 1, s);
+}
+
 template <typename S>
 cudaError_t vort2flux(ib_handle* h, S* gam, S* psi, S* q, S* q1, S* rings) {
+  if constexpr (std::is_same<S, df64>::value) {
+    if (h->v2f_levels) return vort2flux_levels(h, gam, psi, q, q1, rings);
+  }
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t nG = g.nG;
@@ -702,6 +791,7 @@ void destroy_handle(ib_handle* h) {
   h->axy.release();
   h->axx32.release();
   h->axy32.release();
+  h->rplan.release();
   for (auto ev : h->fork_ev)
     if (ev) cudaEventDestroy(ev);
   if (h->side) cudaStreamDestroy(h->side);
@@ -1225,6 +1315,14 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     AL(h->w32, L * nG); AL(h->x032, L * nG);
     if (h->refine >= 2) { AL(h->x132, L * nG); AL(h->r1, L * nG); }
     AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
+    // Vort2Flux over all levels at once: two refinement sweeps, one-warp line passes on both
+    // axes (IBGB300_V2F=sequential keeps the level-by-level order)
+    h->v2f_levels = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    if (const char* env = std::getenv("IBGB300_V2F")) {
+      if (std::strcmp(env, "sequential") == 0) h->v2f_levels = false;
+    }
+    if (h->v2f_levels && (e = h->rplan.build(g)) != cudaSuccess)
+      return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));
   }
   AL(h->status, 4); AL(h->d_counter, 1);
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
@@ -1363,6 +1461,14 @@ int ib_set_state(ib_handle* h, const double* gamma, const double* q, const doubl
     if (nonlin1) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->N[p], nG);
     if (nonlin2) k_to_df64<<<conv_blocks(nG), 256, 0, s>>>(h->N[p ^ 1], nG);
     CK(cudaGetLastError());
+  }
+  // the batched Vort2Flux predicts psi and the rings from the previous call: a new state starts
+  // from its own psi (or zero) and zero rings
+  if (h->v2f_levels) {
+    if (!psi) CK(cudaMemsetAsync(h->psi, 0, nGL, s));
+    CK(cudaMemsetAsync(h->rings, 0, sizeof(double) * g.nlev * g.nbc, s));
+    if (h->rings_w) CK(cudaMemsetAsync(h->rings_w, 0, sizeof(double) * g.nlev * g.nbc, s));
+    if (h->Pw) CK(cudaMemsetAsync(h->Pw, 0, nGL, s));
   }
   CK(cudaStreamSynchronize(s));
   h->t = t;

@@ -206,3 +206,30 @@ def test_two_warp_lines_agree_with_one_warp_lines(ib, monkeypatch):
         out[lanes] = st.qty.gamma.copy()
         s.close()
     assert rel(out["64"], out["32"]) < 1e-9
+
+
+@pytest.mark.parametrize("nx,ny,nl", [(256, 192, 4), (192, 256, 3)])
+def test_levels_vort2flux_matches_level_by_level(ib, monkeypatch, nx, ny, nl):
+    """Mixed-precision Vort2Flux with every level's boundary ring found first (harmonic ring
+    transfer) and the levels solved as one batch, against the reference's level-by-level order
+    (IBGB300_V2F=sequential) in mixed precision and in FP64: the same fields to round-off."""
+    wl = ib.workloads.scaled(ib.workloads.cylinder_small(), nx, ny, nlevels=nl)
+    out = {}
+    for mode, prec in (("levels", "mixed"), ("sequential", "mixed"), ("sequential", "fp64")):
+        monkeypatch.setenv("IBGB300_V2F", mode)
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision=prec)
+        s.vort2flux(st)
+        first = (st.qty.psi.copy(), st.qty.q.copy())
+        cds = []
+        for i in range(12):
+            ib.advance_(st, s, i * wl.dt)
+            cds.append([b.CD for b in st.qty.stress] + [b.CL for b in st.qty.stress])
+        out[mode, prec] = first + (st.qty.psi.copy(), st.qty.q.copy(), st.qty.gamma.copy(), np.array(cds))
+        s.close()
+    lv, sq, fp = out["levels", "mixed"], out["sequential", "mixed"], out["sequential", "fp64"]
+    for k in range(5):  # psi, q of the initial field; psi, q, Gamma after 12 steps
+        assert rel(lv[k], fp[k]) < 1e-10, (k, rel(lv[k], fp[k]), rel(sq[k], fp[k]))
+    assert np.max(np.abs(lv[5] - fp[5]) / np.maximum(1.0, np.abs(fp[5]))) < 1e-8

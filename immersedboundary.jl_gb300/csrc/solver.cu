@@ -381,18 +381,21 @@ cudaError_t vort2flux_levels(ib_handle* h, df64* gam, df64* psi, df64* q, df64* 
   const SolveOp op = op_lap(h);
   const int nf = q ? L : 1;
   df64* r1 = reinterpret_cast<df64*>(h->r1);
-  // x and y line transforms side by side (side stream) where there is one
+  // x and y line transforms side by side (side stream) where there is one.  Only calls that
+  // finish every level fork: the level-0-only calls include the Schur products of the CG loop,
+  // which may be captured into a graph's conditional body (kernels and copies only).
+  const bool fork = q && h->side;
   auto lines2 = [&](const float* inx, int64_t inx_b, float* outx, int64_t outx_b, const float* iny, int64_t iny_b,
                     float* outy, int64_t outy_b, int nl) -> cudaError_t {
     cudaStream_t sy = s;
-    if (h->side) {
+    if (fork) {
       CE(cudaEventRecord(h->fork_ev[0], s));
       CE(cudaStreamWaitEvent(h->side, h->fork_ev[0], 0));
       sy = h->side;
     }
     CE(v2f_lines(ax, inx, inx_b, ncol, outx, outx_b, ncol, nl, s));
     CE(v2f_lines(ay, iny, iny_b, nrow, outy, outy_b, nrow, nl, sy));
-    if (h->side) {
+    if (fork) {
       CE(cudaEventRecord(h->fork_ev[1], h->side));
       CE(cudaStreamWaitEvent(s, h->fork_ev[1], 0));
     }

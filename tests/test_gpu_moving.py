@@ -112,11 +112,14 @@ def test_schur_preconditioned_cg_same_answer_fewer_iterations(ib, precision):
     assert out["schur_ref"][2] < 0.5 * out["none"][2], (out["schur_ref"][2], out["none"][2])
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_captured_moving_step_equals_eager(ib, monkeypatch, precision):
+@pytest.mark.parametrize("precision,grid", [("fp64", (128, 96, 2)), ("mixed", (128, 96, 2)),
+                                            ("mixed", (128, 128, 3))])
+def test_captured_moving_step_equals_eager(ib, monkeypatch, precision, grid):
     """From the third step on a moving step runs as a captured graph with the CG loop driven
-    on the device; it gives the eager step's iterates (IBGB300_NO_GRAPH=1) exactly."""
-    wl = small_heaving(ib, nsteps=10)
+    on the device; it gives the eager step's iterates (IBGB300_NO_GRAPH=1) exactly.  The
+    128 x 128 grid takes the one-warp line passes and the all-levels Vort2Flux inside the loop."""
+    nx, ny, L = grid
+    wl = small_heaving(ib, nx=nx, ny=ny, L=L, nsteps=10)
     wl.dt = 0.005
     out = {}
     for mode in ("graph", "eager"):

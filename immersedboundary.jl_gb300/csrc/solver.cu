@@ -1319,10 +1319,15 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     if (h->refine >= 2) { AL(h->x132, L * nG); AL(h->r1, L * nG); }
     AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
     // Vort2Flux over all levels at once: two refinement sweeps, one-warp line passes on both
-    // axes (IBGB300_V2F=sequential keeps the level-by-level order)
-    h->v2f_levels = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    // axes.  By measurement on GB300 (mixed step, device time) it is the faster order while one
+    // level's passes leave the GPU part idle: 0.32 vs 0.41 ms at 256^2 x 3 levels, 0.67 vs 0.81
+    // at 512^2 x 4, 1.50 vs 1.57 at 1024^2 x 4, but 6.47 vs 6.27 at 2048^2 x 5; so up to 2^20
+    // cells per level.  IBGB300_V2F=levels|sequential overrides the choice.
+    const bool lv_ok = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    h->v2f_levels = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);
     if (const char* env = std::getenv("IBGB300_V2F")) {
       if (std::strcmp(env, "sequential") == 0) h->v2f_levels = false;
+      if (std::strcmp(env, "levels") == 0) h->v2f_levels = lv_ok;
     }
     if (h->v2f_levels && (e = h->rplan.build(g)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));

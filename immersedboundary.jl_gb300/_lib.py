@@ -34,6 +34,7 @@ IB_WARM_ZERO = 2
 IB_WARM_LEARNED = 3
 IB_PC_NONE = 0
 IB_PC_SCHUR_REF = 1
+IB_V2F_AUTO, IB_V2F_LEVELS, IB_V2F_SEQUENTIAL = 0, 1, 2
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -77,6 +78,7 @@ SIGNATURES = {
     "ib_set_cg_options": (C.c_int, [_vp, C.c_double, C.c_int32, C.c_int32]),
     "ib_get_cg_stats": (C.c_int, [_vp, C.c_int32, _ip, _dp]),
     "ib_set_cg_preconditioner": (C.c_int, [_vp, C.c_int32, C.c_int32]),
+    "ib_set_vort2flux_order": (C.c_int, [_vp, C.c_int32]),
     "ib_get_cg_preconditioner_stats": (C.c_int, [_vp, _ip, C.POINTER(C.c_int64), _dp]),
     "ib_get_body_points": (C.c_int, [_vp, _dp, _dp]),
     "ib_get_stress": (C.c_int, [_vp, _dp, _dp, _dp]),

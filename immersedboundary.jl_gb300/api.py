@@ -514,6 +514,14 @@ class Solver:
         m = {"none": _lib.IB_PC_NONE, "schur_ref": _lib.IB_PC_SCHUR_REF}[mode]
         self._check(self.lib.ib_set_cg_preconditioner(self.handle, m, int(refresh_steps)))
 
+    def set_vort2flux_order(self, order: str = "auto"):
+        """Mixed precision: ``"levels"`` (every level's boundary ring first, then all levels in
+        one batch), ``"sequential"`` (the reference's coarse-to-fine order) or ``"auto"`` (levels
+        up to 2^20 cells per level where the grid allows it).  FP64 solvers keep the reference
+        order."""
+        m = {"auto": _lib.IB_V2F_AUTO, "levels": _lib.IB_V2F_LEVELS, "sequential": _lib.IB_V2F_SEQUENTIAL}[order]
+        self._check(self.lib.ib_set_vort2flux_order(self.handle, m))
+
     def cg_preconditioner_stats(self, seconds: bool = False):
         """(assemblies, step of the last one[, its duration in seconds])."""
         n, last, sec = C.c_int32(), C.c_int64(), C.c_double()

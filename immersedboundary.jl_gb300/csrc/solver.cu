@@ -122,6 +122,7 @@ struct ib_handle {
   bool asm_fp64 = false;  // assemble a moving handle's preconditioner in FP64 even in mixed mode
   // mixed precision: Vort2Flux with the rings found first and the levels solved in one batch
   bool v2f_levels = false;
+  bool v2f_ok = false, v2f_auto = false;  // the grid allows it / the size rule picks it
   RingPlan rplan;
   double pc_excess_iters = 0.0;                   // iterations above the base since then
   double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
@@ -1324,7 +1325,9 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     // at 512^2 x 4, 1.50 vs 1.57 at 1024^2 x 4, but 6.47 vs 6.27 at 2048^2 x 5; so up to 2^20
     // cells per level.  IBGB300_V2F=levels|sequential overrides the choice.
     const bool lv_ok = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
-    h->v2f_levels = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);
+    h->v2f_ok = lv_ok;
+    h->v2f_auto = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);
+    h->v2f_levels = h->v2f_auto;
     if (const char* env = std::getenv("IBGB300_V2F")) {
       if (std::strcmp(env, "sequential") == 0) h->v2f_levels = false;
       if (std::strcmp(env, "levels") == 0) h->v2f_levels = lv_ok;
@@ -1571,6 +1574,30 @@ int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps) 
   h->pc_refresh = refresh_steps;
   h->pc_step = -1;
   h->pc_base_iters = -1;
+  return IB_OK;
+}
+
+int ib_set_vort2flux_order(ib_handle* h, int32_t order) {
+  if (!h || order < IB_V2F_AUTO || order > IB_V2F_SEQUENTIAL) return IB_ERR_INVALID;
+  if (h->precision != IB_PREC_MIXED) return IB_OK;
+  CK(cudaSetDevice(h->device));
+  if (order == IB_V2F_LEVELS && !h->v2f_ok)
+    return fail(h, IB_ERR_UNSUPPORTED, "the all-levels Vort2Flux needs one-warp line passes on both axes");
+  const bool lv = order == IB_V2F_LEVELS || (order == IB_V2F_AUTO && h->v2f_auto);
+  if (lv == h->v2f_levels) return IB_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  if (lv && !h->rplan.St) {
+    cudaError_t e = h->rplan.build(h->g);
+    if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "ring transfer tables", e);
+  }
+  h->v2f_levels = lv;
+  // the rings buffers then hold the other order's values: a predictor only, either is valid
+  if (h->gexec[0]) {
+    int rc = capture_graphs(h);
+    if (rc != IB_OK) return rc;
+  }
+  for (auto& ge : h->mgexec)
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
   return IB_OK;
 }
 
@@ -2170,6 +2197,13 @@ int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) 
     return rc;
   };
   if (ce != cudaSuccess) return bail(efail(e, IB_ERR_CUDA, "cudaSetDevice", ce));
+  // static members fill the GPU between them: the level-by-level Vort2Flux there
+  if (n >= 2)
+    for (ib_handle* h : e->m)
+      if (h->motion != IB_MOTION_PRESCRIBED && h->v2f_levels) {
+        const int rc = ib_set_vort2flux_order(h, IB_V2F_SEQUENTIAL);
+        if (rc != IB_OK) return bail(efail(e, rc, "member Vort2Flux order: " + h->err));
+      }
   for (ib_handle* h : e->m) {
     if (h->motion == IB_MOTION_PRESCRIBED) {
       e->any_moving = true;

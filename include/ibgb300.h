@@ -133,8 +133,9 @@ int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv,
 int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_start);
 
 /* Preconditioner of the moving-body CG (no reference counterpart; the reference runs plain cg!):
- * IB_PC_SCHUR_REF uses the inverse Schur matrix B_ref^-1 of a reference configuration (FP64,
- * assembled on the device like the static Binv of cnab/ops.jl:79-96) as P in preconditioned CG.
+ * IB_PC_SCHUR_REF uses the inverse Schur matrix B_ref^-1 of a reference configuration (assembled
+ * on the device like the static Binv of cnab/ops.jl:79-96: FP64, or FP32 transforms in a mixed-
+ * precision handle, which P need not be exact for) as P in preconditioned CG.
  * It is assembled at the next step, then again every `refresh_steps` steps, or, with
  * refresh_steps = 0, once the CG iterations spent above those of the solve after the last
  * assembly have taken as long as that assembly (both timed on the host).  The stopping rule
@@ -142,6 +143,19 @@ int ib_set_cg_options(ib_handle* h, double tol, int32_t maxiter, int32_t warm_st
 #define IB_PC_NONE 0
 #define IB_PC_SCHUR_REF 1
 int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps);
+
+/* Order of the mixed-precision Vort2Flux (fluid-ops.jl:438-472 solves the levels coarse to fine,
+ * each taking its boundary ring from the coarser solution).  IB_V2F_LEVELS finds every level's
+ * ring first (harmonic ring transfer) and solves all levels in one batch; IB_V2F_SEQUENTIAL
+ * keeps the reference's level order; IB_V2F_AUTO (the default) takes LEVELS up to 2^20 cells per
+ * level where the grid has one-warp line passes.  The handle's step graphs are captured again;
+ * a handle in an ensemble must not change it (the ensemble holds its own capture).  FP64
+ * handles keep the reference order (accepted, no effect).  IB_ERR_UNSUPPORTED for LEVELS on a
+ * grid without one-warp line passes. */
+#define IB_V2F_AUTO 0
+#define IB_V2F_LEVELS 1
+#define IB_V2F_SEQUENTIAL 2
+int ib_set_vort2flux_order(ib_handle* h, int32_t order);
 
 /* number of preconditioner assemblies so far, the step of the last one (-1: none) and its
  * host-timed duration in seconds */

@@ -10,7 +10,10 @@
  * assembly) and keep their CG options while in the ensemble; the host reads their CG statistics
  * after every step and re-assembles preconditioners between launches.  The members' own state,
  * history and error reporting work as for single handles; a member must not be advanced on its
- * own while it belongs to an ensemble.
+ * own while it belongs to an ensemble.  In an ensemble of two or more members, static mixed-
+ * precision members are set to the level-by-level Vort2Flux (ib_set_vort2flux_order,
+ * IB_V2F_SEQUENTIAL; it stays set afterwards): the members' branches fill the GPU between them,
+ * and the all-levels order only adds work there (96 members on GB300: 14.0 vs 16.3 ms per step).
  */
 #ifndef IBGB300_ENSEMBLE_H
 #define IBGB300_ENSEMBLE_H

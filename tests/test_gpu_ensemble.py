@@ -21,6 +21,8 @@ def start(ib, wl, precision):
     st = ib.initstate(prob)
     st._gamma[:] = wl.initial_gamma()
     s = ib.initsolver(prob, st, precision=precision)
+    # the order an ensemble gives its static members, here from the start on
+    s.set_vort2flux_order("sequential")
     s.vort2flux(st)
     return prob, st, s
 

@@ -233,3 +233,32 @@ def test_levels_vort2flux_matches_level_by_level(ib, monkeypatch, nx, ny, nl):
     for k in range(5):  # psi, q of the initial field; psi, q, Gamma after 12 steps
         assert rel(lv[k], fp[k]) < 1e-10, (k, rel(lv[k], fp[k]), rel(sq[k], fp[k]))
     assert np.max(np.abs(lv[5] - fp[5]) / np.maximum(1.0, np.abs(fp[5]))) < 1e-8
+
+
+def test_vort2flux_order_setter(ib):
+    """ib_set_vort2flux_order switches a mixed solver between the two Vort2Flux orders (the step
+    graphs are captured again); both give the FP64 steps to round-off.  The all-levels order
+    needs one-warp line passes on both axes."""
+    W = ib.workloads
+    wl = W.scaled(W.two_body_large(), 256, 256, nlevels=3)
+    out = {}
+    for prec, orders in (("fp64", ("auto",)), ("mixed", ("sequential", "levels", "auto"))):
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision=prec)
+        s.vort2flux(st)
+        for k in range(9):
+            s.set_vort2flux_order(orders[k % len(orders)])
+            ib.advance_(st, s, k * wl.dt)
+        out[prec] = st.qty.gamma.copy()
+        s.close()
+    assert rel(out["mixed"], out["fp64"]) < 1e-10
+    wl2 = W.scaled(W.cylinder_small(), 96, 80, nlevels=2)
+    prob = wl2.problem()
+    st = ib.initstate(prob)
+    s = ib.initsolver(prob, st, precision="mixed")
+    with pytest.raises(ib.IBError):
+        s.set_vort2flux_order("levels")
+    s.set_vort2flux_order("sequential")
+    s.close()

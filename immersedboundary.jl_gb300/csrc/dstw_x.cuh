@@ -63,7 +63,9 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const df64* ds = (kD && J > 0) ? xd - ncol : nullptr;
         const df64* dn = (kD && J < nrow - 1) ? xd + ncol : nullptr;
         // ring terms of this row: the whole row at the bottom / top edge, one element at the
-        // left / right edge
+        // left / right edge; loaded with the iterate for a float-float iterate, at their use
+        // otherwise (fewer live registers: 128 vs 156 at P = 32)
+        constexpr bool kPre = kBC && kD;
         const A* bcrow = (kBC && J == 0) ? bc + g.B + 1 : ((kBC && J == nrow - 1) ? bc + g.T + 1 : nullptr);
         // eight elements per lane per round, every load of a round issued before any use
         constexpr int R = 8;
@@ -71,7 +73,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           float c0[R], w0[R], e0[R], s0[R], n0[R];
           float c1[kD ? R : 1], w1[kD ? R : 1], e1[kD ? R : 1], s1[kD ? R : 1], n1[kD ? R : 1];
           df64 v[R];
-          df64 br[kBC ? R : 1], bs[kBC ? R : 1];
+          df64 br[kPre ? R : 1], bs[kPre ? R : 1];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             const int I = I0 + NL * u;
@@ -90,7 +92,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
               n0[u] = (ok && xn) ? xn[I] : 0.0f;
             }
             v[u] = ok ? src[I] : df64(0.0f);
-            if constexpr (kBC) {
+            if constexpr (kPre) {
               br[u] = (ok && bcrow) ? bcrow[I] : df64(0.0f);
               bs[u] = (ok && I == 0) ? bc[g.L + 1 + J] : ((ok && I == ncol - 1) ? bc[g.R + 1 + J] : df64(0.0f));
             }
@@ -135,8 +137,14 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
             df64 vv = v[u];
             if constexpr (kBC) {
               auto addbc = [&](df64 q) { vv = add_sloppy(vv, fac1 ? q : fac * q); };
-              if (bcrow) addbc(br[u]);
-              if (I == 0 || I == ncol - 1) addbc(bs[u]);
+              if constexpr (kPre) {
+                if (bcrow) addbc(br[u]);
+                if (I == 0 || I == ncol - 1) addbc(bs[u]);
+              } else {
+                if (bcrow) addbc(bcrow[I]);
+                if (I == 0) addbc(bc[g.L + 1 + J]);
+                if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
+              }
             }
             U[I + 1] = (T)((vv.hi - mx.hi) + (vv.lo - mx.lo));
             if (rout) rout[I] = add_sloppy(vv, -mx);
@@ -158,11 +166,6 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* x1 = (PRO == kProResid && a.base2) ? a.base2 + off : nullptr;
         const A mc = (PRO == kProResid) ? A(a.mc[b * a.mstep]) : A(0.0);
         const A ma = (PRO == kProResid) ? A(a.ma[b * a.mstep]) : A(0.0);
-        // float-float load with a ring: the formed row can be kept (the next residual's b)
-        A* rout = nullptr;
-        if constexpr (PRO == kProLoad && is_df64<Tin>::value) {
-          if (a.resid_out) rout = static_cast<A*>(a.resid_out) + off;
-        }
 #pragma unroll 4
         for (int I = lane; I < ncol; I += NL) {
           A v = A(src[I]);
@@ -182,7 +185,6 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
             if (J < nrow - 1) lap = lap - X(I + ncol);
             v = v - (mc * xc + ma * lap);
           }
-          if (rout) rout[I] = v;
           U[I + 1] = (T)v;
         }
       }

@@ -135,7 +135,6 @@ struct XArgs {
   int mstep;
   int pro, epi;
   void* resid_out;          // optional (warp passes, float-float input): the residual itself, float-float
-                            // (kProResid), or the formed row in + bc (kProLoad with a ring)
 };
 
 template <typename T, typename Tin, typename Tout>

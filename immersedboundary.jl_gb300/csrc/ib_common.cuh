@@ -283,7 +283,7 @@ struct RingPlan {
   int Kx = 0, Ky = 0, nK = 0, nchunk = 0;  // sine modes kept per bottom/top (left/right) side
   int64_t qls = 0;                          // quarter-line values per level: 2 rows, 2 columns
   double* St = nullptr;                     // [Kx][nx-1] 2 sin(pi (k+1)(I+1)/nx), [Ky][ny-1] (y)
-  double* Aring = nullptr;                  // [nbc][nK] ring entry per harmonic coefficient
+  double* Aring = nullptr;                  // [nK][nbc] ring entry per harmonic coefficient
   int4* pts = nullptr;                      // [nbc] {x0 index, quarter-line index} x (1 or 2)
   float *vrow = nullptr, *ucolp = nullptr, *ucol = nullptr, *qline = nullptr, *sidex = nullptr, *sidey = nullptr;
   double *ringd = nullptr, *coef = nullptr;  // change of each level's ring (FP64), its coefficients

@@ -1321,10 +1321,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
     // Vort2Flux over all levels at once: two refinement sweeps, one-warp line passes on both
     // axes.  By measurement on GB300 (mixed step, device time) it is the faster order while one
-    // level's passes leave the GPU part idle: 0.32 vs 0.41 ms at 256^2 x 3 levels, 0.66 vs 0.80
-    // at 512^2 x 4, equal at 1024^2 x 4 (1.47 ms; C_L/C_D 2e-10 from FP64 instead of 2e-8), but
-    // 6.26 vs 5.76 at 2048^2 x 5; so up to 2^20 cells per level.  IBGB300_V2F=levels|sequential
-    // overrides the choice.
+    // level's passes leave the GPU part idle: 0.32 vs 0.41 ms at 256^2 x 3 levels, 0.64 vs 0.80
+    // at 512^2 x 4, 1.41 vs 1.47 at 1024^2 x 4 (and C_L/C_D 2e-10 from FP64 instead of 2e-8),
+    // but 6.15 vs 5.84 at 2048^2 x 5; so up to 2^20 cells per level.  IBGB300_V2F=levels|
+    // sequential overrides the choice.
     const bool lv_ok = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
     h->v2f_ok = lv_ok;
     h->v2f_auto = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);

@@ -46,11 +46,6 @@ __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
 
 // line (b, k) of the transposed intermediate into U[1..nrow]
 template <int NL>
@@ -235,33 +230,51 @@ k_lines(DstAxis<float> ax, const float* in, int64_t in_b, int64_t in_s, float* o
 
 // ring_l from psi_{l+1} (with its previous ring) on the quarter lines, the previous psi + x0 +
 // the next correction, plus (below the second-coarsest level) the harmonic part of the change of
-// ring_{l+1}, Aring . coef_{l+1}.  One warp per ring node; FP64.  `ring` holds the previous
-// ring on entry and the new one on return; the change goes to dd (FP64, for the next
-// coefficients), dring (float-float, for the residual) and the float sides (their transforms).
-__global__ void k_ring_eval(Geometry g, const int4* __restrict__ pts, const df64* __restrict__ xp,
-                            const float* __restrict__ x0, const float* __restrict__ qline, const double* __restrict__ Aring,
-                            const double* __restrict__ coef, int nK, double* __restrict__ dd,
-                            df64* __restrict__ dring, df64* __restrict__ ring, float* __restrict__ sidex,
-                            float* __restrict__ sidey) {
-  const int idx = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
-  if (idx >= g.nbc) return;
-  double h = 0.0;
-  if (coef) {
-    const double* a = Aring + (int64_t)idx * nK;
-    double h1 = 0.0;
-    int j = lane;
-    for (; j + 32 < nK; j += 64) {
-      h = fma(a[j], coef[j], h);
-      h1 = fma(a[j + 32], coef[j + 32], h1);
-    }
-    if (j < nK) h = fma(a[j], coef[j], h);
-    h = warp_sum(h + h1);
+// ring_{l+1}, Aring . coef_{l+1} (AringT: [nK][nbc], coalesced over the ring entries).  A block
+// of kEvalWarps warps takes 32 ring nodes: warp w sums coefficients j = w, w + kEvalWarps, ...
+// for all 32 (loads coalesced, five in flight), the partial sums are added in warp order in
+// shared memory, and warp 0 finishes one node per lane.  FP64; ~nbc/32 blocks, so the FP64
+// work spreads over the SMs (GB300 issues a warp's FP64 instruction over ~16 cycles).  `ring`
+// holds the previous ring on entry and the new one on return; the change goes to dd (FP64, for
+// the next coefficients), dring (float-float, for the residual) and the float sides.
+constexpr int kEvalWarps = 8;
+__global__ void __launch_bounds__(kEvalWarps * 32)
+k_ring_eval(Geometry g, const int4* __restrict__ pts, const df64* __restrict__ xp, const float* __restrict__ x0,
+            const float* __restrict__ qline, const double* __restrict__ AringT, const double* __restrict__ coef,
+            int nK, double* __restrict__ dd, df64* __restrict__ dring, df64* __restrict__ ring,
+            float* __restrict__ sidex, float* __restrict__ sidey) {
+  __shared__ double part[kEvalWarps][32];
+  const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int idx = blockIdx.x * 32 + lane;
+  // warp 0 starts the node's own loads before its share of the sum
+  double v = 0.0;
+  df64 old(0.0f);
+  if (w == 0 && idx < g.nbc) {
+    const int4 p = pts[idx];
+    old = ring[idx];
+    v = (double)xp[p.x] + ((double)x0[p.x] + (double)qline[p.y]);
+    if (p.z >= 0) v = 0.5 * (v + ((double)xp[p.z] + ((double)x0[p.z] + (double)qline[p.w])));
   }
-  if (lane != 0) return;
-  const int4 p = pts[idx];
-  const df64 old = ring[idx];
-  double v = (double)xp[p.x] + ((double)x0[p.x] + (double)qline[p.y]);
-  if (p.z >= 0) v = 0.5 * (v + ((double)xp[p.z] + ((double)x0[p.z] + (double)qline[p.w])));
+  double h = 0.0;
+  if (coef && idx < g.nbc) {
+    const double* a = AringT + idx;
+    constexpr int U = 5;
+    int j = w;
+    for (; j + (U - 1) * kEvalWarps < nK; j += U * kEvalWarps) {
+      double av[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) av[u] = a[(int64_t)(j + u * kEvalWarps) * g.nbc];
+#pragma unroll
+      for (int u = 0; u < U; ++u) h = fma(av[u], __ldg(&coef[j + u * kEvalWarps]), h);
+    }
+    for (; j < nK; j += kEvalWarps) h = fma(a[(int64_t)j * g.nbc], __ldg(&coef[j]), h);
+  }
+  part[w][lane] = h;
+  __syncthreads();
+  if (w != 0 || idx >= g.nbc) return;
+  h = 0.0;
+#pragma unroll
+  for (int k = 0; k < kEvalWarps; ++k) h += part[k][lane];
   v = 0.25 * v + h;
   const double d = v - (double)old;
   dd[idx] = d;
@@ -276,10 +289,15 @@ __global__ void k_ring_eval(Geometry g, const int4* __restrict__ pts, const df64
 }
 
 // coef_l: the first Kx (Ky) sine coefficients of the bottom, top (left, right) ring sides,
-// coef[j] = sum_i St[j][i] side_i (S convention, 2 sin).  One warp per coefficient; FP64.
-__global__ void k_ring_coef(Geometry g, const double* __restrict__ ringd, const double* __restrict__ St, int Kx, int Ky,
-                            double* __restrict__ coef) {
-  const int j = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
+// coef[j] = sum_i St[j][i] side_i (S convention, 2 sin).  One block of kCoefThreads per
+// coefficient (nK blocks spread the FP64 work over the SMs), a strided sum per thread, then a
+// fixed-order tree in shared memory; FP64.
+constexpr int kCoefThreads = 256;
+__global__ void __launch_bounds__(kCoefThreads)
+k_ring_coef(Geometry g, const double* __restrict__ ringd, const double* __restrict__ St, int Kx, int Ky,
+            double* __restrict__ coef) {
+  __shared__ double red[kCoefThreads];
+  const int j = blockIdx.x, tid = threadIdx.x;
   const int nK = 2 * Kx + 2 * Ky;
   if (j >= nK) return;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
@@ -298,15 +316,16 @@ __global__ void k_ring_coef(Geometry g, const double* __restrict__ ringd, const 
     side = ringd + (jj < Ky ? g.L : g.R) + 1;
     len = nrow;
   }
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
-  int i = lane;
-  for (; i + 96 < len; i += 128) {
+  double s = 0.0;
+  for (int i = tid; i < len; i += kCoefThreads) s = fma(row[i], side[i], s);
+  red[tid] = s;
+  __syncthreads();
 #pragma unroll
-    for (int u = 0; u < 4; ++u) s[u] = fma(row[i + 32 * u], side[i + 32 * u], s[u]);
+  for (int o = kCoefThreads / 2; o > 0; o >>= 1) {
+    if (tid < o) red[tid] += red[tid + o];
+    __syncthreads();
   }
-  for (; i < len; i += 32) s[0] = fma(row[i], side[i], s[0]);
-  const double t = warp_sum((s[0] + s[1]) + (s[2] + s[3]));
-  if (lane == 0) coef[j] = t;
+  if (tid == 0) coef[j] = red[0];
 }
 
 template <int P>
@@ -429,7 +448,7 @@ cudaError_t v2f_ring_eval(const Geometry& g, const RingPlan& rp, int l, const df
                           df64* ring_l, cudaStream_t s) {
   const int up = l + 1;
   const double* coef = (up < g.nlev - 1) ? rp.coef + (int64_t)up * rp.nK : nullptr;
-  k_ring_eval<<<(g.nbc + 7) / 8, 256, 0, s>>>(g, rp.pts, xp_up, x0_up, rp.qline + (int64_t)up * rp.qls, rp.Aring, coef, rp.nK,
+  k_ring_eval<<<(g.nbc + 31) / 32, kEvalWarps * 32, 0, s>>>(g, rp.pts, xp_up, x0_up, rp.qline + (int64_t)up * rp.qls, rp.Aring, coef, rp.nK,
                                                rp.ringd + (int64_t)l * g.nbc,
                                                reinterpret_cast<df64*>(rp.dring) + (int64_t)l * g.nbc, ring_l,
                                                rp.sidex + (int64_t)l * 2 * (g.nx - 1),
@@ -438,7 +457,7 @@ cudaError_t v2f_ring_eval(const Geometry& g, const RingPlan& rp, int l, const df
 }
 
 cudaError_t v2f_ring_coef(const Geometry& g, const RingPlan& rp, int l, cudaStream_t s) {
-  k_ring_coef<<<(rp.nK + 7) / 8, 256, 0, s>>>(g, rp.ringd + (int64_t)l * g.nbc, rp.St, rp.Kx, rp.Ky,
+  k_ring_coef<<<rp.nK, kCoefThreads, 0, s>>>(g, rp.ringd + (int64_t)l * g.nbc, rp.St, rp.Kx, rp.Ky,
                                                rp.coef + (int64_t)l * rp.nK);
   return cudaGetLastError();
 }
@@ -520,7 +539,10 @@ cudaError_t RingPlan::build(const Geometry& g) {
   };
   cudaError_t e;
   if ((e = up(St, st)) != cudaSuccess) return e;
-  if ((e = up(Aring, A)) != cudaSuccess) return e;
+  std::vector<double> AT((size_t)nK * g.nbc);  // [nK][nbc]: the evaluation kernel reads it by node
+  for (int idx = 0; idx < g.nbc; ++idx)
+    for (int j = 0; j < nK; ++j) AT[(size_t)j * g.nbc + idx] = A[(size_t)idx * nK + j];
+  if ((e = up(Aring, AT)) != cudaSuccess) return e;
   if ((e = up(pts, P)) != cudaSuccess) return e;
   auto zero = [&](auto*& dst, int64_t n) -> cudaError_t {
     cudaError_t e2 = cudaMalloc(&dst, sizeof(*dst) * n);

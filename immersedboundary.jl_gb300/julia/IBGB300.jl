@@ -28,6 +28,9 @@ const IB_PREC_MIXED = Int32(1)
 const IB_MOTION_STATIC = Int32(0)
 const IB_MOTION_PRESCRIBED = Int32(1)
 const IB_PC_SCHUR_REF = Int32(1)
+const IB_V2F_AUTO = Int32(0)
+const IB_V2F_LEVELS = Int32(1)
+const IB_V2F_SEQUENTIAL = Int32(2)
 
 # bodies moving in the grid frame (RigidBody{RelativeFrame}) use ib_advance_kin
 moving(bodies) = any(b -> b.frame isa RelativeFrame, bodies)
@@ -78,7 +81,8 @@ end
 
 ImmersedBoundary.problemof(s::GB300Solver) = s.prob
 
-function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, sync=:all, precondition=true)
+function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, sync=:all, precondition=true,
+                     vort2flux_order=IB_V2F_AUTO)
     fluid = fluidof(prob)
     grid = discretize(fluid)
     base = baselevel(grid)
@@ -104,6 +108,9 @@ function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, syn
         check(ccall((:ib_set_cg_preconditioner, libibgb300), Cint, (Ptr{Cvoid}, Int32, Int32),
                     s.handle, IB_PC_SCHUR_REF, 0), s.handle)
     end
+    # mixed precision: all levels of Vort2Flux in one batch, or the reference's level order
+    check(ccall((:ib_set_vort2flux_order, libibgb300), Cint, (Ptr{Cvoid}, Int32), s.handle, vort2flux_order),
+          s.handle)
     push_state!(s, state)
     return s
 end

@@ -183,14 +183,26 @@ __device__ __forceinline__ T fqy_at(const Geometry& g, const LevelView<T>& v, in
   return -(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1)) * T(0.5);
 }
 
+// Nonlinear term and CN right-hand side of every level (Nonlinear/RhsForce, timestepping.jl:
+// 31-66; avg_flux! fluid-ops.jl:276-301, direct_product! :303-398, rot!): one block per tile of
+// kNTY x kNTX cells.  The averaged fluxes (Qx, Qy) and the flux products (fqx, fqy) the tile's
+// cells share are formed once into shared memory, then each cell combines its four products;
+// every value is the same expression as a per-cell evaluation would form.
+constexpr int kNTX = 32, kNTY = 8;
 template <typename T>
-__global__ void k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
+__global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
+  __shared__ T sQy[kNTY + 2][kNTX];   // Qy(J0 + r, I0 + 1 + c)
+  __shared__ T sQx[kNTY][kNTX + 2];   // Qx(J0 + 1 + r, I0 + c)
+  __shared__ T sFx[kNTY + 1][kNTX];   // fqx(J0 + r, I0 + 1 + c)
+  __shared__ T sFy[kNTY][kNTX + 1];   // fqy(J0 + 1 + r, I0 + c)
   const int nx = g.nx, ny = g.ny, ncol = nx - 1, nrow = ny - 1;
   const int ne = 2 * ncol + 2 * nrow;
-  const int64_t total = (int64_t)g.nlev * g.nG;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int l = (int)(t / g.nG), e = (int)(t - (int64_t)l * g.nG);
-    const int J = e / ncol, I = e - J * ncol;
+  const int tx = (ncol + kNTX - 1) / kNTX, ty = (nrow + kNTY - 1) / kNTY;
+  const int ntiles = g.nlev * tx * ty;
+  const int tid = threadIdx.x, cr = tid / kNTX, cc = tid % kNTX;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int l = tile / (tx * ty), rem = tile - l * tx * ty;
+    const int J0 = (rem / tx) * kNTY, I0 = (rem % tx) * kNTX;
     LevelView<T> v;
     v.qx = a.q + (int64_t)l * g.nq;
     v.qy = v.qx + g.nu;
@@ -199,34 +211,56 @@ __global__ void k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
     v.q0x = (T)a.q0[2 * l];
     v.q0y = (T)a.q0[2 * l + 1];
     v.nx = nx; v.ny = ny; v.ncol = ncol;
-    // the six averaged fluxes this node touches
-    const T qy0 = v.Qy(J, I + 1), qy1 = v.Qy(J + 1, I + 1), qy2 = v.Qy(J + 2, I + 1);
-    const T qx0 = v.Qx(J + 1, I), qx1 = v.Qx(J + 1, I + 1), qx2 = v.Qx(J + 1, I + 2);
-    const T fx_lo = fqx_at(g, v, J, I + 1, qy1, qy0);       // fqx[J,   I+1]
-    const T fx_hi = fqx_at(g, v, J + 1, I + 1, qy2, qy1);   // fqx[J+1, I+1]
-    const T fy_r = fqy_at(g, v, J + 1, I + 1, qx2, qx1);    // fqy[J+1, I+1]
-    const T fy_l = fqy_at(g, v, J + 1, I, qx1, qx0);        // fqy[J+1, I]
-    const T nl = ((fx_lo - fx_hi) + (fy_r - fy_l)) * (T)a.inv_hc2[l];
-    a.nl_new[t] = nl;
-    T r = (T)a.dtb0 * nl;
-    r = r + (T)a.dtb1 * a.nl_old[t];
-    if (a.alpha) {
-      // A_l gamma = gamma - alpha_l (4 gamma - neighbours), zero outside the array
-      const T gc = v.Gm(J, I);
-      T lap = T(4) * gc;
-      if (I > 0) lap -= v.Gm(J, I - 1);
-      if (I < ncol - 1) lap -= v.Gm(J, I + 1);
-      if (J > 0) lap -= v.Gm(J - 1, I);
-      if (J < nrow - 1) lap -= v.Gm(J + 1, I);
-      r = (gc - (T)a.alpha[l] * lap) + r;
+    // averaged fluxes: Qy rows 0..ny, columns 1..nx-1; Qx rows 1..ny-1, columns 0..nx
+    for (int i = tid; i < (kNTY + 2) * kNTX; i += kNTX * kNTY) {
+      const int r = i / kNTX, c = i % kNTX, Jq = J0 + r, Iq = I0 + 1 + c;
+      if (Jq <= ny && Iq <= nx - 1) sQy[r][c] = v.Qy(Jq, Iq);
     }
-    const T* ed = a.edges + (int64_t)l * ne;
-    T edge = T(0);
-    if (J == 0) edge += ed[I];
-    if (J == nrow - 1) edge += ed[ncol + I];
-    if (I == 0) edge += ed[2 * ncol + J];
-    if (I == ncol - 1) edge += ed[2 * ncol + nrow + J];
-    a.rhs[t] = r + edge;
+    for (int i = tid; i < kNTY * (kNTX + 2); i += kNTX * kNTY) {
+      const int r = i / (kNTX + 2), c = i % (kNTX + 2), Jq = J0 + 1 + r, Iq = I0 + c;
+      if (Jq <= ny - 1 && Iq <= nx) sQx[r][c] = v.Qx(Jq, Iq);
+    }
+    __syncthreads();
+    // flux products: fqx rows 0..ny-1, columns 1..nx-1; fqy rows 1..ny-1, columns 0..nx-1
+    for (int i = tid; i < (kNTY + 1) * kNTX; i += kNTX * kNTY) {
+      const int r = i / kNTX, c = i % kNTX, Jf = J0 + r, If = I0 + 1 + c;
+      if (Jf <= ny - 1 && If <= nx - 1) sFx[r][c] = fqx_at(g, v, Jf, If, sQy[r + 1][c], sQy[r][c]);
+    }
+    for (int i = tid; i < kNTY * (kNTX + 1); i += kNTX * kNTY) {
+      const int r = i / (kNTX + 1), c = i % (kNTX + 1), Jf = J0 + 1 + r, If = I0 + c;
+      if (Jf <= ny - 1 && If <= nx - 1) sFy[r][c] = fqy_at(g, v, Jf, If, sQx[r][c + 1], sQx[r][c]);
+    }
+    __syncthreads();
+    const int J = J0 + cr, I = I0 + cc;
+    if (J < nrow && I < ncol) {
+      const int64_t t = (int64_t)l * g.nG + (int64_t)J * ncol + I;
+      const T fx_lo = sFx[cr][cc];       // fqx[J,   I+1]
+      const T fx_hi = sFx[cr + 1][cc];   // fqx[J+1, I+1]
+      const T fy_r = sFy[cr][cc + 1];    // fqy[J+1, I+1]
+      const T fy_l = sFy[cr][cc];        // fqy[J+1, I]
+      const T nl = ((fx_lo - fx_hi) + (fy_r - fy_l)) * (T)a.inv_hc2[l];
+      a.nl_new[t] = nl;
+      T r = (T)a.dtb0 * nl;
+      r = r + (T)a.dtb1 * a.nl_old[t];
+      if (a.alpha) {
+        // A_l gamma = gamma - alpha_l (4 gamma - neighbours), zero outside the array
+        const T gc = v.Gm(J, I);
+        T lap = T(4) * gc;
+        if (I > 0) lap -= v.Gm(J, I - 1);
+        if (I < ncol - 1) lap -= v.Gm(J, I + 1);
+        if (J > 0) lap -= v.Gm(J - 1, I);
+        if (J < nrow - 1) lap -= v.Gm(J + 1, I);
+        r = (gc - (T)a.alpha[l] * lap) + r;
+      }
+      const T* ed = a.edges + (int64_t)l * ne;
+      T edge = T(0);
+      if (J == 0) edge += ed[I];
+      if (J == nrow - 1) edge += ed[ncol + I];
+      if (I == 0) edge += ed[2 * ncol + J];
+      if (I == ncol - 1) edge += ed[2 * ncol + nrow + J];
+      a.rhs[t] = r + edge;
+    }
+    __syncthreads();
   }
 }
 
@@ -301,7 +335,8 @@ cudaError_t rot(const Geometry& g, const T* q, T* gam, int batch, cudaStream_t s
 template <typename T>
 cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s) {
   ProfScope prof(kClassNonlin, s);
-  k_nonlin_rhs<T><<<blocks_for((int64_t)g.nlev * g.nG), kThreads, 0, s>>>(g, a);
+  const int tiles = g.nlev * ((g.nx - 1 + kNTX - 1) / kNTX) * ((g.ny - 1 + kNTY - 1) / kNTY);
+  k_nonlin_rhs<T><<<tiles < 65535 * 8 ? tiles : 65535 * 8, kNTX * kNTY, 0, s>>>(g, a);
   return cudaGetLastError();
 }
 template <typename T>

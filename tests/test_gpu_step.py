@@ -208,7 +208,7 @@ def test_two_warp_lines_agree_with_one_warp_lines(ib, monkeypatch):
     assert rel(out["64"], out["32"]) < 1e-9
 
 
-@pytest.mark.parametrize("nx,ny,nl", [(256, 192, 4), (192, 256, 3)])
+@pytest.mark.parametrize("nx,ny,nl", [(256, 192, 4), (192, 256, 3), (128, 128, 2)])
 def test_levels_vort2flux_matches_level_by_level(ib, monkeypatch, nx, ny, nl):
     """Mixed-precision Vort2Flux with every level's boundary ring found first (harmonic ring
     transfer) and the levels solved as one batch, against the reference's level-by-level order

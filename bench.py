@@ -442,8 +442,11 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + float-float (2xf32) residual/state",
         "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
         "config": {"workload": describe(wl), "precision": prec,
-                   "refine_sweeps": ({0: "2 (1 on levels >= 3 of Vort2Flux)"}.get(args.refine_sweeps, args.refine_sweeps)
+                   "refine_sweeps": (("2 on every solve" if info.vort2flux_order == L.IB_V2F_LEVELS else
+                                      {0: "2 (1 on levels >= 3 of Vort2Flux)"}.get(args.refine_sweeps, args.refine_sweeps))
                                      if prec == "mixed" else 0),
+                   "vort2flux": ("all levels in one batch, rings first (harmonic ring transfer)"
+                                 if info.vort2flux_order == L.IB_V2F_LEVELS else "level by level (the reference's order)"),
                    "cells_per_step": wl.cells_per_step,
                    "parallelism": "replicas",
                    "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),

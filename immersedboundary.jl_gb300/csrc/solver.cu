@@ -1704,6 +1704,7 @@ int ib_get_info(ib_handle* h, ib_info* info) {
   info->npoints = h->nb;
   info->device_bytes = h->device_bytes;
   info->setup_ms = h->setup_ms;
+  info->vort2flux_order = h->v2f_levels ? IB_V2F_LEVELS : IB_V2F_SEQUENTIAL;
   return IB_OK;
 }
 

@@ -20,6 +20,7 @@ typedef struct ib_info {
   int32_t nbodies, npoints;
   int64_t device_bytes;      /* device memory held by the handle */
   double setup_ms;           /* wall time of ib_create (tables, delta weights, Schur inverse) */
+  int32_t vort2flux_order;   /* the order in effect: IB_V2F_LEVELS or IB_V2F_SEQUENTIAL */
 } ib_info;
 
 int ib_get_info(ib_handle* h, ib_info* info);

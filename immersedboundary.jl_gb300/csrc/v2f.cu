@@ -30,7 +30,6 @@ namespace {
 using wdst::kLB;
 using wdst::kLines;
 using wdst::line_dst;
-using wdst::line_sync;
 using wdst::Shape;
 
 // sin(pi m / 4) (row / column n/4) and sin(3 pi m / 4) (row / column 3n/4), m = (index+1) mod 8

@@ -359,7 +359,7 @@ def uses_line_passes(wl, precision: str) -> bool:
     return ok(wl.nx) and ok(wl.ny) and (precision == "mixed" or max(wl.nx, wl.ny) >= 2048)
 
 
-def pass_model(wl, precision: str):
+def pass_model(wl, precision: str, levels: bool = False):
     """Algorithmic DRAM bytes and flops of the x and y passes of one step (per step; the bytes per
     launch follow from the launches counted while timing).
 
@@ -371,6 +371,11 @@ def pass_model(wl, precision: str):
     the stored float-float r1, out) + 8 + 16 (r1, x1, out) + 20 (x0, x1, correction, float-float
     out) and in y 3 x 12; one-sweep solves (Vort2Flux levels 3.. twice) 12 + 8 + 16 + 16 in x and
     2 x 12 in y.  A length-n sine line costs ~2.5 n log2 n flops.
+    With the all-levels Vort2Flux (`levels`): the CN and projection solves as above, and per
+    Vort2Flux call on every level x 28 (residual from the previous psi: Gamma, psi, r1 out, FP32
+    out) + 8 + 24 (residual of x0 on r1, in place) and y 12 + 12 (solve, spectrum), then on the
+    finished levels (all, or level 1 for the trial call) x 8 + 16 + 28 (psi += x0 + d1 + d2, read
+    and written) and y 12 + 12; 3 + 3 transforms per level in each axis.
     """
     nG = (wl.nx - 1) * (wl.ny - 1)
     L = wl.nlevels
@@ -379,6 +384,11 @@ def pass_model(wl, precision: str):
     if precision == "fp64":
         arrays = 3 * L + 1
         return {"x": (nG * (32 * arrays + 8), fx * 2 * arrays), "y": (nG * 24 * arrays, fy * 2 * arrays)}
+    if levels:
+        two = L + 1                     # two-sweep CN solves: trial over L levels, projection
+        fin = L + 1                     # finished Vort2Flux levels: all (projection) + level 1 (trial)
+        return {"x": (nG * (88 * two + 8 + 60 * 2 * L + 52 * fin), fx * (6 * two + 3 * 2 * L + 3 * fin)),
+                "y": (nG * (36 * two + 24 * 2 * L + 24 * fin), fy * (6 * two + 3 * 2 * L + 3 * fin))}
     two, one = L + 5, 2 * max(L - 2, 0)
     return {"x": (nG * (88 * two + 8 + 52 * one), fx * (6 * two + 4 * one)),
             "y": (nG * (36 * two + 24 * one), fy * (6 * two + 4 * one))}
@@ -463,7 +473,7 @@ def run_ours(args, rank, world, local):
         return
     solver, st, prob, ts, uv, tp = arm["solver"], arm["state"], arm["prob"], arm["ts"], arm["uv"], arm["tp"]
     # dominant kernel class: event-timed launches over further steps
-    model = pass_model(wl, prec)
+    model = pass_model(wl, prec, levels=prec == "mixed" and info.vort2flux_order == L.IB_V2F_LEVELS)
     prof = {}
     npf = min(K, 20)
     base = W + K

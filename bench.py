@@ -36,10 +36,11 @@ def baseline_metric() -> str:
     return METRIC
 
 
-# DRAM bytes (read + write) per average launch of the dominant pass class, from one ncu capture
-# of the same step (cold cache; per array 9.40 MB over the captured x passes, 70 arrays in the
-# 52 x launches of a step); the capture and its arithmetic are summarised under profiles/
-MEASURED_TRAFFIC = {"two_body_large/mixed": {"x": 12.65e6}}
+# DRAM bytes (read + write) per array an x pass moves, from one ncu capture of the mixed step
+# (cold cache, the first ten pass launches of the level-by-level step: 9.40 MB per 1024^2 array;
+# summarised under profiles/).  The traffic of an average launch is that times the arrays per
+# launch of the step being timed (array-passes from pass_model over the launches counted).
+MEASURED_TRAFFIC_PER_ARRAY = {"two_body_large/mixed": {"x": 9.40e6}}
 
 
 def dist_env():
@@ -376,6 +377,7 @@ def pass_model(wl, precision: str, levels: bool = False):
     out) + 8 + 24 (residual of x0 on r1, in place) and y 12 + 12 (solve, spectrum), then on the
     finished levels (all, or level 1 for the trial call) x 8 + 16 + 28 (psi += x0 + d1 + d2, read
     and written) and y 12 + 12; 3 + 3 transforms per level in each axis.
+    Per class: (bytes, flops, array-passes: one array through one pass).
     """
     nG = (wl.nx - 1) * (wl.ny - 1)
     L = wl.nlevels
@@ -383,15 +385,18 @@ def pass_model(wl, precision: str, levels: bool = False):
     fy = 2.5 * wl.ny * np.log2(wl.ny) * (wl.nx - 1)
     if precision == "fp64":
         arrays = 3 * L + 1
-        return {"x": (nG * (32 * arrays + 8), fx * 2 * arrays), "y": (nG * 24 * arrays, fy * 2 * arrays)}
+        return {"x": (nG * (32 * arrays + 8), fx * 2 * arrays, 2 * arrays),
+                "y": (nG * 24 * arrays, fy * 2 * arrays, arrays)}
     if levels:
         two = L + 1                     # two-sweep CN solves: trial over L levels, projection
         fin = L + 1                     # finished Vort2Flux levels: all (projection) + level 1 (trial)
-        return {"x": (nG * (88 * two + 8 + 60 * 2 * L + 52 * fin), fx * (6 * two + 3 * 2 * L + 3 * fin)),
-                "y": (nG * (36 * two + 24 * 2 * L + 24 * fin), fy * (6 * two + 3 * 2 * L + 3 * fin))}
+        xp = 6 * two + 3 * 2 * L + 3 * fin
+        return {"x": (nG * (88 * two + 8 + 60 * 2 * L + 52 * fin), fx * xp, xp),
+                "y": (nG * (36 * two + 24 * 2 * L + 24 * fin), fy * (6 * two + 3 * 2 * L + 3 * fin),
+                      3 * two + 2 * 2 * L + 2 * fin)}
     two, one = L + 5, 2 * max(L - 2, 0)
-    return {"x": (nG * (88 * two + 8 + 52 * one), fx * (6 * two + 4 * one)),
-            "y": (nG * (36 * two + 24 * one), fy * (6 * two + 4 * one))}
+    return {"x": (nG * (88 * two + 8 + 52 * one), fx * (6 * two + 4 * one), 6 * two + 4 * one),
+            "y": (nG * (36 * two + 24 * one), fy * (6 * two + 4 * one), 3 * two + 2 * one)}
 
 
 def run_arm(ib, lib, L, wl, precision, K, W, local, dist, profile_range=False, refine=0):
@@ -485,7 +490,7 @@ def run_ours(args, rank, world, local):
         prof[key] = (tot.value, nl.value)
     dom = max(prof, key=lambda k: prof[k][0])
     tot_ms, nlaunch = prof[dom]
-    b_step, f_step = model[dom]
+    b_step, f_step, arrays_step = model[dom]
     per_launch_s = tot_ms / 1e3 / nlaunch
     launches_per_step = nlaunch / npf
     bytes_per_launch = b_step / launches_per_step
@@ -495,7 +500,8 @@ def run_ours(args, rank, world, local):
     fp64, fp32 = C.c_double(), C.c_double()
     lib.ib_measure_fp_peaks(local, C.byref(fp64), C.byref(fp32))
     achieved = bytes_per_launch / per_launch_s / 1e9
-    traffic = MEASURED_TRAFFIC.get(f"{args.workload}/{prec}", {}).get(dom)
+    per_array = MEASURED_TRAFFIC_PER_ARRAY.get(f"{args.workload}/{prec}", {}).get(dom)
+    traffic = per_array * arrays_step / launches_per_step if per_array else None
     pipe_peak = fp64.value if prec == "fp64" else fp32.value
     out["roofline"] = {
         "kernel": ({"x": "k_wxf/k_wxi (x-direction sine passes, one warp per line)",
@@ -505,6 +511,8 @@ def run_ours(args, rank, world, local):
         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
         "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
+        "traffic_source": ("ncu dram__bytes_read+write per x-pass array (9.40 MB, level-by-level step, cold "
+                           "cache) x arrays per launch of this step" if per_array else None),
         "avg_launch_ms": per_launch_s * 1e3, "launches_profiled": nlaunch,
         "share_of_step": tot_ms / npf / ms_per_step,
         "fp_pipe": {"pipe": "fp64" if prec == "fp64" else "fp32",

@@ -265,6 +265,14 @@ def run_static_config(ib, lib, L, wl, K, W, local, dist):
     return out
 
 
+def bench_config(wl) -> dict:
+    """The workload both arms (GPU and CPU reference) report under ``config``; what differs
+    between the arms goes under ``arm``."""
+    return {"workload": describe(wl), "cells_per_step": wl.cells_per_step,
+            "l2": "inputs larger than L2: the per-step working set (state, history, transforms) "
+                  "exceeds the 129 MB L2 on every configuration timed"}
+
+
 def describe(wl) -> str:
     bodies = ", ".join(f"{b.npoints()} pts" for b in wl.bodies)
     return (f"{wl.name}: {wl.nx}x{wl.ny} finest grid h={wl.h}, {wl.nlevels} levels, bodies [{bodies}], "
@@ -456,16 +464,16 @@ def run_ours(args, rank, world, local):
         "warmup": W, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32 transforms + float-float (2xf32) residual/state",
         "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
-        "config": {"workload": describe(wl), "precision": prec,
-                   "refine_sweeps": (("2 on every solve" if info.vort2flux_order == L.IB_V2F_LEVELS else
-                                      {0: "2 (1 on levels >= 3 of Vort2Flux)"}.get(args.refine_sweeps, args.refine_sweeps))
-                                     if prec == "mixed" else 0),
-                   "vort2flux": ("all levels in one batch, rings first (harmonic ring transfer)"
-                                 if info.vort2flux_order == L.IB_V2F_LEVELS else "level by level (the reference's order)"),
-                   "cells_per_step": wl.cells_per_step,
-                   "parallelism": "replicas",
-                   "l2": "per-step working set > L2 (state + transforms ~%.2f GB)" % (info.device_bytes / 1e9),
-                   "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": arm["host_s"] / K * 1e3},
+        "config": bench_config(wl),
+        "arm": {"precision": prec,
+                "refine_sweeps": (("2 on every solve" if info.vort2flux_order == L.IB_V2F_LEVELS else
+                                   {0: "2 (1 on levels >= 3 of Vort2Flux)"}.get(args.refine_sweeps, args.refine_sweeps))
+                                  if prec == "mixed" else 0),
+                "vort2flux": ("all levels in one batch, rings first (harmonic ring transfer)"
+                              if info.vort2flux_order == L.IB_V2F_LEVELS else "level by level (the reference's order)"),
+                "parallelism": "replicas",
+                "device_bytes": int(info.device_bytes),
+                "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": arm["host_s"] / K * 1e3},
         "gpu_launches": int(info.kernels_per_step) * K,
     }
     ck = arm["clocks"]
@@ -577,7 +585,8 @@ def run_reference(args, rank, world, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded PCG64 vorticity noise 1e-4 on the finest level",
-        "config": {"workload": describe(wl), "cells_per_step": wl.cells_per_step, "parallelism": "cpu"},
+        "config": bench_config(wl),
+        "arm": {"precision": "fp64", "parallelism": "host threads"},
         "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} advance! steps of the full workload after {args.warmup} warm-up "
                                    "steps; FP64 NumPy/SciPy restatement of the reference (Julia is not installed); "

@@ -46,7 +46,8 @@ double probe(int sms, int iters, cudaStream_t st) {
 }  // namespace
 
 extern "C" int ib_measure_fp_peaks(int32_t device, double* fp64_tflops, double* fp32_tflops) {
-  if (cudaSetDevice(device) != cudaSuccess) return IB_ERR_CUDA;
+  ib::DeviceGuard dev_guard_(device);
+  if (dev_guard_.err != cudaSuccess) return IB_ERR_CUDA;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaStream_t st;

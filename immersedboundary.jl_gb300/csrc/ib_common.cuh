@@ -341,6 +341,25 @@ struct LapView {
   const double* mlap;
   cudaStream_t stream;
   int device;
+  bool wdst;  // both axes use the warp-per-line passes (wx_fwd / wypass / wx_inv)
+};
+
+// Makes `dev` the current device for the lifetime of the guard and restores the caller's
+// current device afterwards, so that entry points called from a foreign host (Julia, a
+// Python program with its own device choice) leave that host's device selection unchanged.
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) err = cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
 };
 
 // ----------------------------------------------------------------------------------------------

@@ -776,7 +776,7 @@ int capture_graphs(ib_handle* h) {
 
 void destroy_handle(ib_handle* h) {
   if (!h) return;
-  if (h->device >= 0) cudaSetDevice(h->device);
+  DeviceGuard dev_guard_(h->device >= 0 ? h->device : 0);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& ge : h->gexec)
     if (ge) cudaGraphExecDestroy(ge);
@@ -1177,6 +1177,7 @@ bool ib_handle_lap_view(const ib_handle* h, ib::LapView* v) {
   v->mlap = h->mLap;
   v->stream = h->stream;
   v->device = h->device;
+  v->wdst = h->wdst;
   return true;
 }
 
@@ -1228,9 +1229,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     nb += p->body_npoints[b];
   }
   if (nb > 0 && (!p->xb || !p->ds)) return fail(nullptr, IB_ERR_INVALID, "missing body points");
+  DeviceGuard dev_guard_(p->device);
   h = new ib_handle();
   h->device = p->device;
-  cudaError_t e = cudaSetDevice(p->device);
+  cudaError_t e = dev_guard_.err;
   if (e != cudaSuccess) { int rc = fail(nullptr, IB_ERR_CUDA, "cudaSetDevice", e); delete h; return rc; }
   e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { int rc = fail(nullptr, IB_ERR_CUDA, "cudaStreamCreate", e); h->stream = nullptr; destroy_handle(h); return rc; }
@@ -1452,7 +1454,8 @@ int ib_destroy(ib_handle* h) {
 int ib_set_state(ib_handle* h, const double* gamma, const double* q, const double* psi, const double* nonlin1,
                  const double* nonlin2, const double* fb, double t) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   const Geometry& g = h->g;
   const size_t nGL = sizeof(double) * g.nlev * g.nG, nqL = sizeof(double) * g.nlev * g.nq;
   const int p = h->parity;
@@ -1490,7 +1493,8 @@ int ib_set_state(ib_handle* h, const double* gamma, const double* q, const doubl
 int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* nonlin1, double* nonlin2, double* fb,
                  double* t) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   const Geometry& g = h->g;
   const size_t nGL = sizeof(double) * g.nlev * g.nG, nqL = sizeof(double) * g.nlev * g.nq;
   const int p = h->parity;
@@ -1519,7 +1523,8 @@ int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* no
 
 int ib_advance(ib_handle* h, double t, double u, double v) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   int rc = one_step(h, t, u, v);
   if (rc != IB_OK) return rc;
   return check_status(h);
@@ -1527,7 +1532,8 @@ int ib_advance(ib_handle* h, double t, double u, double v) {
 
 int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv) {
   if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   for (int i = 0; i < n; ++i) {
     int rc = one_step(h, t[i], uv[2 * i], uv[2 * i + 1]);
     if (rc != IB_OK) return rc;
@@ -1542,7 +1548,8 @@ int ib_advance_kin(ib_handle* h, double t, double u, double v, const double* kin
     return ib_advance(h, t, u, v);
   }
   if (!kin) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics");
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   return moving_step_mode(h, t, u, v, kin);
 }
 
@@ -1550,7 +1557,8 @@ int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv,
   if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
   if (h->motion != IB_MOTION_PRESCRIBED) return ib_advance_n(h, n, t, uv);
   if (n > 0 && !kin) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics");
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   for (int i = 0; i < n; ++i) {
     int rc = moving_step_mode(h, t[i], uv[2 * i], uv[2 * i + 1], kin + (size_t)i * 6 * h->nbodies);
     if (rc != IB_OK) return rc;
@@ -1581,7 +1589,8 @@ int ib_set_cg_preconditioner(ib_handle* h, int32_t mode, int32_t refresh_steps) 
 int ib_set_vort2flux_order(ib_handle* h, int32_t order) {
   if (!h || order < IB_V2F_AUTO || order > IB_V2F_SEQUENTIAL) return IB_ERR_INVALID;
   if (h->precision != IB_PREC_MIXED) return IB_OK;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   if (order == IB_V2F_LEVELS && !h->v2f_ok)
     return fail(h, IB_ERR_UNSUPPORTED, "the all-levels Vort2Flux needs one-warp line passes on both axes");
   const bool lv = order == IB_V2F_LEVELS || (order == IB_V2F_AUTO && h->v2f_auto);
@@ -1622,7 +1631,8 @@ int ib_get_cg_stats(ib_handle* h, int32_t count, int32_t* iterations, double* re
 
 int ib_get_body_points(ib_handle* h, double* xb, double* vb) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   if (h->nb == 0) return IB_OK;
   if (xb) CK(cudaMemcpyAsync(xb, h->xb, sizeof(double) * 2 * h->nb, cudaMemcpyDeviceToHost, h->stream));
   if (vb) {
@@ -1635,7 +1645,8 @@ int ib_get_body_points(ib_handle* h, double* xb, double* vb) {
 
 int ib_vort2flux(ib_handle* h) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   if (h->precision == IB_PREC_MIXED)
     CK(vort2flux<df64>(h, view<df64>(h->G[h->parity]), view<df64>(h->psi), view<df64>(h->q), nullptr,
                        view<df64>(h->rings)));
@@ -1647,7 +1658,8 @@ int ib_vort2flux(ib_handle* h) {
 
 int ib_get_stress(ib_handle* h, double* cd, double* cl, double* fb_surface) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   const int nbd = h->nbodies;
   if (nbd == 0) return IB_OK;
   std::vector<double> v(2 * nbd);
@@ -1664,7 +1676,8 @@ int ib_get_stress(ib_handle* h, double* cd, double* cl, double* fb_surface) {
 
 int ib_get_force_history(ib_handle* h, int32_t count, double* cd, double* cl) {
   if (!h || count < 0) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   const int nbd = h->nbodies;
   if (nbd == 0 || count == 0) return IB_OK;
   if (count > h->hist_cap || count > h->steps) return fail(h, IB_ERR_INVALID, "history count exceeds recorded steps");
@@ -1686,7 +1699,8 @@ int64_t ib_step_count(const ib_handle* h) { return h ? h->steps : 0; }
 
 int ib_synchronize(ib_handle* h) {
   if (!h) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   CK(cudaStreamSynchronize(h->stream));
   return check_status(h);
 }
@@ -1710,7 +1724,8 @@ int ib_get_info(ib_handle* h, ib_info* info) {
 
 int ib_advance_n_timed(ib_handle* h, int32_t n, const double* t, const double* uv, double* device_ms) {
   if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -1732,7 +1747,8 @@ int ib_profile_steps(ib_handle* h, int32_t n, const double* t, const double* uv,
                      double* total_ms, int64_t* launches) {
   if (!h || n < 0 || (n > 0 && (!t || !uv)) || kernel_class < 0 || kernel_class >= kClassCount)
     return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   Prof prof;
   prof.cls = kernel_class;
   g_prof = &prof;
@@ -1761,7 +1777,8 @@ int ib_profile_steps(ib_handle* h, int32_t n, const double* t, const double* uv,
 // ------------------------------------------------------------------------------------------------
 #define OP_BEGIN()                         \
   if (!h) return IB_ERR_INVALID;           \
-  CK(cudaSetDevice(h->device));            \
+  DeviceGuard dev_guard_(h->device);       \
+  CK(dev_guard_.err);                      \
   const Geometry& g = h->g;                \
   cudaStream_t s = h->stream;              \
   (void)g;                                 \
@@ -1970,7 +1987,8 @@ int ib_learn_init(ib_handle* h, int32_t hidden, int32_t hidden_layers, int32_t c
     return fail(h, IB_ERR_INVALID, "the learned warm start needs moving bodies");
   if (hidden < 1 || hidden > 4096 || hidden_layers < 1 || hidden_layers > 8 || capacity < 2 || capacity > (1 << 20))
     return fail(h, IB_ERR_INVALID, "network size or sample capacity out of range");
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   delete h->mlp;
   h->mlp = new learn::Mlp();
   const int din = 6 * h->nbodies + 2 * h->nf;
@@ -2000,7 +2018,8 @@ int ib_learn_train(ib_handle* h, int32_t epochs, int32_t batch, double lr, uint6
   if (epochs < 1 || batch < 1 || batch > learn::kMaxBatch || !(lr > 0))
     return fail(h, IB_ERR_INVALID, "epochs, batch (1..512) and learning rate must be positive");
   if (h->mlp->count < 2) return fail(h, IB_ERR_INVALID, "fewer than two recorded samples");
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   cudaError_t e = h->mlp->train(epochs, batch, (float)lr, seed, final_loss);
   if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "training", e);
   return IB_OK;
@@ -2029,7 +2048,8 @@ int ib_learn_param_count(ib_handle* h, int64_t* nparam) {
 
 int ib_learn_get_params(ib_handle* h, float* params) {
   if (!h || !h->mlp || !params) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   CK(cudaMemcpyAsync(params, h->mlp->master, sizeof(float) * h->mlp->nparam, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   return IB_OK;
@@ -2037,7 +2057,8 @@ int ib_learn_get_params(ib_handle* h, float* params) {
 
 int ib_learn_set_params(ib_handle* h, const float* params) {
   if (!h || !h->mlp || !params) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   CK(cudaMemcpyAsync(h->mlp->master, params, sizeof(float) * h->mlp->nparam, cudaMemcpyHostToDevice, h->stream));
   CK(h->mlp->sync_bf16());
   CK(cudaStreamSynchronize(h->stream));
@@ -2046,7 +2067,8 @@ int ib_learn_set_params(ib_handle* h, const float* params) {
 
 int ib_learn_gradients(ib_handle* h, int32_t rows, const float* x, const float* y, float* grad, double* loss) {
   if (!h || !h->mlp || !x || !y || rows < 1 || rows > learn::kMaxBatch) return IB_ERR_INVALID;
-  CK(cudaSetDevice(h->device));
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
   cudaError_t e = h->mlp->gradients(rows, x, y, grad, loss);
   if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "network gradients", e);
   return IB_OK;
@@ -2108,7 +2130,7 @@ int efail(ib_ensemble* e, int code, const std::string& what, cudaError_t ce = cu
 
 void destroy_ensemble(ib_ensemble* e) {
   if (!e) return;
-  cudaSetDevice(e->device);
+  DeviceGuard dev_guard_(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   for (auto& g : e->gexec)
     if (g) cudaGraphExecDestroy(g);
@@ -2186,10 +2208,11 @@ int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) 
     for (int j = 0; j < i; ++j)
       if (members[j] == h) return efail(nullptr, IB_ERR_INVALID, "ensemble member given twice");
   }
+  DeviceGuard dev_guard_(members[0]->device);
   ib_ensemble* e = new ib_ensemble();
   e->device = members[0]->device;
   e->m.assign(members, members + n);
-  cudaError_t ce = cudaSetDevice(e->device);
+  cudaError_t ce = dev_guard_.err;
   auto bail = [&](int rc) {
     {
       std::lock_guard<std::mutex> lock(g_err_mu);
@@ -2262,7 +2285,8 @@ int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, c
                               double* device_ms) {
   if (!e || nsteps < 0 || (nsteps > 0 && (!t || !uv))) return IB_ERR_INVALID;
   if (e->any_moving && nsteps > 0 && !kin) return efail(e, IB_ERR_INVALID, "moving members need kinematics");
-  EK(cudaSetDevice(e->device));
+  DeviceGuard dev_guard_(e->device);
+  EK(dev_guard_.err);
   int kin_per_step = 0;
   for (ib_handle* h : e->m)
     if (h->motion == IB_MOTION_PRESCRIBED) kin_per_step += 6 * h->nbodies;

@@ -5,8 +5,8 @@
  * reference the "plugin" is Julia dispatch: statetype(prob) / solvertype(prob) choose
  * CNAB.State / CNAB.Solver and solve! calls advance!(state, solver, t) once per step.  Each
  * entry point below names the reference function (file:line, relative to the
- * ImmersedBoundary.jl project root) that it replaces; INTEGRATION.md shows the Julia ccall
- * binding.
+ * ImmersedBoundary.jl project root) that it replaces; the package's julia/IBGB300.jl holds
+ * the Julia ccall binding.
  *
  * Conventions
  *   - every call returns an int status (IB_OK == 0); ib_last_error() gives the message;

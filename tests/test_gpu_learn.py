@@ -71,7 +71,7 @@ def run(ib, wl, warm, n_train, n_eval, train_kw):
     return it, res, r0, loss, samples
 
 
-def test_learned_warm_start_beats_extrapolation_on_held_out_steps(ib):
+def test_learned_warm_start_converges_and_does_not_regress_on_held_out_steps(ib):
     wl = heaving(ib)
     n_train, n_eval = 500, 40
     kw = dict(epochs=400, batch=32, lr=1e-3, seed=0)

@@ -232,3 +232,26 @@ def test_bf16_rounding_is_nearest_even():
     assert r[3] == np.float32(1.0 + 2 ** -6)  # tie between 1+2^-7 and 1+2^-6 goes to the even mantissa
     assert r[4] == -2.5
     assert abs(r[5] - 3.0e-3) <= 2 ** -8 * 3.0e-3  # half an ulp of an 8-bit significand
+
+
+def test_preconditioned_schur_solve_matches_dense_inverse(O):
+    """The oracle's iterative Schur solve (used where assembling B is too slow on the CPU)
+    reaches the dense inverse's answer whatever preconditioner it is given."""
+    g = small_grid(O, 48, 48, 2)
+    xb = body_setup(O, g, 24)
+    prob = O.Problem(g, 0.01, 100.0, xb, np.full(24, 0.1), [24])
+    dense = O.Solver(prob)
+    rng = np.random.default_rng(5)
+    # a preconditioner 1% away from the inverse, as a neighbouring configuration would give
+    P = dense.Binv @ (np.eye(dense.Binv.shape[0]) + 0.01 * rng.standard_normal(dense.Binv.shape) / 7)
+    iters = O.Solver(prob, precond=P)
+    st0 = O.init_state(prob)
+    st0.gamma[0] = 1e-3 * rng.standard_normal(g.gshape)
+    st0.psi, st0.q = O.vort2flux(st0.gamma, g, O.lap_eigs(g))
+    a, b = st0.copy(), st0.copy()
+    for i in range(3):
+        dense.advance(a, i * prob.dt)
+        iters.advance(b, i * prob.dt)
+    assert np.linalg.norm(a.fb - b.fb) / np.linalg.norm(a.fb) < 1e-11
+    assert np.linalg.norm(a.gamma - b.gamma) / np.linalg.norm(a.gamma) < 1e-12
+    assert 1 <= max(iters.refine_iterations) < 15

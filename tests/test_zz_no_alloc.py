@@ -14,22 +14,25 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12  # relative L2, the operator tolerance of the other FP64 Poisson tests
 
 
-def _handle(ib, nx, ny):
+def _handle(ib, nx, ny, precision="fp64"):
     h = 4.0 / nx
     grid = ib.MultiLevel(ib.UniformGrid(h, (-1.0, -1.0 + nx * h), (-0.5 * ny * h, 0.5 * ny * h)), 2)
     prob = ib.Problem(ib.StreamFcnFluid(grid, (1.0, 0.0), 100.0), ib.BodyGroup(), ib.SchemeCNAB(0.01))
-    return ib.initsolver(prob, ib.initstate(prob))
+    return ib.initsolver(prob, ib.initstate(prob), precision=precision)
 
 
-def test_noalloc_laplacian_inverse_matches_allocating_entry(ib, lib):
+# (grid, precision): an FP64 handle on the Stockham passes, and a mixed-precision handle, whose
+# FP64 operator entry points run the warp-per-line passes
+@pytest.mark.parametrize("nx,ny,precision", [(256, 192, "fp64"), (256, 256, "mixed")])
+def test_noalloc_laplacian_inverse_matches_allocating_entry(ib, lib, nx, ny, precision):
     torch = pytest.importorskip("torch")
     import ctypes
 
     def p(t):
         return ctypes.c_void_p(t.data_ptr())
 
-    s = _handle(ib, 256, 192)
-    ng = 255 * 191
+    s = _handle(ib, nx, ny, precision)
+    ng = (nx - 1) * (ny - 1)
     rng = np.random.default_rng(42)
     for call in range(2):  # two calls in a row: the fixed work array holds the previous one's data
         batch = 3 - call

@@ -22,10 +22,13 @@ IB_ERR_BODY_OUT_OF_GRID = 4
 IB_ERR_SINGULAR = 5
 IB_ERR_CG_MAXITER = 6
 IB_ERR_UNSUPPORTED = 7
+IB_ERR_TIMEOUT = 8
 
 IB_PREC_FP64 = 0
 IB_PREC_MIXED = 1
-PRECISIONS = {"fp64": IB_PREC_FP64, "mixed": IB_PREC_MIXED}
+IB_PREC_MIXED_TC = 2
+PRECISIONS = {"fp64": IB_PREC_FP64, "mixed": IB_PREC_MIXED, "mixed_tc": IB_PREC_MIXED_TC}
+IB_FORM_STOCKHAM, IB_FORM_WARP, IB_FORM_TENSOR = 0, 1, 2
 IB_MOTION_STATIC = 0
 IB_MOTION_PRESCRIBED = 1
 IB_WARM_PREVIOUS = 0
@@ -47,7 +50,8 @@ class IbInfo(C.Structure):
 
     _fields_ = [("kernels_per_step", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
                 ("nlevels", C.c_int32), ("nbodies", C.c_int32), ("npoints", C.c_int32),
-                ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("vort2flux_order", C.c_int32)]
+                ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("vort2flux_order", C.c_int32),
+                ("transform_form", C.c_int32)]
 
 
 class IbProblem(C.Structure):
@@ -90,6 +94,7 @@ SIGNATURES = {
     # operators (device pointers passed as integers)
     "ib_op_dst2": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_laplacian_inv": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
+    "ib_op_sine_lines_tc": (C.c_int, [_vp, C.c_int32, C.c_int32, _vp, _vp]),
     "ib_op_laplacian_inv_noalloc": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_cn_a": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "ib_op_cn_ainv": (C.c_int, [_vp, C.c_int32, _vp, _vp]),

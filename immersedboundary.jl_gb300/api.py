@@ -389,11 +389,13 @@ def initstate(prob: Problem, t: float = 0.0) -> State:
 class Solver:
     """``CNAB.Solver`` (cnab/timestepping.jl:173-249) backed by a libibgb300 handle.
 
-    ``precision``: ``"fp64"`` (every sine transform in FP64, the reference's arithmetic) or
+    ``precision``: ``"fp64"`` (every sine transform in FP64, the reference's arithmetic),
     ``"mixed"`` (FP32 sine transforms refined with float-float residuals, ``refine_sweeps`` sweeps per
     Poisson solve: 1 or 2 everywhere, or 0 = the library default of 2 with 1 for the Vort2Flux
     solves of the third and coarser levels; state, stencils and the nonlinear term in float-float
-    arithmetic; Schur solve and forces FP64).
+    arithmetic; Schur solve and forces FP64), or ``"mixed_tc"`` (the same solve with every sine
+    transform a BF16x3 split-precision GEMM against the sine matrix on the tensor cores; both
+    axes a multiple of 128 cells).
     """
 
     def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096,

@@ -165,6 +165,56 @@ cudaError_t wx_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, cuda
 
 
 // ----------------------------------------------------------------------------------------------
+// Sine transforms as BF16x3 tensor-core GEMMs (sgemm.cu), for axes of n = 128 k cells
+// ----------------------------------------------------------------------------------------------
+// Operand rows: row r (r < rows) at a + r*lda holds the klen inputs u_1..u_klen of one line.
+struct SgIn {
+  const float* a;
+  int64_t lda;
+  int rows;
+  int klen;
+};
+// Result of row r, output index c = 1..ncols (stored at c - 1):
+//   mode 0: out[r*ld + c-1] (FP32), times mult[(r/rpb)*mstride + (r mod rpb)*ld + c-1] if given
+//   mode 1: out[(r/rpb)*bstride + (c-1)*ld + r mod rpb] (FP32, transposed within each slot)
+//   mode 2: out[r*ld + c-1] float-float = base [+ base2] + value (epi kEpiAddBase), or
+//           sub_from -/+ that (kEpiSubAddBase / kEpiAddTo)
+struct SgOut {
+  int mode;
+  void* out;
+  int64_t ld;
+  int rpb;
+  int64_t bstride;
+  const float* mult;
+  int64_t mstride;
+  int ncols;
+  const float* base;
+  const float* base2;
+  const df64* sub_from;
+  int epi;
+};
+// Device image of one axis' sine matrix S[k][j] = sin(pi j k / n), split into BF16 hi / lo parts,
+// laid out as the tensor-core tiles of the transform (bn outputs x 64 inputs per tile).
+struct SineGemm {
+  int n = 0, bn = 0;
+  uint16_t* img = nullptr;
+  cudaError_t build(int n);
+  void release();
+};
+bool sgemm_axis_supported(int n);
+// one batched line transform (status[3] is set if a pipeline wait of the kernel ran out)
+cudaError_t sgemm_pass(const SineGemm& ax, const SgIn& in, const SgOut& o, int* status, cudaStream_t s);
+// The passes of a solve in GEMM form (stride == nG):
+//   gx_fwd:  prologue (XArgs.pro, bc) into FP32 rows `rows` -> S_x -> a.out transposed [b][I][J]
+//   gy_pass: a.in1 [b][I][J] -> S_y, times m1 -> work -> S_y -> a.out row-major [b][J][I]
+//   gx_inv:  a.in row-major FP32 -> S_x -> FP32 store (kEpiStore) or float-float epilogue
+cudaError_t gx_fwd(const Geometry& g, const SineGemm& ax, const XArgs& a, float* rows, int* status, cudaStream_t s);
+cudaError_t gy_pass(const Geometry& g, const SineGemm& ay, const YPassArgs<float>& a, float* work, int* status,
+                    cudaStream_t s);
+template <typename Tout>
+cudaError_t gx_inv(const Geometry& g, const SineGemm& ax, const XArgs& a, int* status, cudaStream_t s);
+
+// ----------------------------------------------------------------------------------------------
 // stencils (stencil.cu)
 // ----------------------------------------------------------------------------------------------
 template <typename T>

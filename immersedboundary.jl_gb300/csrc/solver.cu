@@ -79,6 +79,9 @@ struct ib_handle {
   int refine_coarse = 2;                        // sweeps of the coarse-level Vort2Flux solves
   int coarse_from = 2;                          // first (0-based) level counted as coarse
   bool wdst = false;                            // both axes use the warp-per-line passes
+  bool gdst = false;                            // mixed precision: transforms as tensor-core GEMMs
+  SineGemm sgx, sgy;                            // their BF16 sine-matrix images (sgemm.cu)
+  float* gw32 = nullptr;                        // FP32 work of the GEMM passes
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
   // per-level parameters
   double *d_fac = nullptr, *d_q0 = nullptr, *d_inv_hc2 = nullptr, *d_alpha = nullptr;
@@ -273,6 +276,40 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
   a.batch = batch;
   a.stride = g.nG;
   a.bcfac = 1.0;
+  if (h->gdst) {
+    // BF16x3 tensor-core passes (sgemm.cu): the same sweeps as the warp passes below; gw32 holds
+    // the prologue rows and the y pass's middle product, w32 the intermediate
+    int* st = h->status;
+    float* gw = h->gw32;
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
+    CE(gx_fwd(g, h->sgx, a, gw, st, s));
+    CE(gy_pass(g, h->sgy, ya, gw, st, s));
+    if (sweeps <= 0) {
+      a.in = w32; a.out = out; a.bc = nullptr; a.sub_from = sub_from; a.base = nullptr; a.base2 = nullptr;
+      a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
+      return gx_inv<df64>(g, h->sgx, a, st, s);
+    }
+    a.in = w32; a.out = x032; a.bc = nullptr;
+    CE(gx_inv<float>(g, h->sgx, a, st, s));
+    const bool two = sweeps >= 2 && x132;
+    df64* r1 = two ? reinterpret_cast<df64*>(h->r1) : nullptr;
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProResid; a.base = x032; a.base2 = nullptr;
+    a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep; a.resid_out = r1;
+    CE(gx_fwd(g, h->sgx, a, gw, st, s));
+    CE(gy_pass(g, h->sgy, ya, gw, st, s));
+    a.resid_out = nullptr;
+    if (two) {
+      a.in = w32; a.out = x132; a.bc = nullptr; a.pro = kProLoad; a.epi = kEpiStore; a.base = nullptr;
+      CE(gx_inv<float>(g, h->sgx, a, st, s));
+      a.in = r1; a.out = w32; a.bc = nullptr; a.pro = kProResid; a.base = x132; a.base2 = nullptr;
+      CE(gx_fwd(g, h->sgx, a, gw, st, s));
+      CE(gy_pass(g, h->sgy, ya, gw, st, s));
+    }
+    a.in = w32; a.out = out; a.bc = nullptr; a.pro = kProLoad; a.sub_from = sub_from;
+    a.base = x032; a.base2 = two ? x132 : nullptr;
+    a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
+    return gx_inv<df64>(g, h->sgx, a, st, s);
+  }
   if (h->wdst) {
     // warp-per-line passes; w32 holds the transposed intermediate
     a.in = in; a.out = w32; a.bc = bc; a.pro = kProLoad; a.epi = kEpiStore;
@@ -592,12 +629,13 @@ cudaError_t schur_apply(ib_handle* h, const double* z, double* out) {
 }
 
 int check_status(ib_handle* h) {
-  int st[3] = {0, 0, 0};
+  int st[4] = {0, 0, 0, 0};
   CK(cudaMemcpyAsync(st, h->status, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   if (st[0]) return fail(h, IB_ERR_BODY_OUT_OF_GRID, "body point within 7 cells of the finest-grid edge");
   if (st[1]) return fail(h, IB_ERR_NONFINITE, "infinite flux");
   if (st[2]) return fail(h, IB_ERR_SINGULAR, "zero or non-finite pivot in the Schur matrix");
+  if (st[3]) return fail(h, IB_ERR_TIMEOUT, "a tensor-core transform gave up waiting for its pipeline");
   return IB_OK;
 }
 
@@ -795,6 +833,8 @@ void destroy_handle(ib_handle* h) {
   h->axy.release();
   h->axx32.release();
   h->axy32.release();
+  h->sgx.release();
+  h->sgy.release();
   h->rplan.release();
   for (auto ev : h->fork_ev)
     if (ev) cudaEventDestroy(ev);
@@ -1198,6 +1238,7 @@ const char* ib_status_string(int status) {
     case IB_ERR_SINGULAR: return "singular Schur matrix";
     case IB_ERR_CG_MAXITER: return "Schur CG iteration cap reached";
     case IB_ERR_UNSUPPORTED: return "unsupported";
+    case IB_ERR_TIMEOUT: return "device pipeline wait timed out";
     default: return "unknown status";
   }
 }
@@ -1218,7 +1259,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (!dst_axis_supported(p->nx) || !dst_axis_supported(p->ny))
     return fail(nullptr, IB_ERR_INVALID,
                 "nx and ny must be multiples of 4, at most 2048, with n/2 a product of 2, 3 and 5");
-  if (p->precision != IB_PREC_FP64 && p->precision != IB_PREC_MIXED)
+  if (p->precision != IB_PREC_FP64 && p->precision != IB_PREC_MIXED && p->precision != IB_PREC_MIXED_TC)
     return fail(nullptr, IB_ERR_UNSUPPORTED, "precision mode not available");
   if (p->motion != IB_MOTION_STATIC && p->motion != IB_MOTION_PRESCRIBED)
     return fail(nullptr, IB_ERR_INVALID, "unknown body motion");
@@ -1262,7 +1303,11 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   h->nbodies = p->nbodies;
   h->nb = nb;
   h->nf = 2 * nb;
-  h->precision = p->precision;
+  // IB_PREC_MIXED_TC is the mixed-precision solve with the tensor-core transform passes
+  h->precision = p->precision == IB_PREC_FP64 ? IB_PREC_FP64 : IB_PREC_MIXED;
+  const bool want_tc = p->precision == IB_PREC_MIXED_TC;
+  if (want_tc && !(sgemm_axis_supported(p->nx) && sgemm_axis_supported(p->ny)))
+    return bail(fail(h, IB_ERR_UNSUPPORTED, "tensor-core transforms need both axes a multiple of 128 cells"));
   h->motion = p->motion;
   h->hist_cap = p->history_capacity > 0 ? p->history_capacity : 4096;
   if (p->refine_sweeps < 0 || p->refine_sweeps > 2) return bail(fail(h, IB_ERR_INVALID, "refine_sweeps must be 0, 1 or 2"));
@@ -1287,6 +1332,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   // IBGB300_DST=warp|stockham overrides the choice for both precisions.
   const bool wsup = wdst_axis_supported(p->nx) && wdst_axis_supported(p->ny);
   h->wdst = wsup && (p->precision == IB_PREC_MIXED || std::max(p->nx, p->ny) >= 2048);
+  h->gdst = want_tc;
   if (const char* env = std::getenv("IBGB300_DST")) {
     if (std::strcmp(env, "stockham") == 0) h->wdst = false;
     if (std::strcmp(env, "warp") == 0) h->wdst = wsup;
@@ -1299,6 +1345,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (h->precision == IB_PREC_MIXED) {
     if ((e = h->axx32.build(g.nx)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "x transform tables", e));
     if ((e = h->axy32.build(g.ny)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "y transform tables", e));
+  }
+  if (h->gdst) {
+    if ((e = h->sgx.build(g.nx)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "x sine-matrix image", e));
+    if ((e = h->sgy.build(g.ny)) != cudaSuccess) return bail(fail(h, IB_ERR_CUDA, "y sine-matrix image", e));
   }
 #define AL(ptr, n)                                                                       \
   do {                                                                                   \
@@ -1319,6 +1369,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   if (h->precision == IB_PREC_MIXED) {
     AL(h->mLap32, nG); AL(h->mCN1_32, L * nG);
     AL(h->w32, L * nG); AL(h->x032, L * nG);
+    if (h->gdst) AL(h->gw32, L * nG);
     if (h->refine >= 2) { AL(h->x132, L * nG); AL(h->r1, L * nG); }
     AL(h->conv, (int64_t)L * (g.nq > nG ? g.nq : nG));
     // Vort2Flux over all levels at once: two refinement sweeps, one-warp line passes on both
@@ -1327,7 +1378,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     // at 512^2 x 4, 1.41 vs 1.47 at 1024^2 x 4 (and C_L/C_D 2e-10 from FP64 instead of 2e-8),
     // but 6.15 vs 5.84 at 2048^2 x 5; so up to 2^20 cells per level.  IBGB300_V2F=levels|
     // sequential overrides the choice.
-    const bool lv_ok = h->wdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    const bool lv_ok = h->wdst && !h->gdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
     h->v2f_ok = lv_ok;
     h->v2f_auto = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);
     h->v2f_levels = h->v2f_auto;
@@ -1719,6 +1770,7 @@ int ib_get_info(ib_handle* h, ib_info* info) {
   info->device_bytes = h->device_bytes;
   info->setup_ms = h->setup_ms;
   info->vort2flux_order = h->v2f_levels ? IB_V2F_LEVELS : IB_V2F_SEQUENTIAL;
+  info->transform_form = h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM);
   return IB_OK;
 }
 
@@ -1814,6 +1866,21 @@ int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out) {
   cudaFree(w);
   CK(e);
   OP_END();
+}
+
+int ib_op_sine_lines_tc(ib_handle* h, int32_t axis, int32_t rows, const float* in, float* out) {
+  OP_BEGIN();
+  if (rows < 1 || axis < 0 || axis > 1 || !in || !out) return IB_ERR_INVALID;
+  const int n = axis == 0 ? g.nx : g.ny;
+  if (!sgemm_axis_supported(n)) return fail(h, IB_ERR_UNSUPPORTED, "tensor-core transforms need a multiple of 128 cells");
+  SineGemm& t = axis == 0 ? h->sgx : h->sgy;
+  if (!t.img) CK(t.build(n));
+  SgIn si{in, n - 1, rows, n - 1};
+  SgOut so{};
+  so.mode = 0; so.out = out; so.ld = n - 1; so.rpb = rows; so.ncols = n - 1;
+  CK(sgemm_pass(t, si, so, h->status, s));
+  CK(cudaStreamSynchronize(s));
+  return check_status(h);
 }
 
 int ib_op_laplacian_inv(ib_handle* h, int32_t batch, const double* b, double* x) {

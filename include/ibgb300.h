@@ -38,12 +38,17 @@ extern "C" {
 #define IB_ERR_SINGULAR 5           /* zero / non-finite pivot while inverting the Schur matrix */
 #define IB_ERR_CG_MAXITER 6         /* Schur CG hit its iteration cap */
 #define IB_ERR_UNSUPPORTED 7        /* feature not available in this build */
+#define IB_ERR_TIMEOUT 8            /* a device-side pipeline wait ran out (the kernel gave up and
+                                       returned; the context stays usable) */
 
 /* arithmetic of the fluid solve (state, nonlinear term, Schur solve and forces are FP64 in
  * every mode) */
 #define IB_PREC_FP64 0   /* every sine transform in FP64 (the reference's arithmetic) */
 #define IB_PREC_MIXED 1  /* FP32 sine transforms refined with float-float residuals (refine_sweeps);
                             state and stencils in float-float (two-float) arithmetic */
+#define IB_PREC_MIXED_TC 2  /* as IB_PREC_MIXED, with every sine transform a BF16x3 split-precision
+                               GEMM against the sine matrix on the tensor cores (FP32 accumulation);
+                               both axes a multiple of 128 cells; Vort2Flux level by level */
 
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */

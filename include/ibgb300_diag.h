@@ -21,7 +21,12 @@ typedef struct ib_info {
   int64_t device_bytes;      /* device memory held by the handle */
   double setup_ms;           /* wall time of ib_create (tables, delta weights, Schur inverse) */
   int32_t vort2flux_order;   /* the order in effect: IB_V2F_LEVELS or IB_V2F_SEQUENTIAL */
+  int32_t transform_form;    /* the sine-transform passes in effect: IB_FORM_* */
 } ib_info;
+
+#define IB_FORM_STOCKHAM 0   /* shared-memory Stockham FFT passes, 64 threads per line */
+#define IB_FORM_WARP 1       /* warp-per-line FFT passes with a transposed intermediate */
+#define IB_FORM_TENSOR 2     /* BF16x3 sine-matrix GEMMs on the tensor cores (tcgen05) */
 
 int ib_get_info(ib_handle* h, ib_info* info);
 

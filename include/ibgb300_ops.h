@@ -21,6 +21,13 @@ extern "C" {
  * DST-I of `batch` (nx-1)x(ny-1) arrays */
 int ib_op_dst2(ib_handle* h, int32_t batch, const double* in, double* out);
 
+/* The 1-D sine transform of the FFTW RODFT00 plan (fluid-ops.jl:24-25, one axis of it) as a
+ * BF16x3 split-precision GEMM on the tensor cores: for each of `rows` FP32 lines of n-1 values
+ * (n = nx for axis 0, ny for axis 1; a multiple of 128), out_k = sum_j in_j sin(pi j k / n),
+ * k = 1..n-1 (half the RODFT00 value).  Relative error ~2^-16 of the row's magnitude; the
+ * mixed-precision solves refine it away.  IB_ERR_UNSUPPORTED for other sizes. */
+int ib_op_sine_lines_tc(ib_handle* h, int32_t axis, int32_t rows, const float* in, float* out);
+
 /* LaplacianInv with lap_eigs (fluid-ops.jl:42-61): x = DST(DST(b) * scale / Λ) */
 int ib_op_laplacian_inv(ib_handle* h, int32_t batch, const double* b, double* x);
 

@@ -36,11 +36,23 @@ def baseline_metric() -> str:
     return METRIC
 
 
-# DRAM bytes (read + write) per array an x pass moves, from one ncu capture of the mixed step
-# (cold cache, the first ten pass launches of the level-by-level step: 9.40 MB per 1024^2 array;
-# summarised under profiles/).  The traffic of an average launch is that times the arrays per
-# launch of the step being timed (array-passes from pass_model over the launches counted).
-MEASURED_TRAFFIC_PER_ARRAY = {"two_body_large/mixed": {"x": 9.40e6}}
+# DRAM bytes (read + write) per launch of each pass class, from an ncu capture of one step of the
+# same workload and precision with the kernel choice the bench runs (dram__bytes_read.sum +
+# dram__bytes_write.sum over every launch of the class in the step, divided by the launches).
+# The summary with the command that made it is under profiles/; its machine-readable lines read
+#   traffic <workload> <precision> <form> <class> <bytes per launch> <launches>
+TRAFFIC_PROFILE = ROOT / "profiles" / "traffic_two_body_large.md"
+
+
+def measured_traffic(workload: str, precision: str, form: str, cls: str):
+    """(bytes per launch, launches captured, source) from the committed capture, or None."""
+    if not TRAFFIC_PROFILE.exists():
+        return None
+    for line in TRAFFIC_PROFILE.read_text().splitlines():
+        f = line.strip().strip("`").split()
+        if len(f) == 7 and f[0] == "traffic" and f[1:5] == [workload, precision, form, cls]:
+            return float(f[5]), int(f[6]), f"{TRAFFIC_PROFILE.relative_to(ROOT)} (ncu, one step, {f[6]} launches)"
+    return None
 
 
 def dist_env():
@@ -251,6 +263,53 @@ def run_ensemble_config(ib, lib, n=96, K=20, W=3, moving=True):
     }
 
 
+def run_precision_table(ib, wl, checkpoints=(100, 1000, 2000)):
+    """Error of the mixed-precision solve against the FP64 GPU path at the given steps, with the
+    sine transforms in FP32 (warp-per-line FFT passes) and as BF16x3 tensor-core GEMMs: relative
+    L2 of the vorticity (circulation) and streamfunction over all levels, and the largest C_D /
+    C_L error of any body over the steps so far (relative to max(1, |C|))."""
+    arms = (("fp64", "fp64", {}), ("fp32", "mixed", {"IBGB300_DST": "warp"}), ("bf16x3", "mixed_tc", {}))
+    res = {}
+    for name, prec, env in arms:
+        old = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            prob = wl.problem()
+            st = ib.initstate(prob)
+            st._gamma[:] = wl.initial_gamma()
+            s = ib.initsolver(prob, st, precision=prec, history_capacity=max(checkpoints) + 8)
+        finally:
+            for k, v in old.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        s.vort2flux(st)
+        done, snaps, t0 = 0, {}, time.perf_counter()
+        for cp in checkpoints:
+            s.advance_n(st, [i * wl.dt for i in range(done, cp)])
+            done = cp
+            cd, cl = s.force_history(cp)
+            snaps[cp] = (st.qty.gamma.copy(), st.qty.psi.copy(), cd, cl)
+        res[name] = (snaps, (time.perf_counter() - t0) / max(checkpoints))
+        s.close()
+
+    def rl2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    table = {}
+    for name in ("fp32", "bf16x3"):
+        rows = {}
+        for cp in checkpoints:
+            g, p, cd, cl = res[name][0][cp]
+            g0, p0, cd0, cl0 = res["fp64"][0][cp]
+            cerr = max(float(np.max(np.abs(cd - cd0) / np.maximum(1.0, np.abs(cd0)))),
+                       float(np.max(np.abs(cl - cl0) / np.maximum(1.0, np.abs(cl0)))))
+            rows[str(cp)] = {"omega_rel_l2": rl2(g, g0), "psi_rel_l2": rl2(p, p0), "cl_cd_err_max": cerr}
+        table[name] = rows
+    return {"workload": describe(wl), "reference_arm": "FP64 GPU path (FP64 sine transforms)",
+            "errors": table, "host_s_per_step": {k: v[1] for k, v in res.items()}}
+
+
 def run_static_config(ib, lib, L, wl, K, W, local, dist):
     arm = run_arm(ib, lib, L, wl, "mixed", K, W, local, dist)
     ref = run_arm(ib, lib, L, wl, "fp64", K, W, local, dist)
@@ -358,14 +417,14 @@ def cpu_reference(ib, wl, nsteps: int, warmup: int):
 # ----------------------------------------------------------------------------------------------
 # algorithmic bytes / flops of the sine-transform passes (per step)
 # ----------------------------------------------------------------------------------------------
-def uses_line_passes(wl, precision: str) -> bool:
-    """The library's kernel choice: line-parallel passes when both axes have 64 P cells
-    (P = 2^k or 3 2^k <= 32), for the mixed path, and for FP64 at 2048-cell axes."""
-    def ok(n):
-        return n % 64 == 0 and (n // 64) in (1, 2, 3, 4, 6, 8, 12, 16, 24, 32)
-    if os.environ.get("IBGB300_DST") in ("warp", "stockham"):
-        return os.environ["IBGB300_DST"] == "warp" and ok(wl.nx) and ok(wl.ny)
-    return ok(wl.nx) and ok(wl.ny) and (precision == "mixed" or max(wl.nx, wl.ny) >= 2048)
+def algorithmic_step_bytes(wl, precision: str) -> float:
+    """Compulsory DRAM bytes of one step: w L (5 nGamma + 2 nq) + 8 nf^2 (read Gamma, q and the
+    previous nonlinear term, write Gamma, q, psi and the new nonlinear term on every level, read
+    the dense Schur inverse once); w = 8 (FP64 values, or float-float pairs)."""
+    nG = (wl.nx - 1) * (wl.ny - 1)
+    nq = (wl.nx + 1) * wl.ny + wl.nx * (wl.ny + 1)
+    nf = 2 * sum(b.npoints() for b in wl.bodies)
+    return 8.0 * wl.nlevels * (5 * nG + 2 * nq) + 8.0 * nf * nf
 
 
 def pass_model(wl, precision: str, levels: bool = False):
@@ -472,6 +531,9 @@ def run_ours(args, rank, world, local):
                 "vort2flux": ("all levels in one batch, rings first (harmonic ring transfer)"
                               if info.vort2flux_order == L.IB_V2F_LEVELS else "level by level (the reference's order)"),
                 "parallelism": "replicas",
+                "transforms": {0: "Stockham FFT passes", 1: "warp-per-line FFT passes",
+                               2: "BF16x3 tensor-core sine GEMMs"}.get(int(info.transform_form)),
+                "autotune": arm["solver"].autotune(),
                 "device_bytes": int(info.device_bytes),
                 "setup_s": info.setup_ms / 1e3, "host_wall_ms_per_step": arm["host_s"] / K * 1e3},
         "gpu_launches": int(info.kernels_per_step) * K,
@@ -498,7 +560,7 @@ def run_ours(args, rank, world, local):
         prof[key] = (tot.value, nl.value)
     dom = max(prof, key=lambda k: prof[k][0])
     tot_ms, nlaunch = prof[dom]
-    b_step, f_step, arrays_step = model[dom]
+    b_step, f_step, _ = model[dom]
     per_launch_s = tot_ms / 1e3 / nlaunch
     launches_per_step = nlaunch / npf
     bytes_per_launch = b_step / launches_per_step
@@ -508,19 +570,28 @@ def run_ours(args, rank, world, local):
     fp64, fp32 = C.c_double(), C.c_double()
     lib.ib_measure_fp_peaks(local, C.byref(fp64), C.byref(fp32))
     achieved = bytes_per_launch / per_launch_s / 1e9
-    per_array = MEASURED_TRAFFIC_PER_ARRAY.get(f"{args.workload}/{prec}", {}).get(dom)
-    traffic = per_array * arrays_step / launches_per_step if per_array else None
+    form = {0: "stockham", 1: "warp", 2: "tensor"}.get(int(info.transform_form), "stockham")
+    v2f = "levels" if info.vort2flux_order == L.IB_V2F_LEVELS else "sequential"
+    meas = measured_traffic(args.workload, prec, f"{form}/{v2f}", dom)
+    traffic = meas[0] if meas else None
     pipe_peak = fp64.value if prec == "fp64" else fp32.value
+    step_bytes = algorithmic_step_bytes(wl, prec)
     out["roofline"] = {
-        "kernel": ({"x": "k_wxf/k_wxi (x-direction sine passes, one warp per line)",
-                    "y": "k_wy (y-direction sine passes + spectral op, one warp per column)"}
-                   if uses_line_passes(wl, prec) else
-                   {"x": "k_xpass (x-direction sine pass)", "y": "k_ypass (y-direction sine pass + spectral op)"})[dom],
+        "kernel": {"warp": {"x": "k_wxf/k_wxi (x-direction sine passes, one warp per line)",
+                            "y": "k_wy (y-direction sine passes + spectral op, one warp per column)"},
+                   "stockham": {"x": "k_xpass (x-direction sine pass)",
+                                "y": "k_ypass (y-direction sine pass + spectral op)"},
+                   "tensor": {"x": "k_gpro + k_sgemm (x-direction BF16x3 sine GEMMs)",
+                              "y": "k_sgemm (y-direction BF16x3 sine GEMMs)"}}[form][dom],
         "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s",
         "traffic": traffic, "algorithmic_bytes_per_launch": bytes_per_launch,
-        "traffic_source": ("ncu dram__bytes_read+write per x-pass array (9.40 MB, level-by-level step, cold "
-                           "cache) x arrays per launch of this step" if per_array else None),
+        "traffic_source": meas[2] if meas else None,
+        "traffic_frac": (traffic / per_launch_s / 1e9 / hbm) if traffic else None,
+        "step": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms_per_step / 1e3) / 1e9,
+                 "frac": step_bytes / (ms_per_step / 1e3) / 1e9 / hbm,
+                 "note": "w L (5 nGamma + 2 nq) + 8 nf^2 per step (w = 8 bytes per value: FP64, or a "
+                         "float-float pair) over the device time of a step"},
         "avg_launch_ms": per_launch_s * 1e3, "launches_profiled": nlaunch,
         "share_of_step": tot_ms / npf / ms_per_step,
         "fp_pipe": {"pipe": "fp64" if prec == "fp64" else "fp32",
@@ -607,16 +678,26 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the per-configuration summaries (2048^2 four cylinders, moving plate)")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"],
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "mixed_tc"],
                     help="arithmetic of the timed arm (mixed: FP32 transforms + FP64 residual refinement)")
     ap.add_argument("--no-fp64-arm", action="store_true", help="skip timing the FP64 GPU path beside it")
     ap.add_argument("--refine-sweeps", type=int, default=0,
                     help="mixed precision: residual sweeps per solve (0: default policy, 1 or 2 everywhere)")
+    ap.add_argument("--precision-table", action="store_true",
+                    help="print the FP64 / FP32 / BF16x3 error table of the 2048^2 four-cylinder workload "
+                         "at steps 100, 1000 and 2000 and exit")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl != "reference" else args.warmup
     rank, world, local = dist_env()
+    if args.precision_table:
+        import __graft_entry__ as ge
+        ib = ge.package()
+        ge.build()
+        ib.load_library()
+        print(json.dumps(run_precision_table(ib, make_workload(ib, "four_cylinders"))), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, local)
     else:

@@ -476,6 +476,20 @@ class Solver:
             _lib.dptr(st._nonlin[0]), _lib.dptr(st._nonlin[1]),
             _lib.dptr(st._fb) if st._fb.size else None, C.byref(t)))
 
+    _FORMS = ("stockham", "warp", "tensor")
+
+    def autotune(self) -> dict:
+        """The setup-time autotuner's measurements: device ms of its timed unit per candidate
+        ``"<form>/<order>"`` (form: stockham, warp or tensor; order: levels or sequential) and
+        the candidate in effect (``None`` if the tuner did not run)."""
+        ms = np.zeros(6)
+        ch = C.c_int32()
+        self._check(self.lib.ib_get_autotune(self.handle, _lib.dptr(ms), C.byref(ch)))
+        out = {f"{self._FORMS[i // 2]}/{'levels' if i % 2 else 'sequential'}": float(ms[i])
+               for i in range(6) if ms[i] > 0}
+        c = ch.value
+        return {"ms": out, "chosen": None if c < 0 else f"{self._FORMS[c // 2]}/{'levels' if c % 2 else 'sequential'}"}
+
     def stress(self):
         nbd = max(self.nbodies, 1)
         cd = np.zeros(nbd)

@@ -27,7 +27,10 @@ namespace ib {
 namespace wdst {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kLines = 4;  // lines per block
+#ifndef IB_WDST_LINES
+#define IB_WDST_LINES 4
+#endif
+constexpr int kLines = IB_WDST_LINES;  // lines per block
 
 // (lanes per line, values per lane) pairs with compiled passes: one warp per line, or two
 // (IBGB300_LINE_LANES=64, axes with M = 64 P, P = 2..16)

@@ -12,9 +12,10 @@
 // accuracy, as they do for the FP32 FFT passes.
 //
 // Kernel (one CTA = 128 lines x BN outputs, K = n in chunks of 64, two smem stages):
-//   * all 8 warps load the chunk's line values (FP32, any row stride), split them into BF16
-//     hi / lo and store them in the 128-byte-swizzled K-major layout the MMA reads
-//     (8-row x 128-byte atoms, 16-byte units XOR-ed with the row in the atom);
+//   * all 8 warps load the chunk's line values (FP32, any row stride; one chunk ahead, so the
+//     loads are in flight while the previous chunk's MMAs run), split them into BF16 hi / lo
+//     and store them in the 128-byte-swizzled K-major layout the MMA reads (8-row x 128-byte
+//     atoms, 16-byte units XOR-ed with the row in the atom);
 //   * the sine operand is stored in global memory already in that tile image, per
 //     (N tile, K chunk, part), and one thread brings each 32 KB part in with one bulk copy
 //     (cp.async.bulk, completion counted on an mbarrier);
@@ -183,6 +184,20 @@ k_sgemm(SgIn in, SgOut o, const uint16_t* __restrict__ img, int n, int* __restri
   // thread 0's record of asynchronous work in flight, for a bounded drain after a timeout
   int issued_b[kStages] = {0, 0}, waited_b[kStages] = {0, 0}, committed[kStages] = {0, 0}, drained[kStages] = {0, 0};
   bool bad = false;
+  // line values of one K chunk: warp w owns rows 16 w .. 16 w + 15, lane l the K pair (2l, 2l+1)
+  float va[16], vb[16];
+  auto load_chunk = [&](int cc) {
+    const int j0 = cc * BK + 2 * lane;  // K index of the pair's first element (input j0 - 1)
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int r = m0 + warp * 16 + i;
+      const float* row = in.a + (int64_t)r * in.lda;
+      const bool ok = r < in.rows;
+      va[i] = (ok && j0 >= 1 && j0 <= in.klen) ? row[j0 - 1] : 0.0f;
+      vb[i] = (ok && j0 + 1 <= in.klen) ? row[j0] : 0.0f;
+    }
+  };
+  load_chunk(0);
   int c = 0;
   for (; c < nkc; ++c) {
     const int s = c & 1;
@@ -204,30 +219,20 @@ k_sgemm(SgIn in, SgOut o, const uint16_t* __restrict__ img, int n, int* __restri
       bulk_g2s(B_lo, src + BN * BK, TL::kB, &full[s]);
       issued_b[s]++;
     }
-    // the chunk's line values: warp w owns rows 16 w .. 16 w + 15, lane l the K pair (2l, 2l+1)
-    {
-      const int j0 = c * BK + 2 * lane;  // K index of the pair's first element (input j0 - 1)
-      float va[16], vb[16];
+    // the chunk's line values (loaded during the previous chunk) into the swizzled tiles, then
+    // the next chunk's values into registers, in flight while this chunk's MMAs run
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int r = m0 + warp * 16 + i;
-        const float* row = in.a + (int64_t)r * in.lda;
-        const bool ok = r < in.rows;
-        va[i] = (ok && j0 >= 1 && j0 <= in.klen) ? row[j0 - 1] : 0.0f;
-        vb[i] = (ok && j0 + 1 <= in.klen) ? row[j0] : 0.0f;
-      }
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int rr = warp * 16 + i;
-        uint32_t lo;
-        const uint32_t hi = split_pair(va[i], vb[i], lo);
-        const uint32_t off = sw128_off(rr, lane);
-        *reinterpret_cast<uint32_t*>(A_hi + off) = hi;
-        *reinterpret_cast<uint32_t*>(A_lo + off) = lo;
-      }
+    for (int i = 0; i < 16; ++i) {
+      const int rr = warp * 16 + i;
+      uint32_t lo;
+      const uint32_t hi = split_pair(va[i], vb[i], lo);
+      const uint32_t off = sw128_off(rr, lane);
+      *reinterpret_cast<uint32_t*>(A_hi + off) = hi;
+      *reinterpret_cast<uint32_t*>(A_lo + off) = lo;
     }
     fence_async_smem();
     __syncthreads();
+    if (c + 1 < nkc) load_chunk(c + 1);
     if (tid == 0) {
       if (!mbar_wait(&full[s], u & 1)) {
         bad = true;
@@ -270,7 +275,8 @@ k_sgemm(SgIn in, SgOut o, const uint16_t* __restrict__ img, int n, int* __restri
   }
   tc_fence_after();
   // epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (tile rows), columns of half w >> 2
-  {
+  if (MODE == 1) {
+    // transposed store: the 32 lanes (consecutive rows) write consecutive addresses
     const int q = warp & 3, half = warp >> 2;
     const int r = m0 + 32 * q + lane;
     const bool rok = r < in.rows;
@@ -286,15 +292,44 @@ k_sgemm(SgIn in, SgOut o, const uint16_t* __restrict__ img, int n, int* __restri
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int cidx = cbase + i;
-        if (cidx < 1 || cidx > o.ncols) continue;
-        float x = v[i];
+        if (cidx >= 1 && cidx <= o.ncols)
+          static_cast<float*>(o.out)[slot * o.bstride + (int64_t)(cidx - 1) * o.ld + rr] = v[i];
+      }
+    }
+  } else {
+    // row-major results: the tile goes through shared memory (the operand stages are free now;
+    // row stride BN + 1 words, so a warp's 32 rows fall in 32 banks), then every warp stores
+    // whole rows, 32 consecutive columns per instruction
+    float* tile = reinterpret_cast<float*>(sm);
+    constexpr int TS = BN + 1;
+    {
+      const int q = warp & 3, half = warp >> 2;
+      const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16);
+      float* trow = tile + (32 * q + lane) * TS;
+#pragma unroll 1
+      for (int cc = 0; cc < BN / 2; cc += 16) {
+        const int col0 = half * (BN / 2) + cc;
+        float v[16];
+        tmem_ld16(tb + (uint32_t)col0, v);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) trow[col0 + i] = v[i];
+      }
+    }
+    __syncthreads();
+    const int c_lo = max(1, nt * BN), c_hi = min(o.ncols, nt * BN + BN - 1);  // output indices c
+#pragma unroll 1
+    for (int rr0 = warp; rr0 < BM; rr0 += kThreads / 32) {
+      const int r = m0 + rr0;
+      if (r >= in.rows) break;
+      const float* trow = tile + rr0 * TS - nt * BN;  // indexed by c
+      const int slot = r / o.rpb, rr = r - slot * o.rpb;
+      for (int cidx = c_lo + lane; cidx <= c_hi; cidx += 32) {
+        const float x = trow[cidx];
+        const int64_t e = (int64_t)r * o.ld + (cidx - 1);
         if (MODE == 0) {
-          if (o.mult) x *= __ldg(&o.mult[slot * o.mstride + (int64_t)rr * o.ld + (cidx - 1)]);
-          static_cast<float*>(o.out)[(int64_t)r * o.ld + (cidx - 1)] = x;
-        } else if (MODE == 1) {
-          static_cast<float*>(o.out)[slot * o.bstride + (int64_t)(cidx - 1) * o.ld + rr] = x;
+          const float m = o.mult ? __ldg(&o.mult[slot * o.mstride + (int64_t)rr * o.ld + (cidx - 1)]) : 1.0f;
+          static_cast<float*>(o.out)[e] = o.mult ? x * m : x;
         } else {
-          const int64_t e = (int64_t)r * o.ld + (cidx - 1);
           df64 xv = o.base ? two_sum(o.base[e], o.base2 ? o.base2[e] : 0.0f) : df64(0.0f);
           xv = two_sum(xv.hi, xv.lo + x);
           df64* dst = static_cast<df64*>(o.out);

@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -127,6 +128,10 @@ struct ib_handle {
   bool v2f_levels = false;
   bool v2f_ok = false, v2f_auto = false;  // the grid allows it / the size rule picks it
   RingPlan rplan;
+  // setup-time autotuner: modelled step time of each candidate (form * 2 + levels order), ms;
+  // -1 where not tried
+  double tune_ms[6] = {-1, -1, -1, -1, -1, -1};
+  bool tuned = false;
   double pc_excess_iters = 0.0;                   // iterations above the base since then
   double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
   double *Gw = nullptr, *Pw = nullptr, *qw = nullptr, *rings_w = nullptr;
@@ -1192,6 +1197,198 @@ int moving_step_mode(ib_handle* h, double t, double u, double v, const double* k
   return graph ? moving_step_graph<double>(h, t, u, v, kin) : moving_step<double>(h, t, u, v, kin);
 }
 
+// ---- setup-time autotuner ---------------------------------------------------------------------
+// Chooses, by timing on this GPU, the transform form of the solves (Stockham FFT passes, warp-per-
+// line FFT passes, or BF16x3 tensor-core GEMMs for mixed precision) and, for mixed precision on
+// warp passes, the Vort2Flux order (all levels in one batch, or level by level).  The timed unit
+// is the transform work a step repeats: the batched Crank-Nicolson solve over all levels, a
+// projection-size solve, a full Vort2Flux and a level-1-only Vort2Flux, run on scratch arrays
+// (the state is not touched); the stencil, body and Schur kernels are the same for every
+// candidate.  Each candidate runs once to warm up, then three times; the fastest run counts.
+// IBGB300_DST / IBGB300_V2F pin a choice, IBGB300_AUTOTUNE=0 keeps the fixed size rules.
+template <typename S>
+cudaError_t tune_unit(ib_handle* h, double* gam, double* psi, double* q, double* q1, double* rings, double* in,
+                      double* out) {
+  const int L = h->g.nlev;
+  CE(solve(h, view<S>(in), view<S>(out), L, nullptr, op_cn_all(h), nullptr));
+  CE(solve(h, view<S>(in), view<S>(out), 1, nullptr, op_cn1(h), view<S>(out)));
+  CE(vort2flux<S>(h, view<S>(gam), view<S>(psi), view<S>(q), nullptr, view<S>(rings)));
+  return vort2flux<S>(h, view<S>(gam), view<S>(psi), nullptr, view<S>(q1), view<S>(rings));
+}
+
+double tune_time(ib_handle* h, double* gam, double* psi, double* q, double* q1, double* rings, double* in, double* out) {
+  cudaStream_t s = h->stream;
+  auto run = [&]() {
+    return h->precision == IB_PREC_MIXED ? tune_unit<df64>(h, gam, psi, q, q1, rings, in, out)
+                                         : tune_unit<double>(h, gam, psi, q, q1, rings, in, out);
+  };
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1.0;
+  double best = -1.0;
+  bool ok = run() == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+  for (int r = 0; ok && r < 3; ++r) {
+    float ms = 0.0f;
+    ok = cudaEventRecord(e0, s) == cudaSuccess && run() == cudaSuccess && cudaEventRecord(e1, s) == cudaSuccess &&
+         cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
+    if (ok && (best < 0 || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (!ok) {
+    cudaGetLastError();  // a candidate that cannot run is skipped
+    cudaStreamSynchronize(s);
+    return -1.0;
+  }
+  return best;
+}
+
+// Decisions are kept per process for each (device, grid, levels, sweeps, what is tuned), so every
+// handle of one shape in a process (an ensemble member and the same problem stepped alone, say)
+// takes the same choice and gives the same bits.
+struct TuneRecord {
+  double ms[6];
+  int best;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneRecord> g_tune_cache;
+
+int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
+  const Geometry& g = h->g;
+  const int L = g.nlev;
+  char keybuf[160];
+  std::snprintf(keybuf, sizeof(keybuf), "%d/%d/%d/%d/%d/%d/%d/%d/%d/%d", h->device, g.nx, g.ny, L, h->precision, h->refine,
+                (int)tune_form, (int)tune_v2f, (int)h->wdst, (int)h->gdst);
+  const std::string key(keybuf);
+  std::lock_guard<std::mutex> tune_lock(g_tune_mu);
+  const auto hit = g_tune_cache.find(key);
+  const bool mixed = h->precision == IB_PREC_MIXED;
+  const bool wsup = wdst_axis_supported(g.nx) && wdst_axis_supported(g.ny);
+  const bool tsup = mixed && sgemm_axis_supported(g.nx) && sgemm_axis_supported(g.ny);
+  std::vector<void*> tmp;
+  const bool timing = hit == g_tune_cache.end();
+  auto scratch = [&](size_t n) -> double* {
+    if (!timing) return reinterpret_cast<double*>(16);  // unused: the choice is known
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(double) * (n > 0 ? n : 1)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, sizeof(double) * (n > 0 ? n : 1));
+    tmp.push_back(p);
+    return static_cast<double*>(p);
+  };
+  const int64_t nG = g.nG;
+  double* gam = scratch(L * nG);
+  double* psi = scratch(L * nG);
+  double* q = scratch((int64_t)L * g.nq);
+  double* q1 = scratch(g.nq);
+  double* rings = scratch((int64_t)L * g.nbc);
+  double* in = scratch(L * nG);
+  double* out = scratch(L * nG);
+  auto release = [&]() {
+    for (void* p : tmp) cudaFree(p);
+  };
+  if (!gam || !psi || !q || !q1 || !rings || !in || !out) {
+    release();
+    return fail(h, IB_ERR_CUDA, "autotuner scratch allocation");
+  }
+  const bool wdst0 = h->wdst, gdst0 = h->gdst, lv0 = h->v2f_levels;
+  struct Cand { int form; bool levels; };
+  std::vector<Cand> cands;
+  std::vector<int> forms;
+  if (tune_form) {
+    forms.push_back(IB_FORM_STOCKHAM);
+    if (wsup) forms.push_back(IB_FORM_WARP);
+    if (tsup) forms.push_back(IB_FORM_TENSOR);
+  } else {
+    forms.push_back(h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM));
+  }
+  for (int f : forms) {
+    const bool lv_ok = mixed && lv_base && f == IB_FORM_WARP;
+    if (tune_v2f) {
+      cands.push_back({f, false});
+      if (lv_ok) cands.push_back({f, true});
+    } else {
+      cands.push_back({f, lv0 && lv_ok});
+    }
+  }
+  bool need_tc = false, need_lv = false;
+  if (hit != g_tune_cache.end()) {
+    need_tc = hit->second.best / 2 == IB_FORM_TENSOR;
+    need_lv = (hit->second.best & 1) != 0;
+  } else {
+    for (const Cand& c : cands) {
+      need_tc |= c.form == IB_FORM_TENSOR;
+      need_lv |= c.levels;
+    }
+  }
+  cudaError_t e;
+  const bool tc_own = need_tc && !h->gw32;  // the tensor-core resources are the tuner's to keep or free
+  if (tc_own) {
+    if ((e = h->sgx.build(g.nx)) != cudaSuccess || (e = h->sgy.build(g.ny)) != cudaSuccess) {
+      release();
+      return fail(h, IB_ERR_CUDA, "sine-matrix image", e);
+    }
+    void* p = nullptr;
+    if ((e = cudaMalloc(&p, sizeof(float) * L * nG)) != cudaSuccess) {
+      release();
+      return fail(h, IB_ERR_CUDA, "autotuner work allocation", e);
+    }
+    h->gw32 = static_cast<float*>(p);
+  }
+  if (need_lv && !h->rplan.St) {
+    if ((e = h->rplan.build(g)) != cudaSuccess) {
+      release();
+      return fail(h, IB_ERR_CUDA, "ring transfer tables", e);
+    }
+  }
+  int best = -1;
+  double best_ms = -1.0;
+  if (hit != g_tune_cache.end()) {
+    best = hit->second.best;
+    for (int i = 0; i < 6; ++i) h->tune_ms[i] = hit->second.ms[i];
+  } else {
+    for (const Cand& c : cands) {
+      h->wdst = c.form == IB_FORM_WARP;
+      h->gdst = c.form == IB_FORM_TENSOR;
+      h->v2f_levels = c.levels;
+      const double ms = tune_time(h, gam, psi, q, q1, rings, in, out);
+      const int idx = c.form * 2 + (c.levels ? 1 : 0);
+      h->tune_ms[idx] = ms;
+      if (ms > 0 && (best < 0 || ms < best_ms)) {
+        best = idx;
+        best_ms = ms;
+      }
+    }
+    if (best >= 0) {
+      TuneRecord rec;
+      for (int i = 0; i < 6; ++i) rec.ms[i] = h->tune_ms[i];
+      rec.best = best;
+      g_tune_cache[key] = rec;
+    }
+  }
+  release();
+  if (best < 0) {
+    h->wdst = wdst0;
+    h->gdst = gdst0;
+    h->v2f_levels = lv0;
+  } else {
+    h->wdst = best / 2 == IB_FORM_WARP;
+    h->gdst = best / 2 == IB_FORM_TENSOR;
+    h->v2f_levels = (best & 1) != 0;
+  }
+  // keep what the choice uses: the tensor-core tables and work array, the ring-transfer plan
+  if (tc_own && !h->gdst) {
+    cudaFree(h->gw32);
+    h->gw32 = nullptr;
+    h->sgx.release();
+    h->sgy.release();
+  } else if (tc_own) {
+    h->allocs.push_back(h->gw32);
+    h->device_bytes += (int64_t)sizeof(float) * L * nG;
+  }
+  if (!h->v2f_levels && h->rplan.St) h->rplan.release();
+  h->tuned = best >= 0;
+  return cudaGetLastError() == cudaSuccess ? IB_OK : fail(h, IB_ERR_CUDA, "autotuner");
+}
+
 int one_step(ib_handle* h, double t, double u, double v) {
   if (h->motion == IB_MOTION_PRESCRIBED) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics (ib_advance_kin)");
   int rc = stage_q0(h, u, v);
@@ -1333,10 +1530,14 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   const bool wsup = wdst_axis_supported(p->nx) && wdst_axis_supported(p->ny);
   h->wdst = wsup && (p->precision == IB_PREC_MIXED || std::max(p->nx, p->ny) >= 2048);
   h->gdst = want_tc;
+  bool pin_form = want_tc, pin_v2f = false;
   if (const char* env = std::getenv("IBGB300_DST")) {
-    if (std::strcmp(env, "stockham") == 0) h->wdst = false;
-    if (std::strcmp(env, "warp") == 0) h->wdst = wsup;
+    if (std::strcmp(env, "stockham") == 0) { h->wdst = false; pin_form = true; }
+    if (std::strcmp(env, "warp") == 0) { h->wdst = wsup; pin_form = true; }
   }
+  // the setup-time autotuner (autotune() above) replaces these size rules unless switched off
+  const char* tune_env = std::getenv("IBGB300_AUTOTUNE");
+  const bool autotune_on = !(tune_env && tune_env[0] == '0');
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t nG = g.nG;
@@ -1378,15 +1579,16 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     // at 512^2 x 4, 1.41 vs 1.47 at 1024^2 x 4 (and C_L/C_D 2e-10 from FP64 instead of 2e-8),
     // but 6.15 vs 5.84 at 2048^2 x 5; so up to 2^20 cells per level.  IBGB300_V2F=levels|
     // sequential overrides the choice.
-    const bool lv_ok = h->wdst && !h->gdst && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    const bool lv_base = wsup && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    const bool lv_ok = lv_base && h->wdst && !h->gdst;
     h->v2f_ok = lv_ok;
     h->v2f_auto = lv_ok && (int64_t)g.nx * g.ny <= (int64_t(1) << 20);
     h->v2f_levels = h->v2f_auto;
     if (const char* env = std::getenv("IBGB300_V2F")) {
-      if (std::strcmp(env, "sequential") == 0) h->v2f_levels = false;
-      if (std::strcmp(env, "levels") == 0) h->v2f_levels = lv_ok;
+      if (std::strcmp(env, "sequential") == 0) { h->v2f_levels = false; pin_v2f = true; }
+      if (std::strcmp(env, "levels") == 0) { h->v2f_levels = lv_ok; pin_v2f = true; }
     }
-    if (h->v2f_levels && (e = h->rplan.build(g)) != cudaSuccess)
+    if (h->v2f_levels && !autotune_on && (e = h->rplan.build(g)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));
   }
   AL(h->status, 4); AL(h->d_counter, 1);
@@ -1422,6 +1624,25 @@ int ib_create(const ib_problem* p, ib_handle** out) {
       if ((e = cudaMemcpy(h->mLap32, l32.data(), sizeof(float) * l32.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
           (e = cudaMemcpy(h->mCN1_32, c32.data(), sizeof(float) * c32.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
         return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    }
+  }
+  {
+    const bool mixed = h->precision == IB_PREC_MIXED;
+    const bool lv_base = mixed && wsup && L > 1 && h->refine >= 2 && h->axx32.d.wNL == 32 && h->axy32.d.wNL == 32;
+    // mixed precision only: the FP64 path keeps its fixed, measured kernel rule, so that its
+    // results are the same bits from run to run
+    const bool tune_form = mixed && autotune_on && !pin_form;
+    const bool tune_v2f = mixed && autotune_on && !pin_v2f && lv_base;
+    if (tune_form || tune_v2f) {
+      int rc = autotune(h, tune_form, tune_v2f, lv_base);
+      if (rc != IB_OK) return bail(rc);
+    } else if (mixed && h->v2f_levels && !h->rplan.St && (e = h->rplan.build(g)) != cudaSuccess) {
+      return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));
+    }
+    if (mixed) {
+      h->v2f_ok = lv_base && h->wdst && !h->gdst;
+      if (h->tuned) h->v2f_auto = h->v2f_levels;
+      else h->v2f_auto = h->v2f_auto && h->v2f_ok;
     }
   }
   if (nb > 0) {
@@ -1771,6 +1992,16 @@ int ib_get_info(ib_handle* h, ib_info* info) {
   info->setup_ms = h->setup_ms;
   info->vort2flux_order = h->v2f_levels ? IB_V2F_LEVELS : IB_V2F_SEQUENTIAL;
   info->transform_form = h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM);
+  return IB_OK;
+}
+
+int ib_get_autotune(ib_handle* h, double* ms, int32_t* chosen) {
+  if (!h) return IB_ERR_INVALID;
+  if (ms)
+    for (int i = 0; i < 6; ++i) ms[i] = h->tune_ms[i];
+  if (chosen)
+    *chosen = h->tuned ? (h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 + (h->v2f_levels ? 1 : 0)
+                       : -1;
   return IB_OK;
 }
 

@@ -22,7 +22,7 @@ using wdst::line_dst;
 using wdst::line_sync;
 
 template <typename T, typename Tin, int P, int NL, int PRO, bool kBC>
-__global__ void __launch_bounds__(kLines * NL)
+__global__ void __launch_bounds__(kLines * NL, IB_WDST_XMINB)
 k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
   // exact arithmetic of the prologue: FP64, or float-float when the input is float-float
   using A = typename std::conditional<is_df64<Tin>::value, df64, double>::type;
@@ -211,7 +211,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
 }
 
 template <typename T, typename Tout, int P, int NL, int EPI>
-__global__ void __launch_bounds__(kLines * NL)
+__global__ void __launch_bounds__(kLines * NL, IB_WDST_XMINB)
 k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
   using A = typename std::conditional<is_df64<Tout>::value, df64, double>::type;
   using Sh = Shape<T, P, NL>;

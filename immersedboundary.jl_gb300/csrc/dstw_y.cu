@@ -13,7 +13,7 @@ using wdst::line_dst;
 using wdst::line_sync;
 
 template <typename T, int P, int NL, SpecOp OP>
-__global__ void __launch_bounds__(kLines * NL)
+__global__ void __launch_bounds__(kLines * NL, IB_WDST_YMINB)
 k_wy(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
   using Sh = Shape<T, P, NL>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

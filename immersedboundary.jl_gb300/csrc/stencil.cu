@@ -16,6 +16,17 @@ inline int blocks_for(int64_t n) {
   return (int)(b < 1 ? 1 : b);
 }
 
+// x * s for a power of two s: exact, so a float-float value scales part by part (the general
+// float-float product would spend ~7 FP32 operations on it)
+template <typename T>
+__device__ __forceinline__ T xscale(T x, float s) {
+  return x * T(s);
+}
+template <>
+__device__ __forceinline__ df64 xscale<df64>(df64 x, float s) {
+  return df64(x.hi * s, x.lo * s);
+}
+
 // get_bc! value at ring index idx (fluid-ops.jl:210-239), including the final *0.25.
 template <typename T>
 __device__ __forceinline__ T ring_value(const Geometry& g, const T* __restrict__ r, int idx) {
@@ -31,7 +42,7 @@ __device__ __forceinline__ T ring_value(const Geometry& g, const T* __restrict__
       v = r[(ny4 - 1 + t) * ncol + col];
     } else {
       const int t = (jb + 1) >> 1;
-      v = T(0.5) * (r[(ny4 - 1 + t) * ncol + col] + r[(ny4 - 2 + t) * ncol + col]);
+      v = xscale(r[(ny4 - 1 + t) * ncol + col] + r[(ny4 - 2 + t) * ncol + col], 0.5f);
     }
   } else {  // bottom (idx < T) or top block, node along x
     const bool top = idx >= g.T;
@@ -42,10 +53,10 @@ __device__ __forceinline__ T ring_value(const Geometry& g, const T* __restrict__
       v = r[row * ncol + nx4 - 1 + t];
     } else {
       const int t = (ib + 1) >> 1;
-      v = T(0.5) * (r[row * ncol + nx4 - 1 + t] + r[row * ncol + nx4 - 2 + t]);
+      v = xscale(r[row * ncol + nx4 - 1 + t] + r[row * ncol + nx4 - 2 + t], 0.5f);
     }
   }
-  return v * T(0.25);
+  return xscale(v, 0.25f);
 }
 
 template <typename T>
@@ -98,8 +109,8 @@ __global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__
     const int J = 2 * s + 1, I = 2 * tt + 1;
     const int c = J * ncol + I;
     const T v = f[c]
-                + T(0.5) * (f[c + 1] + f[c + ncol] + f[c - 1] + f[c - ncol])
-                + T(0.25) * (f[c + ncol + 1] + f[c - ncol + 1] + f[c - ncol - 1] + f[c + ncol - 1]);
+                + xscale(f[c + 1] + f[c + ncol] + f[c - 1] + f[c - ncol], 0.5f)
+                + xscale(f[c + ncol + 1] + f[c - ncol + 1] + f[c - ncol - 1] + f[c + ncol - 1], 0.25f);
     gc[(int64_t)b * stride + (int64_t)(g.ny / 4 + s) * ncol + g.nx / 4 + tt] = v;
   }
 }
@@ -160,10 +171,10 @@ struct LevelView {
   int nx, ny, ncol;
   // avg_flux!: Qx at (Jq in 1..ny-1, Iq in 0..nx), Qy at (Jq in 0..ny, Iq in 1..nx-1)
   __device__ __forceinline__ T Qx(int Jq, int Iq) const {
-    return (((qx[Jq * (nx + 1) + Iq] + qx[(Jq - 1) * (nx + 1) + Iq]) + q0x) + q0x) * T(0.5);
+    return xscale((((qx[Jq * (nx + 1) + Iq] + qx[(Jq - 1) * (nx + 1) + Iq]) + q0x) + q0x), 0.5f);
   }
   __device__ __forceinline__ T Qy(int Jq, int Iq) const {
-    return (((qy[Jq * nx + Iq] + qy[Jq * nx + Iq - 1]) + q0y) + q0y) * T(0.5);
+    return xscale((((qy[Jq * nx + Iq] + qy[Jq * nx + Iq - 1]) + q0y) + q0y), 0.5f);
   }
   __device__ __forceinline__ T Gm(int J, int I) const { return G[J * ncol + I]; }
 };
@@ -171,16 +182,16 @@ struct LevelView {
 // fqx at (Jf, If), If in 1..nx-1 (direct_product_loops!, fluid-ops.jl:329-362)
 template <typename T>
 __device__ __forceinline__ T fqx_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qyHi, T qyLo) {
-  if (Jf == 0) return (qyHi * v.Gm(0, If - 1) + qyLo * v.bc[g.B + If]) * T(0.5);
-  if (Jf == v.ny - 1) return (qyLo * v.Gm(v.ny - 2, If - 1) + qyHi * v.bc[g.T + If]) * T(0.5);
-  return (qyHi * v.Gm(Jf, If - 1) + qyLo * v.Gm(Jf - 1, If - 1)) * T(0.5);
+  if (Jf == 0) return xscale(qyHi * v.Gm(0, If - 1) + qyLo * v.bc[g.B + If], 0.5f);
+  if (Jf == v.ny - 1) return xscale(qyLo * v.Gm(v.ny - 2, If - 1) + qyHi * v.bc[g.T + If], 0.5f);
+  return xscale(qyHi * v.Gm(Jf, If - 1) + qyLo * v.Gm(Jf - 1, If - 1), 0.5f);
 }
 // fqy at (Jf, If), Jf in 1..ny-1 (fluid-ops.jl:365-398); qxHi = Qx(Jf, If+1), qxLo = Qx(Jf, If)
 template <typename T>
 __device__ __forceinline__ T fqy_at(const Geometry& g, const LevelView<T>& v, int Jf, int If, T qxHi, T qxLo) {
-  if (If == 0) return -(qxHi * v.Gm(Jf - 1, 0) + qxLo * v.bc[g.L + Jf]) * T(0.5);
-  if (If == v.nx - 1) return -(qxLo * v.Gm(Jf - 1, v.nx - 2) + qxHi * v.bc[g.R + Jf]) * T(0.5);
-  return -(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1)) * T(0.5);
+  if (If == 0) return xscale(qxHi * v.Gm(Jf - 1, 0) + qxLo * v.bc[g.L + Jf], -0.5f);
+  if (If == v.nx - 1) return xscale(qxLo * v.Gm(Jf - 1, v.nx - 2) + qxHi * v.bc[g.R + Jf], -0.5f);
+  return xscale(qxHi * v.Gm(Jf - 1, If) + qxLo * v.Gm(Jf - 1, If - 1), -0.5f);
 }
 
 // Nonlinear term and CN right-hand side of every level (Nonlinear/RhsForce, timestepping.jl:
@@ -195,6 +206,7 @@ __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinAr
   __shared__ T sQx[kNTY][kNTX + 2];   // Qx(J0 + 1 + r, I0 + c)
   __shared__ T sFx[kNTY + 1][kNTX];   // fqx(J0 + r, I0 + 1 + c)
   __shared__ T sFy[kNTY][kNTX + 1];   // fqy(J0 + 1 + r, I0 + c)
+  __shared__ T sK[6];                 // the tile level's q0x, q0y, 1/hc^2, alpha; dt beta0, dt beta1
   const int nx = g.nx, ny = g.ny, ncol = nx - 1, nrow = ny - 1;
   const int ne = 2 * ncol + 2 * nrow;
   const int tx = (ncol + kNTX - 1) / kNTX, ty = (nrow + kNTY - 1) / kNTY;
@@ -208,8 +220,19 @@ __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinAr
     v.qy = v.qx + g.nu;
     v.G = a.gamma + (int64_t)l * g.nG;
     v.bc = a.bcn + (int64_t)l * g.nbc;
-    v.q0x = (T)a.q0[2 * l];
-    v.q0y = (T)a.q0[2 * l + 1];
+    // the level's constants, converted once per tile (a double-to-float-float conversion costs
+    // FP64 operations, which GB300 runs at 1/64 of its FP32 rate)
+    if (tid < 6) {
+      const double kv = tid == 0 ? a.q0[2 * l]
+                      : tid == 1 ? a.q0[2 * l + 1]
+                      : tid == 2 ? a.inv_hc2[l]
+                      : tid == 3 ? (a.alpha ? a.alpha[l] : 0.0)
+                      : tid == 4 ? a.dtb0 : a.dtb1;
+      sK[tid] = (T)kv;
+    }
+    __syncthreads();
+    v.q0x = sK[0];
+    v.q0y = sK[1];
     v.nx = nx; v.ny = ny; v.ncol = ncol;
     // averaged fluxes: Qy rows 0..ny, columns 1..nx-1; Qx rows 1..ny-1, columns 0..nx
     for (int i = tid; i < (kNTY + 2) * kNTX; i += kNTX * kNTY) {
@@ -238,19 +261,19 @@ __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinAr
       const T fx_hi = sFx[cr + 1][cc];   // fqx[J+1, I+1]
       const T fy_r = sFy[cr][cc + 1];    // fqy[J+1, I+1]
       const T fy_l = sFy[cr][cc];        // fqy[J+1, I]
-      const T nl = ((fx_lo - fx_hi) + (fy_r - fy_l)) * (T)a.inv_hc2[l];
+      const T nl = ((fx_lo - fx_hi) + (fy_r - fy_l)) * sK[2];
       a.nl_new[t] = nl;
-      T r = (T)a.dtb0 * nl;
-      r = r + (T)a.dtb1 * a.nl_old[t];
+      T r = sK[4] * nl;
+      r = r + sK[5] * a.nl_old[t];
       if (a.alpha) {
         // A_l gamma = gamma - alpha_l (4 gamma - neighbours), zero outside the array
         const T gc = v.Gm(J, I);
-        T lap = T(4) * gc;
+        T lap = xscale(gc, 4.0f);
         if (I > 0) lap -= v.Gm(J, I - 1);
         if (I < ncol - 1) lap -= v.Gm(J, I + 1);
         if (J > 0) lap -= v.Gm(J - 1, I);
         if (J < nrow - 1) lap -= v.Gm(J + 1, I);
-        r = (gc - (T)a.alpha[l] * lap) + r;
+        r = (gc - sK[3] * lap) + r;
       }
       const T* ed = a.edges + (int64_t)l * ne;
       T edge = T(0);
@@ -278,7 +301,7 @@ __global__ void k_trial_rings(Geometry g, const T* __restrict__ gamma, T* __rest
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     if (t < nb_total) {
       const int l = (int)(t / g.nbc), idx = (int)(t - (int64_t)l * g.nbc);
-      bcn[t] = (l < nl - 1) ? ring_value(g, gamma + (int64_t)(l + 1) * g.nG, idx) * T(0.25) : T(0);
+      bcn[t] = (l < nl - 1) ? xscale(ring_value(g, gamma + (int64_t)(l + 1) * g.nG, idx), 0.25f) : T(0);
     } else {
       const int64_t u = t - nb_total;
       const int l = (int)(u / ne), e = (int)(u - (int64_t)l * ne);

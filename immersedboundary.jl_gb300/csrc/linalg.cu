@@ -195,9 +195,44 @@ __global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int n
 
 }  // namespace
 
+// y = A x for row-major A with an even row length (16-byte aligned rows): one warp per row,
+// 16-byte loads and four independent partial sums per lane (more loads in flight per warp, as
+// the ~n / 32 warps of this launch fill only part of the GPU), combined in a fixed order.
+__global__ void k_gemv_rm2(const double* __restrict__ A, const double* __restrict__ x, double* __restrict__ y, int n) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (row >= n) return;
+  const double2* a = reinterpret_cast<const double2*>(A + row * (int64_t)n);
+  const double2* xv = reinterpret_cast<const double2*>(x);
+  const int n2 = n / 2;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  int j = lane;
+  for (; j + 96 < n2; j += 128) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 av = __ldg(&a[j + 32 * u]), xw = __ldg(&xv[j + 32 * u]);
+      acc[u] = fma(av.x, xw.x, acc[u]);
+      acc[u] = fma(av.y, xw.y, acc[u]);
+    }
+  }
+  for (int u = 0; j < n2; j += 32, ++u) {
+    const double2 av = __ldg(&a[j]), xw = __ldg(&xv[j]);
+    acc[u & 3] = fma(av.x, xw.x, acc[u & 3]);
+    acc[u & 3] = fma(av.y, xw.y, acc[u & 3]);
+  }
+  double t = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) y[row] = t;
+}
+
 cudaError_t gemv_rowmajor(const double* A, const double* x, double* y, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t threads = (int64_t)n * 32;
+  if (n % 2 == 0 && ((uintptr_t)A % 16) == 0 && ((uintptr_t)x % 16) == 0) {
+    k_gemv_rm2<<<(int)((threads + 127) / 128), 128, 0, s>>>(A, x, y, n);
+    return cudaGetLastError();
+  }
   k_gemv_rm<<<(int)((threads + 255) / 256), 256, 0, s>>>(A, x, y, n);
   return cudaGetLastError();
 }

@@ -81,6 +81,7 @@ struct ib_handle {
   int coarse_from = 2;                          // first (0-based) level counted as coarse
   bool wdst = false;                            // both axes use the warp-per-line passes
   bool gdst = false;                            // mixed precision: transforms as tensor-core GEMMs
+  bool cn_pred = false;                         // mixed: trial CN solve refined from Gamma_n
   SineGemm sgx, sgy;                            // their BF16 sine-matrix images (sgemm.cu)
   float* gw32 = nullptr;                        // FP32 work of the GEMM passes
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
@@ -266,7 +267,8 @@ cudaError_t poisson64(ib_handle* h, const double* in, double* out, int batch, co
 // on the FP32 pipe; w32 / x032 / x132: FP32 work of batch arrays.  sweeps = 0 (warp passes
 // only) is the transform-only solve x = x0, FP32-accurate, and needs w32 alone.
 cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, const df64* bc, const SolveOp& op,
-                          const df64* sub_from, float* w32, float* x032, float* x132, int sweeps) {
+                          const df64* sub_from, float* w32, float* x032, float* x132, int sweeps,
+                          const df64* pred = nullptr) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   YPassArgs<float> ya{};
@@ -314,6 +316,28 @@ cudaError_t poisson_mixed(ib_handle* h, const df64* in, df64* out, int batch, co
     a.base = x032; a.base2 = two ? x132 : nullptr;
     a.epi = sub_from ? kEpiSubAddBase : kEpiAddBase;
     return gx_inv<df64>(g, h->sgx, a, st, s);
+  }
+  if (h->wdst && pred && h->r1 && !sub_from) {
+    // from a predictor p (float-float, e.g. the previous step's value of the unknown):
+    //   d1 = F32 solve(r0), r0 = b [+ bc] - M p (kept);  d2 = F32 solve(r0 - M d1)
+    //   x = p + d1 + d2
+    // two transform solves instead of three; the sweeps carry only the change from p
+    df64* r1 = reinterpret_cast<df64*>(h->r1);
+    a.in = in; a.out = w32; a.bc = bc; a.pro = kProResidD; a.based = pred; a.epi = kEpiStore;
+    a.mc = op.mc; a.ma = op.ma; a.mstep = op.mstep; a.resid_out = r1;
+    CE((wx_fwd<float, df64>(g, h->axx32.d, a, s)));
+    CE(wypass<float>(g, h->axy32.d, ya, s));
+    XArgs b{};
+    b.batch = batch; b.stride = g.nG; b.bcfac = 1.0;
+    b.in = w32; b.out = x032; b.pro = kProLoad; b.epi = kEpiStore;
+    CE((wx_inv<float, float>(g, h->axx32.d, b, s)));
+    b.in = r1; b.out = w32; b.pro = kProResid; b.base = x032; b.mc = op.mc; b.ma = op.ma; b.mstep = op.mstep;
+    CE((wx_fwd<float, df64>(g, h->axx32.d, b, s)));
+    CE(wypass<float>(g, h->axy32.d, ya, s));
+    b = XArgs{};
+    b.batch = batch; b.stride = g.nG; b.bcfac = 1.0;
+    b.in = w32; b.out = out; b.pro = kProLoad; b.sub_from = pred; b.base = x032; b.epi = kEpiAddTo;
+    return wx_inv<float, df64>(g, h->axx32.d, b, s);
   }
   if (h->wdst) {
     // warp-per-line passes; w32 holds the transposed intermediate
@@ -574,8 +598,16 @@ cudaError_t enqueue_trial(ib_handle* h, int p) {
   na.dtb0 = h->dt * h->beta0;
   na.dtb1 = h->dt * h->beta1;
   CE(nonlin_rhs<S>(g, na, s));
-  // Gamma_s[l] = Ainv_l rhs[l] for every level in one batched solve
-  CE(solve(h, view<S>(h->rhs), gs, L, nullptr, op_cn_all(h), nullptr));
+  // Gamma_s[l] = Ainv_l rhs[l] for every level in one batched solve (mixed precision: refined
+  // from Gamma_n[l], the change over one step being what the FP32 sweeps carry)
+  if constexpr (std::is_same<S, df64>::value) {
+    if (h->cn_pred)
+      CE(poisson_mixed(h, view<S>(h->rhs), gs, L, nullptr, op_cn_all(h), nullptr, h->w32, h->x032, h->x132, 2, gam));
+    else
+      CE(solve(h, view<S>(h->rhs), gs, L, nullptr, op_cn_all(h), nullptr));
+  } else {
+    CE(solve(h, view<S>(h->rhs), gs, L, nullptr, op_cn_all(h), nullptr));
+  }
   return vort2flux<S>(h, gs, view<S>(h->psi), nullptr, view<S>(h->qs1), view<S>(h->rings));
 }
 
@@ -1527,6 +1559,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     if (v >= 1) h->coarse_from = v;
   }
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
+  // mixed precision with two sweeps: the trial Crank-Nicolson solve starts from Gamma_n (two
+  // FP32 transform solves instead of three; IBGB300_CN_PREDICTOR=0 keeps three)
+  h->cn_pred = h->refine >= 2;
+  if (const char* env = std::getenv("IBGB300_CN_PREDICTOR")) h->cn_pred = h->cn_pred && env[0] != '0';
   if (const char* env = std::getenv("IBGB300_PC_ASSEMBLY")) h->asm_fp64 = std::strcmp(env, "fp64") == 0;
   // transform kernels, by measurement on GB300: FP32 (mixed) transforms run faster one warp
   // per line where both axes allow it; FP64 transforms are FP64-pipe bound and the shared-memory

@@ -115,36 +115,42 @@ __global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__
   }
 }
 
-// Multilevel curl! (fluid-ops.jl:138-182); bc == nullptr means a zero ring.
+// Multilevel curl! (fluid-ops.jl:138-182); bc == nullptr means a zero ring.  One block row per
+// flux row: blockIdx.y runs over the batch's rows (ny rows of qx, then ny + 1 rows of qy), so
+// an element's indices need no division.
 template <typename T>
 __global__ void k_curl(Geometry g, const T* __restrict__ psi, const T* __restrict__ bc, T* __restrict__ q, int batch) {
   const int nx = g.nx, ny = g.ny, ncol = nx - 1;
-  const int64_t total = (int64_t)batch * g.nq;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(t / g.nq), e = (int)(t - (int64_t)b * g.nq);
-    const T* p = psi + (int64_t)b * g.nG;
-    const T* c = bc ? bc + (int64_t)b * g.nbc : nullptr;
+  const int rows = 2 * ny + 1;
+  const int b = blockIdx.y / rows, row = blockIdx.y - b * rows;
+  const T* p = psi + (int64_t)b * g.nG;
+  const T* c = bc ? bc + (int64_t)b * g.nbc : nullptr;
+  T* qb = q + (int64_t)b * g.nq;
 #define BC(i) (c ? c[(i)] : T(0))
-    T v;
-    if (e < g.nu) {
-      const int J = e / (nx + 1), I = e - J * (nx + 1);
+  if (row < ny) {
+    const int J = row;
+    for (int I = blockIdx.x * blockDim.x + threadIdx.x; I <= nx; I += gridDim.x * blockDim.x) {
+      T v;
       if (I == 0) v = BC(g.L + J + 1) - BC(g.L + J);
       else if (I == nx) v = BC(g.R + J + 1) - BC(g.R + J);
       else if (J == 0) v = p[I - 1] - BC(g.B + I);
       else if (J == ny - 1) v = BC(g.T + I) - p[(ny - 2) * ncol + I - 1];
       else v = p[J * ncol + I - 1] - p[(J - 1) * ncol + I - 1];
-    } else {
-      const int e2 = e - g.nu;
-      const int J = e2 / nx, I = e2 - J * nx;
+      qb[J * (nx + 1) + I] = v;
+    }
+  } else {
+    const int J = row - ny;
+    for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nx; I += gridDim.x * blockDim.x) {
+      T v;
       if (J == 0) v = BC(g.B + I) - BC(g.B + I + 1);
       else if (J == ny) v = BC(g.T + I) - BC(g.T + I + 1);
       else if (I == 0) v = BC(g.L + J) - p[(J - 1) * ncol];
       else if (I == nx - 1) v = p[(J - 1) * ncol + nx - 2] - BC(g.R + J);
       else v = p[(J - 1) * ncol + I - 1] - p[(J - 1) * ncol + I];
+      qb[g.nu + J * nx + I] = v;
     }
-#undef BC
-    q[t] = v;
   }
+#undef BC
 }
 
 // rot! = C^T (fluid-ops.jl:117-129)
@@ -347,7 +353,17 @@ cudaError_t coarsify(const Geometry& g, T* gc, const T* gf, int batch, int64_t s
 }
 template <typename T>
 cudaError_t curl(const Geometry& g, const T* psi, const T* bc, T* q, int batch, cudaStream_t s) {
-  k_curl<T><<<blocks_for((int64_t)batch * g.nq), kThreads, 0, s>>>(g, psi, bc, q, batch);
+  if (batch <= 0) return cudaSuccess;
+  const int64_t rows = (int64_t)batch * (2 * g.ny + 1);
+  if (rows > 65535) {
+    for (int b = 0; b < batch; ++b) {
+      cudaError_t e = curl<T>(g, psi + (int64_t)b * g.nG, bc ? bc + (int64_t)b * g.nbc : nullptr, q + (int64_t)b * g.nq, 1, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  const dim3 grid((g.nx + 1 + kThreads - 1) / kThreads, (unsigned)rows);
+  k_curl<T><<<grid, kThreads, 0, s>>>(g, psi, bc, q, batch);
   return cudaGetLastError();
 }
 template <typename T>

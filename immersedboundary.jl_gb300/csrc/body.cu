@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(256) k_reg_scatter_tiles(Geometry g, const dou
                                                            const int* __restrict__ body_idx,
                                                            const double* __restrict__ weight, int nb, T* __restrict__ q,
                                                            int tiles_x0, int tiles_y0, int tiles_x1, int tiles_y1,
-                                                           int* __restrict__ status) {
+                                                           int* __restrict__ status, const int* __restrict__ box) {
   __shared__ int list[kChunk];
   __shared__ int count;
   __shared__ int warp_counts[8];
@@ -56,6 +56,10 @@ __global__ void __launch_bounds__(256) k_reg_scatter_tiles(Geometry g, const dou
   const int tile = blockIdx.x % (ntx * nty);
   const int c = blockIdx.x / (ntx * nty);
   const int tx = tiles_x0 + tile % ntx, ty = tiles_y0 + tile / ntx;
+  // tiles outside the box of all windows have no point: their faces are left unwritten (the
+  // caller reads the flux only inside the box)
+  if (box && (tx * kTile > box[1] || (tx + 1) * kTile <= box[0] || ty * kTile > box[3] || (ty + 1) * kTile <= box[2]))
+    return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int fi = tx * kTile + (threadIdx.x % kTile), fj = ty * kTile + (threadIdx.x / kTile);
   const int pitch = (c == 0) ? g.nx + 1 : g.nx;
@@ -107,11 +111,46 @@ __global__ void __launch_bounds__(256) k_reg_scatter_tiles(Geometry g, const dou
 }
 
 // rot of the scattered flux: full circulation array, zero outside the body box
+// Face box of every point's 13x13 window, box = {i_lo, i_hi, j_lo, j_hi} (one block; the
+// flux faces E^T can touch, both components).
+__global__ void k_body_box(Geometry g, const int* __restrict__ body_idx, int nb, int* __restrict__ box) {
+  __shared__ int s[4][256];
+  int v[4] = {1 << 30, -(1 << 30), 1 << 30, -(1 << 30)};
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+    const int i0 = body_idx[2 * k] - kSupp - 1, j0 = body_idx[2 * k + 1] - kSupp - 1;
+    v[0] = min(v[0], i0);
+    v[1] = max(v[1], i0 + kWin - 1);
+    v[2] = min(v[2], j0);
+    v[3] = max(v[3], j0 + kWin - 1);
+  }
+  for (int i = 0; i < 4; ++i) s[i][threadIdx.x] = v[i];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s[0][threadIdx.x] = min(s[0][threadIdx.x], s[0][threadIdx.x + o]);
+      s[1][threadIdx.x] = max(s[1][threadIdx.x], s[1][threadIdx.x + o]);
+      s[2][threadIdx.x] = min(s[2][threadIdx.x], s[2][threadIdx.x + o]);
+      s[3][threadIdx.x] = max(s[3][threadIdx.x], s[3][threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    box[0] = max(s[0][0], 0);
+    box[1] = min(s[1][0], g.nx);
+    box[2] = max(s[2][0], 0);
+    box[3] = min(s[3][0], g.ny);
+  }
+}
+
 template <typename T>
-__global__ void k_rot_box(Geometry g, const T* __restrict__ q, T* __restrict__ gam, int i_lo, int i_hi, int j_lo, int j_hi) {
+__global__ void k_rot_box(Geometry g, const T* __restrict__ q, T* __restrict__ gam, int i_lo, int i_hi, int j_lo, int j_hi,
+                          const int* __restrict__ box) {
   const int nx = g.nx, ncol = nx - 1;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < g.nG; t += (int64_t)gridDim.x * blockDim.x) {
-    const int J = (int)(t / ncol), I = (int)(t - (int64_t)J * ncol);
+  if (box) {
+    i_lo = box[0]; i_hi = box[1]; j_lo = box[2]; j_hi = box[3];
+  }
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < g.nG; t += gridDim.x * blockDim.x) {
+    const int J = t / ncol, I = t - J * ncol;
     T v = T(0);
     // node (J, I) touches qx faces (J, I+1), (J+1, I+1) and qy faces (J+1, I), (J+1, I+1)
     if (I + 1 >= i_lo && I <= i_hi && J + 1 >= j_lo && J <= j_hi) {
@@ -217,18 +256,27 @@ template <typename T>
 cudaError_t reg_scatter(const Geometry& g, const double* f, const int* body_idx, const double* weight, int nb, T* q,
                         int* status, cudaStream_t s) {
   const int tx = (g.nx + 1 + kTile - 1) / kTile, ty = (g.ny + 1 + kTile - 1) / kTile;
-  k_reg_scatter_tiles<T><<<2 * tx * ty, 256, 0, s>>>(g, f, body_idx, weight, nb, q, 0, 0, tx, ty, status);
+  k_reg_scatter_tiles<T><<<2 * tx * ty, 256, 0, s>>>(g, f, body_idx, weight, nb, q, 0, 0, tx, ty, status, nullptr);
   return cudaGetLastError();
 }
 
+// rot(E^T f): the scatter covers only the faces inside the box of the windows (box: 4 ints of
+// device scratch, or nullptr for the whole flux domain), the rot reads only those
 template <typename T>
 cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_idx, const double* weight, int nb,
-                            T* qtmp, T* gam, int ncols, int64_t fstride, int* status, cudaStream_t s) {
+                            T* qtmp, T* gam, int ncols, int64_t fstride, int* status, int* box, cudaStream_t s) {
   (void)ncols;
   (void)fstride;
-  cudaError_t e = reg_scatter<T>(g, f, body_idx, weight, nb, qtmp, status, s);
-  if (e != cudaSuccess) return e;
-  k_rot_box<T><<<nblk(g.nG), 256, 0, s>>>(g, qtmp, gam, 0, g.nx, 0, g.ny);
+  if (box && nb > 0) {
+    k_body_box<<<1, 256, 0, s>>>(g, body_idx, nb, box);
+    const int tx = (g.nx + 1 + kTile - 1) / kTile, ty = (g.ny + 1 + kTile - 1) / kTile;
+    k_reg_scatter_tiles<T><<<2 * tx * ty, 256, 0, s>>>(g, f, body_idx, weight, nb, qtmp, 0, 0, tx, ty, status, box);
+  } else {
+    cudaError_t e = reg_scatter<T>(g, f, body_idx, weight, nb, qtmp, status, s);
+    if (e != cudaSuccess) return e;
+    box = nullptr;
+  }
+  k_rot_box<T><<<nblk(g.nG), 256, 0, s>>>(g, qtmp, gam, 0, g.nx, 0, g.ny, nb > 0 ? box : nullptr);
   return cudaGetLastError();
 }
 
@@ -259,9 +307,9 @@ template cudaError_t reg_scatter<double>(const Geometry&, const double*, const i
 template cudaError_t reg_scatter<df64>(const Geometry&, const double*, const int*, const double*, int, df64*, int*,
                                         cudaStream_t);
 template cudaError_t reg_scatter_rot<double>(const Geometry&, const double*, const int*, const double*, int, double*,
-                                             double*, int, int64_t, int*, cudaStream_t);
+                                             double*, int, int64_t, int*, int*, cudaStream_t);
 template cudaError_t reg_scatter_rot<df64>(const Geometry&, const double*, const int*, const double*, int, df64*,
-                                            df64*, int, int64_t, int*, cudaStream_t);
+                                            df64*, int, int64_t, int*, int*, cudaStream_t);
 template cudaError_t unit_scatter_rot<double>(const Geometry&, const int*, const double*, int, int, int, double*,
                                               cudaStream_t);
 template cudaError_t unit_scatter_rot<df64>(const Geometry&, const int*, const double*, int, int, int, df64*,

@@ -270,11 +270,13 @@ template <typename T>
 cudaError_t reg_gather(const Geometry& g, const T* q, const double* q0, const int* body_idx,
                        const double* weight, int nb, double* fb, int ncols, int64_t qstride,
                        int64_t fstride, cudaStream_t s);
-// E^T followed by rot restricted to the body box: gamma_out = rot(E^T f) (whole array written)
+// E^T followed by rot: gamma_out = rot(E^T f) (whole array written).  With box (4 ints of
+// device scratch) the scatter and the rot's reads cover only the face box of the points'
+// windows (found on the device first), and qtmp is left unwritten outside it.
 template <typename T>
 cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_idx,
                             const double* weight, int nb, T* qtmp, T* gam, int ncols,
-                            int64_t fstride, int* status, cudaStream_t s);
+                            int64_t fstride, int* status, int* box, cudaStream_t s);
 // E^T alone (operator test entry point)
 template <typename T>
 cudaError_t reg_scatter(const Geometry& g, const double* f, const int* body_idx, const double* weight,

@@ -81,7 +81,9 @@ struct ib_handle {
   int coarse_from = 2;                          // first (0-based) level counted as coarse
   bool wdst = false;                            // both axes use the warp-per-line passes
   bool gdst = false;                            // mixed precision: transforms as tensor-core GEMMs
-  bool cn_pred = false;                         // mixed: trial CN solve refined from Gamma_n
+  bool cn_pred = false;                         // mixed: trial CN solve refined from Gamma_n,
+  double* cprev = nullptr;                      //   the projection from its previous correction
+  cudaEvent_t stress_ev[2] = {nullptr, nullptr};  // fork / join of the stress branch
   SineGemm sgx, sgy;                            // their BF16 sine-matrix images (sgemm.cu)
   float* gw32 = nullptr;                        // FP32 work of the GEMM passes
   double *d_one = nullptr, *d_zero = nullptr;   // residual operator coefficients
@@ -142,7 +144,8 @@ struct ib_handle {
   int warm_start = IB_WARM_PREVIOUS;
   std::vector<int> cg_iters;
   std::vector<double> cg_res;
-  int* status = nullptr;  // [0] out of grid, [1] non-finite flux, [2] singular Schur matrix
+  int* status = nullptr;  // [0] out of grid, [1] non-finite flux, [2] singular Schur matrix, [3] pipeline timeout
+  int* d_box = nullptr;   // face box of the body windows (E^T scatter scratch)
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool use_graph = true;
   int kernels_per_step = 0;
@@ -627,8 +630,19 @@ cudaError_t enqueue_project(ib_handle* h, int p) {
   S* gs = view<S>(h->G[p ^ 1]);
   if (h->nb > 0) {
     CE(reg_scatter_rot<S>(g, h->fb, h->body_idx, h->weight, h->nb, view<S>(h->qtmp), view<S>(h->gtmp), 1, h->nf,
-                          h->status + 1, h->stream));
-    CE(solve(h, view<S>(h->gtmp), gs, 1, nullptr, op_cn1(h), gs));
+                          h->status + 1, h->d_box, h->stream));
+    bool done = false;
+    if constexpr (std::is_same<S, df64>::value) {
+      if (h->cn_pred && h->cprev && h->wdst) {
+        // c = Ainv_1 C^T E^T Fb refined from the previous step's c (kept in cprev), then
+        // Gamma_s1 -= c
+        df64* c = view<df64>(h->cprev);
+        CE(poisson_mixed(h, view<S>(h->gtmp), c, 1, nullptr, op_cn1(h), nullptr, h->w32, h->x032, h->x132, 2, c));
+        CE(axpby<df64>(gs, c, df64(-1.0f), df64(1.0f), g.nG, h->stream));
+        done = true;
+      }
+    }
+    if (!done) CE(solve(h, view<S>(h->gtmp), gs, 1, nullptr, op_cn1(h), gs));
   }
   return vort2flux<S>(h, gs, view<S>(h->psi), view<S>(h->q), nullptr, view<S>(h->rings));
 }
@@ -642,6 +656,19 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
     CE(reg_gather<S>(h->g, view<S>(h->qs1), h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, h->g.nq, h->nf,
                      h->stream));
     CE(gemv_rowmajor(h->binv_rm, h->ftmp, h->fb, h->nf, h->stream));
+    if (h->side && h->stress_ev[0]) {
+      // C_D / C_L and the surface stress only read Fb: a branch beside the projection
+      CE(cudaEventRecord(h->stress_ev[0], h->stream));
+      CE(cudaStreamWaitEvent(h->side, h->stress_ev[0], 0));
+      cudaStream_t main = h->stream;
+      h->stream = h->side;
+      const cudaError_t es = enqueue_stress(h);
+      h->stream = main;
+      CE(es);
+      CE(cudaEventRecord(h->stress_ev[1], h->side));
+      CE(enqueue_project<S>(h, p));
+      return cudaStreamWaitEvent(h->stream, h->stress_ev[1], 0);
+    }
     CE(enqueue_stress(h));
   }
   return enqueue_project<S>(h, p);
@@ -658,7 +685,7 @@ cudaError_t schur_apply(ib_handle* h, const double* z, double* out) {
   cudaStream_t s = h->stream;
   S* Gw = view<S>(h->Gw);
   CE(reg_scatter_rot<S>(g, z, h->body_idx, h->weight, h->nb, view<S>(h->qtmp), view<S>(h->gtmp), 1, h->nf,
-                        h->status + 1, s));
+                        h->status + 1, h->d_box, s));
   CE(solve(h, view<S>(h->gtmp), Gw, 1, nullptr, op_cn1(h), nullptr));
   if (g.nlev > 1) CE(cudaMemsetAsync(Gw + g.nG, 0, sizeof(S) * (g.nlev - 1) * g.nG, s));
   CE(vort2flux<S>(h, Gw, view<S>(h->Pw), nullptr, view<S>(h->qw), view<S>(h->rings_w)));
@@ -874,6 +901,8 @@ void destroy_handle(ib_handle* h) {
   h->sgy.release();
   h->rplan.release();
   for (auto ev : h->fork_ev)
+    if (ev) cudaEventDestroy(ev);
+  for (auto ev : h->stress_ev)
     if (ev) cudaEventDestroy(ev);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1634,7 +1663,13 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     if (h->v2f_levels && !autotune_on && (e = h->rplan.build(g)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));
   }
-  AL(h->status, 4); AL(h->d_counter, 1);
+  AL(h->status, 4); AL(h->d_counter, 1); AL(h->d_box, 4);
+  if (h->precision == IB_PREC_MIXED && h->cn_pred) AL(h->cprev, nG);
+  for (auto& ev : h->stress_ev)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
+      ev = nullptr;
+      return bail(fail(h, IB_ERR_CUDA, "cudaEventCreate", e));
+    }
   AL(h->cdcl, 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->hist, (int64_t)h->hist_cap * 2 * (h->nbodies > 0 ? h->nbodies : 1));
   AL(h->stress, h->nf);
@@ -1794,6 +1829,8 @@ int ib_set_state(ib_handle* h, const double* gamma, const double* q, const doubl
   }
   // the batched Vort2Flux predicts psi and the rings from the previous call: a new state starts
   // from its own psi (or zero) and zero rings
+  // the projection's correction predicts the next one: a new state starts from zero
+  if (h->cprev) CK(cudaMemsetAsync(h->cprev, 0, sizeof(double) * g.nG, s));
   if (h->v2f_levels) {
     if (!psi) CK(cudaMemsetAsync(h->psi, 0, nGL, s));
     CK(cudaMemsetAsync(h->rings, 0, sizeof(double) * g.nlev * g.nbc, s));

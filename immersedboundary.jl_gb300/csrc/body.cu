@@ -14,6 +14,7 @@ template <typename T>
 __global__ void k_reg_gather(Geometry g, const T* __restrict__ q, const double* __restrict__ q0v, const int* __restrict__ body_idx,
                              const double* __restrict__ weight, int nb, double* __restrict__ fb, int ncols,
                              int64_t qstride, int64_t fstride) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t total = (int64_t)ncols * 2 * nb;
@@ -49,6 +50,7 @@ __global__ void __launch_bounds__(256) k_reg_scatter_tiles(Geometry g, const dou
                                                            const double* __restrict__ weight, int nb, T* __restrict__ q,
                                                            int tiles_x0, int tiles_y0, int tiles_x1, int tiles_y1,
                                                            int* __restrict__ status, const int* __restrict__ box) {
+  pdl_begin();
   __shared__ int list[kChunk];
   __shared__ int count;
   __shared__ int warp_counts[8];
@@ -114,6 +116,7 @@ __global__ void __launch_bounds__(256) k_reg_scatter_tiles(Geometry g, const dou
 // Face box of every point's 13x13 window, box = {i_lo, i_hi, j_lo, j_hi} (one block; the
 // flux faces E^T can touch, both components).
 __global__ void k_body_box(Geometry g, const int* __restrict__ body_idx, int nb, int* __restrict__ box) {
+  pdl_begin();
   __shared__ int s[4][256];
   int v[4] = {1 << 30, -(1 << 30), 1 << 30, -(1 << 30)};
   for (int k = threadIdx.x; k < nb; k += blockDim.x) {
@@ -145,6 +148,7 @@ __global__ void k_body_box(Geometry g, const int* __restrict__ body_idx, int nb,
 template <typename T>
 __global__ void k_rot_box(Geometry g, const T* __restrict__ q, T* __restrict__ gam, int i_lo, int i_hi, int j_lo, int j_hi,
                           const int* __restrict__ box) {
+  pdl_begin();
   const int nx = g.nx, ncol = nx - 1;
   if (box) {
     i_lo = box[0]; i_hi = box[1]; j_lo = box[2]; j_hi = box[3];
@@ -203,6 +207,7 @@ __global__ void k_unit_columns(double* f, int nf, int col0, int ncols) {
 __global__ void k_update_stress(const double* __restrict__ fb, int nb, const int* __restrict__ body_start,
                                 const double* __restrict__ ds, double h, double dt, double* __restrict__ out,
                                 double* __restrict__ stress) {
+  pdl_begin();
   __shared__ double sx[256], sy[256];
   const int body = blockIdx.x;
   const int s0 = body_start[body], s1 = body_start[body + 1], n = s1 - s0;
@@ -246,8 +251,7 @@ cudaError_t reg_gather(const Geometry& g, const T* q, const double* q0, const in
                        cudaStream_t s) {
   if (nb <= 0) return cudaSuccess;
   const int64_t warps = (int64_t)ncols * 2 * nb;
-  k_reg_gather<T><<<nblk(warps * 32), 256, 0, s>>>(g, q, q0, body_idx, weight, nb, fb, ncols, qstride, fstride);
-  return cudaGetLastError();
+  return launch_k(k_reg_gather<T>, dim3(nblk(warps * 32)), dim3(256), 0, s, g, q, q0, body_idx, weight, nb, fb, ncols, qstride, fstride);
 }
 
 // The body box (in faces) is taken from the whole flux domain; tiles outside every window
@@ -268,16 +272,19 @@ cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_
   (void)ncols;
   (void)fstride;
   if (box && nb > 0) {
-    k_body_box<<<1, 256, 0, s>>>(g, body_idx, nb, box);
+    cudaError_t e = launch_k(k_body_box, dim3(1), dim3(256), 0, s, g, body_idx, nb, box);
+    if (e != cudaSuccess) return e;
     const int tx = (g.nx + 1 + kTile - 1) / kTile, ty = (g.ny + 1 + kTile - 1) / kTile;
-    k_reg_scatter_tiles<T><<<2 * tx * ty, 256, 0, s>>>(g, f, body_idx, weight, nb, qtmp, 0, 0, tx, ty, status, box);
+    e = launch_k(k_reg_scatter_tiles<T>, dim3(2 * tx * ty), dim3(256), 0, s, g, f, body_idx, weight, nb, qtmp, 0, 0, tx, ty, status,
+                 (const int*)box);
+    if (e != cudaSuccess) return e;
   } else {
     cudaError_t e = reg_scatter<T>(g, f, body_idx, weight, nb, qtmp, status, s);
     if (e != cudaSuccess) return e;
     box = nullptr;
   }
-  k_rot_box<T><<<nblk(g.nG), 256, 0, s>>>(g, qtmp, gam, 0, g.nx, 0, g.ny, nb > 0 ? box : nullptr);
-  return cudaGetLastError();
+  return launch_k(k_rot_box<T>, dim3(nblk(g.nG)), dim3(256), 0, s, g, (const T*)qtmp, gam, 0, g.nx, 0, g.ny,
+                  (const int*)(nb > 0 ? box : nullptr));
 }
 
 template <typename T>
@@ -294,8 +301,7 @@ cudaError_t unit_columns(double* f, int nf, int col0, int ncols, cudaStream_t s)
 
 cudaError_t update_stress_hd(const double* fb, int nb, int nbodies, const int* body_start, const double* ds, double h,
                              double dt, double* cd_cl_out, double* stress_out, cudaStream_t s) {
-  k_update_stress<<<nbodies, 256, 0, s>>>(fb, nb, body_start, ds, h, dt, cd_cl_out, stress_out);
-  return cudaGetLastError();
+  return launch_k(k_update_stress, dim3(nbodies), dim3(256), 0, s, fb, nb, body_start, ds, h, dt, cd_cl_out, stress_out);
 }
 
 template cudaError_t reg_gather<double>(const Geometry&, const double*, const double*, const int*, const double*, int,

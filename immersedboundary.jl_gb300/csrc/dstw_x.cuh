@@ -24,6 +24,7 @@ using wdst::line_sync;
 template <typename T, typename Tin, int P, int NL, int PRO, bool kBC>
 __global__ void __launch_bounds__(kLines * NL, IB_WDST_XMINB)
 k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
+  pdl_begin();
   // exact arithmetic of the prologue: FP64, or float-float when the input is float-float
   using A = typename std::conditional<is_df64<Tin>::value, df64, double>::type;
   using Sh = Shape<T, P, NL>;
@@ -213,6 +214,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
 template <typename T, typename Tout, int P, int NL, int EPI>
 __global__ void __launch_bounds__(kLines * NL, IB_WDST_XMINB)
 k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
+  pdl_begin();
   using A = typename std::conditional<is_df64<Tout>::value, df64, double>::type;
   using Sh = Shape<T, P, NL>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -320,8 +322,7 @@ cudaError_t launch_fwd(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, 
   cudaError_t e = set_smem_limit((const void*)k, smem);
   if (e != cudaSuccess) return e;
   const int total = a.batch * (g.ny - 1);
-  k<<<(total + kLines - 1) / kLines, kLines * NL, smem, s>>>(g, ax, a);
-  return cudaGetLastError();
+  return launch_k(k, dim3((total + kLines - 1) / kLines), dim3(kLines * NL), smem, s, g, ax, a);
 }
 
 template <typename T, typename Tin, int P, int NL>
@@ -354,8 +355,7 @@ cudaError_t launch_inv(const Geometry& g, const DstAxis<T>& ax, const XArgs& a, 
   cudaError_t e = set_smem_limit((const void*)k, smem);
   if (e != cudaSuccess) return e;
   const int total = a.batch * (g.ny - 1);
-  k<<<(total + kLines - 1) / kLines, kLines * NL, smem, s>>>(g, ax, a);
-  return cudaGetLastError();
+  return launch_k(k, dim3((total + kLines - 1) / kLines), dim3(kLines * NL), smem, s, g, ax, a);
 }
 
 // epilogues per output type: FP64 path store / subtract; mixed path FP32 store of the iterate

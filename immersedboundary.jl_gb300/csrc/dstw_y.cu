@@ -15,6 +15,7 @@ using wdst::line_sync;
 template <typename T, int P, int NL, SpecOp OP>
 __global__ void __launch_bounds__(kLines * NL, IB_WDST_YMINB)
 k_wy(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
+  pdl_begin();
   using Sh = Shape<T, P, NL>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int w = threadIdx.x / NL, lane = threadIdx.x % NL;
@@ -69,11 +70,11 @@ cudaError_t launch(const Geometry& g, const DstAxis<T>& ax, const YPassArgs<T>& 
   if (a.op == SpecOp::kFwd) {
     auto k = k_wy<T, P, NL, SpecOp::kFwd>;
     if ((e = set_smem_limit((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, kLines * NL, smem, s>>>(g, ax, a);
+    if ((e = launch_k(k, dim3(blocks), dim3(kLines * NL), smem, s, g, ax, a)) != cudaSuccess) return e;
   } else {
     auto k = k_wy<T, P, NL, SpecOp::kScale>;
     if ((e = set_smem_limit((const void*)k, smem)) != cudaSuccess) return e;
-    k<<<blocks, kLines * NL, smem, s>>>(g, ax, a);
+    if ((e = launch_k(k, dim3(blocks), dim3(kLines * NL), smem, s, g, ax, a)) != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }

@@ -354,6 +354,39 @@ cudaError_t v2f_ring_eval(const Geometry& g, const RingPlan& rp, int l, const df
                           df64* ring_l, cudaStream_t s);
 cudaError_t v2f_ring_coef(const Geometry& g, const RingPlan& rp, int l, cudaStream_t s);
 
+// ----------------------------------------------------------------------------------------------
+// Programmatic dependent launch: while g_pdl is set (the capture of a static step's graph), the
+// step kernels are launched so that each one may be scheduled while its predecessor in the
+// stream drains; every such kernel begins with pdl_begin(), which waits for the predecessor to
+// complete and its writes to be visible before anything else, and lets the next kernel launch.
+// Launched the ordinary way (g_pdl clear) pdl_begin() has nothing to wait for.
+// ----------------------------------------------------------------------------------------------
+extern thread_local bool g_pdl;
+
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  if (!g_pdl) {
+    k<<<grid, block, smem, s>>>(args...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 enum KClass : int { kClassXPass = 0, kClassYPass = 1, kClassNonlin = 2, kClassCount = 3 };
 struct Prof {
   int cls = -1;

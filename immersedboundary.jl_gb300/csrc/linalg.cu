@@ -16,6 +16,7 @@ constexpr int NB = 64;  // pivot block width
 
 // y = A x, A row-major n x n; one warp per row, lanes stride the row, fixed-order reduction.
 __global__ void k_gemv_rm(const double* __restrict__ A, const double* __restrict__ x, double* __restrict__ y, int n) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (row >= n) return;
@@ -199,6 +200,7 @@ __global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int n
 // 16-byte loads and four independent partial sums per lane (more loads in flight per warp, as
 // the ~n / 32 warps of this launch fill only part of the GPU), combined in a fixed order.
 __global__ void k_gemv_rm2(const double* __restrict__ A, const double* __restrict__ x, double* __restrict__ y, int n) {
+  pdl_begin();
   const int lane = threadIdx.x & 31;
   const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (row >= n) return;
@@ -230,8 +232,7 @@ cudaError_t gemv_rowmajor(const double* A, const double* x, double* y, int n, cu
   if (n <= 0) return cudaSuccess;
   const int64_t threads = (int64_t)n * 32;
   if (n % 2 == 0 && ((uintptr_t)A % 16) == 0 && ((uintptr_t)x % 16) == 0) {
-    k_gemv_rm2<<<(int)((threads + 127) / 128), 128, 0, s>>>(A, x, y, n);
-    return cudaGetLastError();
+    return launch_k(k_gemv_rm2, dim3((int)((threads + 127) / 128)), dim3(128), 0, s, A, x, y, n);
   }
   k_gemv_rm<<<(int)((threads + 255) / 256), 256, 0, s>>>(A, x, y, n);
   return cudaGetLastError();

@@ -35,6 +35,7 @@ using namespace ib;
 
 namespace ib {
 thread_local Prof* g_prof = nullptr;
+thread_local bool g_pdl = false;
 }
 
 namespace {
@@ -148,6 +149,7 @@ struct ib_handle {
   int* d_box = nullptr;   // face box of the body windows (E^T scatter scratch)
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   bool use_graph = true;
+  bool use_pdl = true;  // programmatic dependent launch inside the static step graph
   int kernels_per_step = 0;
   int64_t device_bytes = 0;
   double setup_ms = 0.0;
@@ -554,6 +556,7 @@ cudaError_t vort2flux(ib_handle* h, S* gam, S* psi, S* q, S* q1, S* rings) {
 
 __global__ void k_hist_append(const double* __restrict__ cdcl, double* __restrict__ hist, int cap, int n,
                               int* __restrict__ counter) {
+  pdl_begin();
   const int idx = *counter % cap;
   for (int i = threadIdx.x; i < n; i += blockDim.x) hist[(int64_t)idx * n + i] = cdcl[i];
   __syncthreads();
@@ -618,8 +621,8 @@ cudaError_t enqueue_trial(ib_handle* h, int p) {
 cudaError_t enqueue_stress(ib_handle* h) {
   cudaStream_t s = h->stream;
   CE(update_stress_hd(h->fb, h->nb, h->nbodies, h->body_start, h->ds, h->g.h, h->dt, h->cdcl, h->stress, s));
-  k_hist_append<<<1, 64, 0, s>>>(h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies, h->d_counter);
-  return cudaGetLastError();
+  return launch_k(k_hist_append, dim3(1), dim3(64), 0, s, (const double*)h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies,
+                  h->d_counter);
 }
 
 // g. CircProjecter (timestepping.jl:156-171): Gamma_1 = Gamma_s1 - Ainv_1 C^T E^T Fb, then
@@ -854,7 +857,9 @@ int capture_graphs(ib_handle* h) {
     if (h->gexec[p]) { cudaGraphExecDestroy(h->gexec[p]); h->gexec[p] = nullptr; }
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    g_pdl = h->use_pdl;  // kernels of the static step overlap their launch with the predecessor's tail
     cudaError_t e = enqueue_step_mode(h, p);
+    g_pdl = false;
     cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
     if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return fail(h, IB_ERR_CUDA, "step capture", e); }
     if (e2 != cudaSuccess) return fail(h, IB_ERR_CUDA, "step capture", e2);
@@ -1588,6 +1593,7 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     if (v >= 1) h->coarse_from = v;
   }
   if (const char* env = std::getenv("IBGB300_NO_GRAPH")) h->use_graph = !(env[0] == '1');
+  if (const char* env = std::getenv("IBGB300_PDL")) h->use_pdl = env[0] != '0';
   // mixed precision with two sweeps: the trial Crank-Nicolson solve starts from Gamma_n (two
   // FP32 transform solves instead of three; IBGB300_CN_PREDICTOR=0 keeps three)
   h->cn_pred = h->refine >= 2;

@@ -61,6 +61,7 @@ __device__ __forceinline__ T ring_value(const Geometry& g, const T* __restrict__
 
 template <typename T>
 __global__ void k_get_bc(Geometry g, const T* __restrict__ r, T* __restrict__ bc, int batch, T extra) {
+  pdl_begin();
   const int64_t total = (int64_t)batch * g.nbc;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int b = (int)(t / g.nbc), idx = (int)(t - (int64_t)b * g.nbc);
@@ -71,6 +72,7 @@ __global__ void k_get_bc(Geometry g, const T* __restrict__ r, T* __restrict__ bc
 // apply_bc! (fluid-ops.jl:249-275): rows first, then columns (same order as the reference).
 template <typename T>
 __global__ void k_apply_bc_rows(Geometry g, T* __restrict__ r, const T* __restrict__ bc, T fac, int batch) {
+  pdl_begin();
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int64_t total = (int64_t)batch * ncol;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -83,6 +85,7 @@ __global__ void k_apply_bc_rows(Geometry g, T* __restrict__ r, const T* __restri
 }
 template <typename T>
 __global__ void k_apply_bc_cols(Geometry g, T* __restrict__ r, const T* __restrict__ bc, T fac, int batch) {
+  pdl_begin();
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int64_t total = (int64_t)batch * nrow;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
@@ -97,6 +100,7 @@ __global__ void k_apply_bc_cols(Geometry g, T* __restrict__ r, const T* __restri
 // coarsify! (fluid-ops.jl:184-202)
 template <typename T>
 __global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__ gf, int batch, int64_t stride) {
+  pdl_begin();
   const int ncol = g.nx - 1;
   const int ct = g.nx / 2 - 1, cs = g.ny / 2 - 1;  // coarse centre extent
   const int64_t per = (int64_t)ct * cs;
@@ -120,6 +124,7 @@ __global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__
 // an element's indices need no division.
 template <typename T>
 __global__ void k_curl(Geometry g, const T* __restrict__ psi, const T* __restrict__ bc, T* __restrict__ q, int batch) {
+  pdl_begin();
   const int nx = g.nx, ny = g.ny, ncol = nx - 1;
   const int rows = 2 * ny + 1;
   const int b = blockIdx.y / rows, row = blockIdx.y - b * rows;
@@ -208,6 +213,7 @@ __device__ __forceinline__ T fqy_at(const Geometry& g, const LevelView<T>& v, in
 constexpr int kNTX = 32, kNTY = 8;
 template <typename T>
 __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinArgs<T> a) {
+  pdl_begin();
   __shared__ T sQy[kNTY + 2][kNTX];   // Qy(J0 + r, I0 + 1 + c)
   __shared__ T sQx[kNTY][kNTX + 2];   // Qx(J0 + 1 + r, I0 + c)
   __shared__ T sFx[kNTY + 1][kNTX];   // fqx(J0 + r, I0 + 1 + c)
@@ -299,6 +305,7 @@ __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinAr
 template <typename T>
 __global__ void k_trial_rings(Geometry g, const T* __restrict__ gamma, T* __restrict__ bcn, T* __restrict__ edges,
                               const double* __restrict__ fac) {
+  pdl_begin();
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int ne = 2 * ncol + 2 * nrow;
   const int nl = g.nlev;
@@ -329,6 +336,7 @@ __global__ void k_fill(T* p, T v, int64_t n) {
 }
 template <typename T>
 __global__ void k_axpby(T* y, const T* x, T a, T b, int64_t n) {
+  pdl_begin();
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
     y[t] = a * x[t] + b * y[t];
 }
@@ -337,19 +345,17 @@ __global__ void k_axpby(T* y, const T* x, T a, T b, int64_t n) {
 
 template <typename T>
 cudaError_t get_bc(const Geometry& g, const T* r, T* bc, int batch, T extra, cudaStream_t s) {
-  k_get_bc<T><<<blocks_for((int64_t)batch * g.nbc), kThreads, 0, s>>>(g, r, bc, batch, extra);
-  return cudaGetLastError();
+  return launch_k(k_get_bc<T>, dim3(blocks_for((int64_t)batch * g.nbc)), dim3(kThreads), 0, s, g, r, bc, batch, extra);
 }
 template <typename T>
 cudaError_t apply_bc(const Geometry& g, T* r, const T* bc, T fac, int batch, cudaStream_t s) {
-  k_apply_bc_rows<T><<<blocks_for((int64_t)batch * (g.nx - 1)), kThreads, 0, s>>>(g, r, bc, fac, batch);
-  k_apply_bc_cols<T><<<blocks_for((int64_t)batch * (g.ny - 1)), kThreads, 0, s>>>(g, r, bc, fac, batch);
-  return cudaGetLastError();
+  cudaError_t e = launch_k(k_apply_bc_rows<T>, dim3(blocks_for((int64_t)batch * (g.nx - 1))), dim3(kThreads), 0, s, g, r, bc, fac, batch);
+  if (e != cudaSuccess) return e;
+  return launch_k(k_apply_bc_cols<T>, dim3(blocks_for((int64_t)batch * (g.ny - 1))), dim3(kThreads), 0, s, g, r, bc, fac, batch);
 }
 template <typename T>
 cudaError_t coarsify(const Geometry& g, T* gc, const T* gf, int batch, int64_t stride, cudaStream_t s) {
-  k_coarsify<T><<<blocks_for((int64_t)batch * (g.nx / 2 - 1) * (g.ny / 2 - 1)), kThreads, 0, s>>>(g, gc, gf, batch, stride);
-  return cudaGetLastError();
+  return launch_k(k_coarsify<T>, dim3(blocks_for((int64_t)batch * (g.nx / 2 - 1) * (g.ny / 2 - 1))), dim3(kThreads), 0, s, g, gc, gf, batch, stride);
 }
 template <typename T>
 cudaError_t curl(const Geometry& g, const T* psi, const T* bc, T* q, int batch, cudaStream_t s) {
@@ -363,8 +369,7 @@ cudaError_t curl(const Geometry& g, const T* psi, const T* bc, T* q, int batch, 
     return cudaSuccess;
   }
   const dim3 grid((g.nx + 1 + kThreads - 1) / kThreads, (unsigned)rows);
-  k_curl<T><<<grid, kThreads, 0, s>>>(g, psi, bc, q, batch);
-  return cudaGetLastError();
+  return launch_k(k_curl<T>, grid, dim3(kThreads), 0, s, g, psi, bc, q, batch);
 }
 template <typename T>
 cudaError_t rot(const Geometry& g, const T* q, T* gam, int batch, cudaStream_t s) {
@@ -375,14 +380,12 @@ template <typename T>
 cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s) {
   ProfScope prof(kClassNonlin, s);
   const int tiles = g.nlev * ((g.nx - 1 + kNTX - 1) / kNTX) * ((g.ny - 1 + kNTY - 1) / kNTY);
-  k_nonlin_rhs<T><<<tiles < 65535 * 8 ? tiles : 65535 * 8, kNTX * kNTY, 0, s>>>(g, a);
-  return cudaGetLastError();
+  return launch_k(k_nonlin_rhs<T>, dim3(tiles < 65535 * 8 ? tiles : 65535 * 8), dim3(kNTX * kNTY), 0, s, g, a);
 }
 template <typename T>
 cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac, cudaStream_t s) {
   const int64_t n = (int64_t)g.nlev * g.nbc + (int64_t)g.nlev * (2 * (g.nx - 1) + 2 * (g.ny - 1));
-  k_trial_rings<T><<<blocks_for(n), kThreads, 0, s>>>(g, gamma, bcn, edges, fac);
-  return cudaGetLastError();
+  return launch_k(k_trial_rings<T>, dim3(blocks_for(n)), dim3(kThreads), 0, s, g, gamma, bcn, edges, fac);
 }
 template <typename T>
 cudaError_t fill(T* p, T v, int64_t n, cudaStream_t s) {
@@ -391,8 +394,7 @@ cudaError_t fill(T* p, T v, int64_t n, cudaStream_t s) {
 }
 template <typename T>
 cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s) {
-  k_axpby<T><<<blocks_for(n), kThreads, 0, s>>>(y, x, a, b, n);
-  return cudaGetLastError();
+  return launch_k(k_axpby<T>, dim3(blocks_for(n)), dim3(kThreads), 0, s, y, x, a, b, n);
 }
 
 #define IB_INST(T)                                                                                   \

@@ -64,6 +64,7 @@ __device__ __forceinline__ void load_line(float* U, const float* src, int nrow, 
 template <int P>
 __global__ void __launch_bounds__(kLines * 32)
 k_wy_spec(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, float* vrow) {
+  pdl_begin();
   using Sh = Shape<float, P, 32>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wi = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -113,6 +114,7 @@ template <int P>
 __global__ void __launch_bounds__(kLines * 32)
 k_wy_ring(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, const float* sidex, const float* sidey,
           const float* sinx, const float* siny) {
+  pdl_begin();
   using Sh = Shape<float, P, 32>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wi = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -164,6 +166,7 @@ k_wy_ring(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, co
 //   ucolp[b][s][c][l] = sum_{k in chunk c} sin(pi (k+1)(I_s+1)/nx) spec[b][k][l]
 constexpr int kColChunk = 32;  // k per thread
 __global__ void k_colsum(Geometry g, const float* __restrict__ w, int batch, int nchunk, float* __restrict__ ucolp) {
+  pdl_begin();
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int l = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y % nchunk, b = blockIdx.y / nchunk;
@@ -190,6 +193,7 @@ __global__ void k_colsum(Geometry g, const float* __restrict__ w, int batch, int
 
 // ucol[t][l] = sum_c ucolp[t][c][l] in chunk order, t = 2 b + s
 __global__ void k_colred(int nlines, int nchunk, int nrow, const float* __restrict__ ucolp, float* __restrict__ ucol) {
+  pdl_begin();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nlines * nrow) return;
   const int t = (int)(i / nrow), l = (int)(i - (int64_t)t * nrow);
@@ -212,6 +216,7 @@ template <int P>
 __global__ void __launch_bounds__(kLines * 32)
 k_lines(DstAxis<float> ax, const float* in, int64_t in_b, int64_t in_s, float* out, int64_t out_b, int64_t out_s,
         int nlines) {
+  pdl_begin();
   using Sh = Shape<float, P, 32>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int wi = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -242,6 +247,7 @@ k_ring_eval(Geometry g, const int4* __restrict__ pts, const df64* __restrict__ x
             const float* __restrict__ qline, const double* __restrict__ AringT, const double* __restrict__ coef,
             int nK, double* __restrict__ dd, df64* __restrict__ dring, df64* __restrict__ ring,
             float* __restrict__ sidex, float* __restrict__ sidey) {
+  pdl_begin();
   __shared__ double part[kEvalWarps][32];
   const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int idx = blockIdx.x * 32 + lane;
@@ -295,6 +301,7 @@ constexpr int kCoefThreads = 256;
 __global__ void __launch_bounds__(kCoefThreads)
 k_ring_coef(Geometry g, const double* __restrict__ ringd, const double* __restrict__ St, int Kx, int Ky,
             double* __restrict__ coef) {
+  pdl_begin();
   __shared__ double red[kCoefThreads];
   const int j = blockIdx.x, tid = threadIdx.x;
   const int nK = 2 * Kx + 2 * Ky;
@@ -365,13 +372,19 @@ int modes_kept(int n, int d) {
 
 }  // namespace
 
+#define CE_V(x)                      \
+  do {                               \
+    cudaError_t e_ = (x);            \
+    if (e_ != cudaSuccess) return e_; \
+  } while (0)
+
 template <int P>
 static cudaError_t launch_lines_p(const DstAxis<float>& ax, const float* in, int64_t in_b, int64_t in_s, float* out,
                                   int64_t out_b, int64_t out_s, int nlines, cudaStream_t s) {
   const size_t smem = line_smem<P>();
   cudaError_t e = set_smem_limit((const void*)k_lines<P>, smem);
   if (e != cudaSuccess) return e;
-  k_lines<P><<<(nlines + kLines - 1) / kLines, kLines * 32, smem, s>>>(ax, in, in_b, in_s, out, out_b, out_s, nlines);
+  CE_V(launch_k(k_lines<P>, dim3((nlines + kLines - 1) / kLines), dim3(kLines * 32), smem, s, ax, in, in_b, in_s, out, out_b, out_s, nlines));
   return cudaGetLastError();
 }
 
@@ -402,7 +415,7 @@ cudaError_t v2f_yspec(const Geometry& g, const DstAxis<float>& ax, float* w, con
     const size_t smem = line_smem<P>();                                                  \
     cudaError_t e = set_smem_limit((const void*)k_wy_spec<P>, smem);                     \
     if (e != cudaSuccess) return e;                                                      \
-    k_wy_spec<P><<<blocks, kLines * 32, smem, s>>>(g, ax, w, m, batch, vrow);            \
+    CE_V(launch_k(k_wy_spec<P>, dim3(blocks), dim3(kLines * 32), smem, s, g, ax, w, m, batch, vrow));            \
     return cudaGetLastError();                                                           \
   }
     IB_V2F_P(IB_C)
@@ -422,7 +435,7 @@ cudaError_t v2f_yring(const Geometry& g, const DstAxis<float>& axy, const DstAxi
     const size_t smem = line_smem<P>();                                                                   \
     cudaError_t e = set_smem_limit((const void*)k_wy_ring<P>, smem);                                      \
     if (e != cudaSuccess) return e;                                                                       \
-    k_wy_ring<P><<<blocks, kLines * 32, smem, s>>>(g, axy, w, m, batch, sidex, sidey, axx.sintab, axy.sintab); \
+    CE_V(launch_k(k_wy_ring<P>, dim3(blocks), dim3(kLines * 32), smem, s, g, axy, w, m, batch, sidex, sidey, axx.sintab, axy.sintab)); \
     return cudaGetLastError();                                                                            \
   }
     IB_V2F_P(IB_C)
@@ -435,11 +448,11 @@ cudaError_t v2f_yring(const Geometry& g, const DstAxis<float>& axy, const DstAxi
 cudaError_t v2f_colsum(const Geometry& g, const RingPlan& rp, const float* w, int batch, cudaStream_t s) {
   const int nrow = g.ny - 1;
   dim3 grid((nrow + 127) / 128, batch * rp.nchunk);
-  k_colsum<<<grid, 128, 0, s>>>(g, w, batch, rp.nchunk, rp.ucolp);
+  CE_V(launch_k(k_colsum, grid, dim3(128), 0, s, g, w, batch, rp.nchunk, rp.ucolp));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int64_t n = (int64_t)2 * batch * nrow;
-  k_colred<<<(int)((n + 255) / 256), 256, 0, s>>>(2 * batch, rp.nchunk, nrow, rp.ucolp, rp.ucol);
+  CE_V(launch_k(k_colred, dim3((int)((n + 255) / 256)), dim3(256), 0, s, 2 * batch, rp.nchunk, nrow, rp.ucolp, rp.ucol));
   return cudaGetLastError();
 }
 
@@ -447,18 +460,15 @@ cudaError_t v2f_ring_eval(const Geometry& g, const RingPlan& rp, int l, const df
                           df64* ring_l, cudaStream_t s) {
   const int up = l + 1;
   const double* coef = (up < g.nlev - 1) ? rp.coef + (int64_t)up * rp.nK : nullptr;
-  k_ring_eval<<<(g.nbc + 31) / 32, kEvalWarps * 32, 0, s>>>(g, rp.pts, xp_up, x0_up, rp.qline + (int64_t)up * rp.qls, rp.Aring, coef, rp.nK,
-                                               rp.ringd + (int64_t)l * g.nbc,
-                                               reinterpret_cast<df64*>(rp.dring) + (int64_t)l * g.nbc, ring_l,
-                                               rp.sidex + (int64_t)l * 2 * (g.nx - 1),
-                                               rp.sidey + (int64_t)l * 2 * (g.ny - 1));
-  return cudaGetLastError();
+  return launch_k(k_ring_eval, dim3((g.nbc + 31) / 32), dim3(kEvalWarps * 32), 0, s, g, (const int4*)rp.pts, xp_up,
+                  x0_up, (const float*)(rp.qline + (int64_t)up * rp.qls), (const double*)rp.Aring, coef, rp.nK,
+                  rp.ringd + (int64_t)l * g.nbc, reinterpret_cast<df64*>(rp.dring) + (int64_t)l * g.nbc, ring_l,
+                  rp.sidex + (int64_t)l * 2 * (g.nx - 1), rp.sidey + (int64_t)l * 2 * (g.ny - 1));
 }
 
 cudaError_t v2f_ring_coef(const Geometry& g, const RingPlan& rp, int l, cudaStream_t s) {
-  k_ring_coef<<<rp.nK, kCoefThreads, 0, s>>>(g, rp.ringd + (int64_t)l * g.nbc, rp.St, rp.Kx, rp.Ky,
-                                               rp.coef + (int64_t)l * rp.nK);
-  return cudaGetLastError();
+  return launch_k(k_ring_coef, dim3(rp.nK), dim3(kCoefThreads), 0, s, g, (const double*)(rp.ringd + (int64_t)l * g.nbc),
+                  (const double*)rp.St, rp.Kx, rp.Ky, rp.coef + (int64_t)l * rp.nK);
 }
 
 // Host tables: truncation, St, Aring and the quarter-line nodes of each ring entry.

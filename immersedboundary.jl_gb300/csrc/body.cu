@@ -266,13 +266,19 @@ cudaError_t reg_scatter(const Geometry& g, const double* f, const int* body_idx,
 
 // rot(E^T f): the scatter covers only the faces inside the box of the windows (box: 4 ints of
 // device scratch, or nullptr for the whole flux domain), the rot reads only those
+cudaError_t body_box(const Geometry& g, const int* body_idx, int nb, int* box, cudaStream_t s) {
+  if (nb <= 0) return cudaSuccess;
+  return launch_k(k_body_box, dim3(1), dim3(256), 0, s, g, body_idx, nb, box);
+}
+
 template <typename T>
 cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_idx, const double* weight, int nb,
-                            T* qtmp, T* gam, int ncols, int64_t fstride, int* status, int* box, cudaStream_t s) {
+                            T* qtmp, T* gam, int ncols, int64_t fstride, int* status, int* box, bool box_ready,
+                            cudaStream_t s) {
   (void)ncols;
   (void)fstride;
   if (box && nb > 0) {
-    cudaError_t e = launch_k(k_body_box, dim3(1), dim3(256), 0, s, g, body_idx, nb, box);
+    cudaError_t e = box_ready ? cudaSuccess : body_box(g, body_idx, nb, box, s);
     if (e != cudaSuccess) return e;
     const int tx = (g.nx + 1 + kTile - 1) / kTile, ty = (g.ny + 1 + kTile - 1) / kTile;
     e = launch_k(k_reg_scatter_tiles<T>, dim3(2 * tx * ty), dim3(256), 0, s, g, f, body_idx, weight, nb, qtmp, 0, 0, tx, ty, status,
@@ -313,9 +319,9 @@ template cudaError_t reg_scatter<double>(const Geometry&, const double*, const i
 template cudaError_t reg_scatter<df64>(const Geometry&, const double*, const int*, const double*, int, df64*, int*,
                                         cudaStream_t);
 template cudaError_t reg_scatter_rot<double>(const Geometry&, const double*, const int*, const double*, int, double*,
-                                             double*, int, int64_t, int*, int*, cudaStream_t);
+                                             double*, int, int64_t, int*, int*, bool, cudaStream_t);
 template cudaError_t reg_scatter_rot<df64>(const Geometry&, const double*, const int*, const double*, int, df64*,
-                                            df64*, int, int64_t, int*, int*, cudaStream_t);
+                                            df64*, int, int64_t, int*, int*, bool, cudaStream_t);
 template cudaError_t unit_scatter_rot<double>(const Geometry&, const int*, const double*, int, int, int, double*,
                                               cudaStream_t);
 template cudaError_t unit_scatter_rot<df64>(const Geometry&, const int*, const double*, int, int, int, df64*,

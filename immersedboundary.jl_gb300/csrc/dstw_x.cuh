@@ -272,6 +272,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const float* bs2 = a.base2 ? a.base2 + off : nullptr;
         constexpr bool kF = EPI == kEpiSubAddBase || EPI == kEpiAddTo;
         const df64* sf = kF ? static_cast<const df64*>(a.sub_from) + off : nullptr;
+        df64* s2 = (EPI == kEpiAddTo && a.sub2) ? static_cast<df64*>(a.sub2) + off : nullptr;
         constexpr int R = 8;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
@@ -290,7 +291,9 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
             if (I >= ncol) break;
             const df64 x01 = two_sum(b0[u], b1[u]);
             const df64 xv = two_sum(x01.hi, x01.lo + (float)U[I + 1]);
-            dst[I] = (EPI == kEpiSubAddBase) ? add_sloppy(f[u], -xv) : (EPI == kEpiAddTo) ? add_sloppy(f[u], xv) : xv;
+            const df64 y = (EPI == kEpiSubAddBase) ? add_sloppy(f[u], -xv) : (EPI == kEpiAddTo) ? add_sloppy(f[u], xv) : xv;
+            dst[I] = y;
+            if (EPI == kEpiAddTo && s2) s2[I] = add_sloppy(s2[I], -y);
           }
         }
       } else {

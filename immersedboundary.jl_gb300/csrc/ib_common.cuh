@@ -135,6 +135,7 @@ struct XArgs {
   int mstep;
   int pro, epi;
   void* resid_out;          // optional (warp passes, float-float input): the residual itself, float-float
+  void* sub2;               // optional with kEpiAddTo (warp passes): sub2 -= out as well, float-float
 };
 
 template <typename T, typename Tin, typename Tout>
@@ -271,12 +272,15 @@ cudaError_t reg_gather(const Geometry& g, const T* q, const double* q0, const in
                        const double* weight, int nb, double* fb, int ncols, int64_t qstride,
                        int64_t fstride, cudaStream_t s);
 // E^T followed by rot: gamma_out = rot(E^T f) (whole array written).  With box (4 ints of
-// device scratch) the scatter and the rot's reads cover only the face box of the points'
-// windows (found on the device first), and qtmp is left unwritten outside it.
+// device memory) the scatter and the rot's reads cover only the face box of the points'
+// windows, and qtmp is left unwritten outside it; the box is found on the device first unless
+// box_ready (it already holds body_box of the current points).
 template <typename T>
 cudaError_t reg_scatter_rot(const Geometry& g, const double* f, const int* body_idx,
                             const double* weight, int nb, T* qtmp, T* gam, int ncols,
-                            int64_t fstride, int* status, int* box, cudaStream_t s);
+                            int64_t fstride, int* status, int* box, bool box_ready, cudaStream_t s);
+// box = {i_lo, i_hi, j_lo, j_hi}: the flux faces every point's 13x13 window covers
+cudaError_t body_box(const Geometry& g, const int* body_idx, int nb, int* box, cudaStream_t s);
 // E^T alone (operator test entry point)
 template <typename T>
 cudaError_t reg_scatter(const Geometry& g, const double* f, const int* body_idx, const double* weight,

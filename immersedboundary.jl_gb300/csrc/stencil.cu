@@ -103,11 +103,11 @@ __global__ void k_coarsify(Geometry g, T* __restrict__ gc, const T* __restrict__
   pdl_begin();
   const int ncol = g.nx - 1;
   const int ct = g.nx / 2 - 1, cs = g.ny / 2 - 1;  // coarse centre extent
-  const int64_t per = (int64_t)ct * cs;
-  const int64_t total = (int64_t)batch * per;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)(t / per);
-    const int rem = (int)(t - (int64_t)b * per);
+  const int per = ct * cs;  // batch * per < 2^31 (batch <= 64 slots of at most 4095^2 / 4 values)
+  const int total = batch * per;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int b = t / per;
+    const int rem = t - b * per;
     const int s = rem / ct, tt = rem - s * ct;
     const T* f = gf + (int64_t)b * stride;
     const int J = 2 * s + 1, I = 2 * tt + 1;

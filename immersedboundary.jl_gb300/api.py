@@ -480,15 +480,19 @@ class Solver:
 
     def autotune(self) -> dict:
         """The setup-time autotuner's measurements: device ms of its timed unit per candidate
-        ``"<form>/<order>"`` (form: stockham, warp or tensor; order: levels or sequential) and
-        the candidate in effect (``None`` if the tuner did not run)."""
-        ms = np.zeros(6)
+        ``"<form>/<order>[/y8]"`` (form: stockham, warp or tensor; order: levels or sequential;
+        ``/y8``: the warp y pass compiled for 8 resident blocks per SM) and the candidate in
+        effect (``None`` if the tuner did not run)."""
+        ms = np.zeros(12)
         ch = C.c_int32()
         self._check(self.lib.ib_get_autotune(self.handle, _lib.dptr(ms), C.byref(ch)))
-        out = {f"{self._FORMS[i // 2]}/{'levels' if i % 2 else 'sequential'}": float(ms[i])
-               for i in range(6) if ms[i] > 0}
+
+        def name(i):
+            return (f"{self._FORMS[i // 4]}/{'levels' if (i // 2) % 2 else 'sequential'}"
+                    + ("/y8" if i % 2 else ""))
+        out = {name(i): float(ms[i]) for i in range(12) if ms[i] > 0}
         c = ch.value
-        return {"ms": out, "chosen": None if c < 0 else f"{self._FORMS[c // 2]}/{'levels' if c % 2 else 'sequential'}"}
+        return {"ms": out, "chosen": None if c < 0 else name(c)}
 
     def stress(self):
         nbd = max(self.nbodies, 1)

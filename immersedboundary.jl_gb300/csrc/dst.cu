@@ -463,6 +463,7 @@ cudaError_t AxisTables<T>::build(int n) {
   }
   d.wP = P;
   d.wNL = NL;
+  d.wMinB = IB_WDST_YMINB;
   const int G = !P ? 1 : (NL % P == 0 ? NL / P : 32);
   int lg = 0;
   while ((1 << lg) < G) ++lg;

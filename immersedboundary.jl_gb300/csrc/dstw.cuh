@@ -31,16 +31,7 @@ constexpr unsigned kFull = 0xffffffffu;
 #define IB_WDST_LINES 4
 #endif
 constexpr int kLines = IB_WDST_LINES;  // lines per block
-// Resident blocks per SM the x / y pass kernels are compiled for, which caps their registers
-// (x: 128 per thread, y: 85).  By measurement on GB300 (mixed step, device time): 1.355 ms per
-// 1024^2 x 4 step and 0.541 ms per 512^2 x 4 step with (4, 6), against 1.405 / 0.587 uncapped
-// (the residual x pass then used 168 registers, 3 blocks per SM) and 1.477 / 0.565 with x at 5.
-#ifndef IB_WDST_XMINB
-#define IB_WDST_XMINB 4
-#endif
-#ifndef IB_WDST_YMINB
-#define IB_WDST_YMINB 6
-#endif
+// resident blocks per SM of the pass kernels: IB_WDST_XMINB / IB_WDST_YMINB (ib_common.cuh)
 
 // (lanes per line, values per lane) pairs with compiled passes: one warp per line, or two
 // (IBGB300_LINE_LANES=64, axes with M = 64 P, P = 2..16)

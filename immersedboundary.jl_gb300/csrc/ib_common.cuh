@@ -14,6 +14,18 @@
 #include <string>
 #include <vector>
 
+// Resident blocks per SM the x / y pass kernels are compiled for, which caps their registers
+// (x: 128 per thread, y: 85).  By measurement on GB300 (mixed step, device time): 1.355 ms per
+// 1024^2 x 4 step and 0.541 ms per 512^2 x 4 step with (4, 6), against 1.405 / 0.587 uncapped
+// (the residual x pass then used 168 registers, 3 blocks per SM) and 1.477 / 0.565 with x at 5.
+#ifndef IB_WDST_XMINB
+#define IB_WDST_XMINB 4
+#endif
+#ifndef IB_WDST_YMINB
+#define IB_WDST_YMINB 6
+#endif
+// (the y pass is also compiled for 8 blocks per SM; the autotuner may choose it per grid)
+
 namespace ib {
 
 // ----------------------------------------------------------------------------------------------
@@ -53,6 +65,7 @@ template <typename T> struct DstAxis {
   // wP = 0 for axes without them.  Tables in lane order (entry [s][lane] at s*wNL + lane),
   // G = wNL / wP (or 32 when wP does not divide wNL):
   int wP, wNL;
+  int wMinB;                // y pass: resident blocks per SM of the compiled variant to use
   const c2_t<T>* wtw1;      // [wP][wNL]     e^{-2 pi i lane a / M}
   const c2_t<T>* wtw2;      // [wP][wNL]     e^{-2 pi i (lane mod G) c / wNL}
   const c2_t<T>* wtw3;      // [log2 G][wNL] radix-2 twiddles of the cross-lane stages

@@ -133,8 +133,8 @@ struct ib_handle {
   bool v2f_ok = false, v2f_auto = false;  // the grid allows it / the size rule picks it
   RingPlan rplan;
   // setup-time autotuner: modelled step time of each candidate (form * 2 + levels order), ms;
-  // -1 where not tried
-  double tune_ms[6] = {-1, -1, -1, -1, -1, -1};
+  // -1 where not tried; index (form * 2 + levels) * 2 + (y pass at 8 blocks per SM)
+  double tune_ms[12] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
   bool tuned = false;
   double pc_excess_iters = 0.0;                   // iterations above the base since then
   double cg_iter_s = 0.0;                         // measured time of one CG iteration (running mean)
@@ -1316,7 +1316,7 @@ double tune_time(ib_handle* h, double* gam, double* psi, double* q, double* q1, 
 // handle of one shape in a process (an ensemble member and the same problem stepped alone, say)
 // takes the same choice and gives the same bits.
 struct TuneRecord {
-  double ms[6];
+  double ms[12];
   int best;
 };
 std::mutex g_tune_mu;
@@ -1360,7 +1360,7 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
     return fail(h, IB_ERR_CUDA, "autotuner scratch allocation");
   }
   const bool wdst0 = h->wdst, gdst0 = h->gdst, lv0 = h->v2f_levels;
-  struct Cand { int form; bool levels; };
+  struct Cand { int form; bool levels; bool yalt; };
   std::vector<Cand> cands;
   std::vector<int> forms;
   if (tune_form) {
@@ -1372,17 +1372,21 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
   }
   for (int f : forms) {
     const bool lv_ok = mixed && lv_base && f == IB_FORM_WARP;
-    if (tune_v2f) {
-      cands.push_back({f, false});
-      if (lv_ok) cands.push_back({f, true});
-    } else {
-      cands.push_back({f, lv0 && lv_ok});
+    // the warp y pass has a second compiled occupancy (8 blocks per SM) to try
+    const int ny_alt = (mixed && f == IB_FORM_WARP && IB_WDST_YMINB != 8) ? 2 : 1;
+    for (int ya = 0; ya < ny_alt; ++ya) {
+      if (tune_v2f) {
+        cands.push_back({f, false, ya == 1});
+        if (lv_ok) cands.push_back({f, true, ya == 1});
+      } else {
+        cands.push_back({f, lv0 && lv_ok, ya == 1});
+      }
     }
   }
   bool need_tc = false, need_lv = false;
   if (hit != g_tune_cache.end()) {
-    need_tc = hit->second.best / 2 == IB_FORM_TENSOR;
-    need_lv = (hit->second.best & 1) != 0;
+    need_tc = hit->second.best / 4 == IB_FORM_TENSOR;
+    need_lv = (hit->second.best / 2) % 2 != 0;
   } else {
     for (const Cand& c : cands) {
       need_tc |= c.form == IB_FORM_TENSOR;
@@ -1413,7 +1417,7 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
   double best_ms = -1.0;
   if (hit != g_tune_cache.end()) {
     best = hit->second.best;
-    for (int i = 0; i < 6; ++i) h->tune_ms[i] = hit->second.ms[i];
+    for (int i = 0; i < 12; ++i) h->tune_ms[i] = hit->second.ms[i];
   } else {
     // two interleaved rounds (so a clock ramp or a neighbour's burst does not favour one
     // candidate), the fastest run of each candidate counts
@@ -1422,13 +1426,14 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
         h->wdst = c.form == IB_FORM_WARP;
         h->gdst = c.form == IB_FORM_TENSOR;
         h->v2f_levels = c.levels;
+        h->axy32.d.wMinB = c.yalt ? 8 : IB_WDST_YMINB;
         const double ms = tune_time(h, gam, psi, q, q1, rings, in, out);
-        const int idx = c.form * 2 + (c.levels ? 1 : 0);
+        const int idx = (c.form * 2 + (c.levels ? 1 : 0)) * 2 + (c.yalt ? 1 : 0);
         if (ms > 0 && (h->tune_ms[idx] < 0 || ms < h->tune_ms[idx])) h->tune_ms[idx] = ms;
       }
     // the fastest, unless the size rule's choice is within 2% of it (timing noise)
-    const int rule = (gdst0 ? IB_FORM_TENSOR : (wdst0 ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 + (lv0 ? 1 : 0);
-    for (int i = 0; i < 6; ++i)
+    const int rule = ((gdst0 ? IB_FORM_TENSOR : (wdst0 ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 + (lv0 ? 1 : 0)) * 2;
+    for (int i = 0; i < 12; ++i)
       if (h->tune_ms[i] > 0 && (best < 0 || h->tune_ms[i] < best_ms)) {
         best = i;
         best_ms = h->tune_ms[i];
@@ -1436,7 +1441,7 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
     if (best >= 0 && h->tune_ms[rule] > 0 && h->tune_ms[rule] <= 1.02 * best_ms) best = rule;
     if (best >= 0) {
       TuneRecord rec;
-      for (int i = 0; i < 6; ++i) rec.ms[i] = h->tune_ms[i];
+      for (int i = 0; i < 12; ++i) rec.ms[i] = h->tune_ms[i];
       rec.best = best;
       g_tune_cache[key] = rec;
     }
@@ -1446,10 +1451,12 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
     h->wdst = wdst0;
     h->gdst = gdst0;
     h->v2f_levels = lv0;
+    h->axy32.d.wMinB = IB_WDST_YMINB;
   } else {
-    h->wdst = best / 2 == IB_FORM_WARP;
-    h->gdst = best / 2 == IB_FORM_TENSOR;
-    h->v2f_levels = (best & 1) != 0;
+    h->wdst = best / 4 == IB_FORM_WARP;
+    h->gdst = best / 4 == IB_FORM_TENSOR;
+    h->v2f_levels = (best / 2) % 2 != 0;
+    h->axy32.d.wMinB = (best % 2) ? 8 : IB_WDST_YMINB;
   }
   // keep what the choice uses: the tensor-core tables and work array, the ring-transfer plan
   if (tc_own && !h->gdst) {
@@ -2091,9 +2098,10 @@ int ib_get_info(ib_handle* h, ib_info* info) {
 int ib_get_autotune(ib_handle* h, double* ms, int32_t* chosen) {
   if (!h) return IB_ERR_INVALID;
   if (ms)
-    for (int i = 0; i < 6; ++i) ms[i] = h->tune_ms[i];
+    for (int i = 0; i < 12; ++i) ms[i] = h->tune_ms[i];
   if (chosen)
-    *chosen = h->tuned ? (h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 + (h->v2f_levels ? 1 : 0)
+    *chosen = h->tuned ? ((h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 +
+                          (h->v2f_levels ? 1 : 0)) * 2 + (h->axy32.d.wMinB == 8 ? 1 : 0)
                        : -1;
   return IB_OK;
 }

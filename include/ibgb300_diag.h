@@ -30,13 +30,14 @@ typedef struct ib_info {
 
 int ib_get_info(ib_handle* h, ib_info* info);
 
-/* The setup-time autotuner's measurements: ms[form * 2 + levels] = device time of the timed unit
- * (the batched Crank-Nicolson solve of all levels, a projection solve, a full and a level-1
- * Vort2Flux) for transform form IB_FORM_* and Vort2Flux order (levels = 1: all levels in one
- * batch), -1 where the candidate was not tried; *chosen = the index in effect (-1 when the
- * tuner did not run: IBGB300_AUTOTUNE=0 or every choice pinned).  No counterpart in the
- * reference, whose FFTW plans are chosen by FFTW's own EXHAUSTIVE planner (fluid-ops.jl:25). */
-int ib_get_autotune(ib_handle* h, double* ms /* [6] */, int32_t* chosen);
+/* The setup-time autotuner's measurements: ms[(form * 2 + levels) * 2 + y8] = device time of the
+ * timed unit (the batched Crank-Nicolson solve of all levels, a projection solve, a full and a
+ * level-1 Vort2Flux) for transform form IB_FORM_*, Vort2Flux order (levels = 1: all levels in
+ * one batch) and warp y-pass occupancy (y8 = 1: the variant compiled for 8 resident blocks per
+ * SM), -1 where the candidate was not tried; *chosen = the index in effect (-1 when the tuner
+ * did not run: IBGB300_AUTOTUNE=0 or every choice pinned).  No counterpart in the reference,
+ * whose FFTW plans are chosen by FFTW's own EXHAUSTIVE planner (fluid-ops.jl:25). */
+int ib_get_autotune(ib_handle* h, double* ms /* [12] */, int32_t* chosen);
 
 /* ib_advance_n bracketed by CUDA events on the handle's stream: *device_ms is the device time
  * of the n steps (graph replays plus their per-step base-flux uploads) */

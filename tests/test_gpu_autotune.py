@@ -29,12 +29,15 @@ def test_choice_is_the_fastest_measured_and_in_effect(ib, lib):
     tune = s.autotune()
     assert tune["chosen"] is not None
     ms = tune["ms"]
-    # the warp passes in both orders, the Stockham passes and the tensor-core GEMMs were timed
-    assert {"warp/levels", "warp/sequential", "stockham/sequential", "tensor/sequential"} <= set(ms)
-    assert ms[tune["chosen"]] == min(ms.values())
+    # the warp passes in both orders and both y-pass occupancies, the Stockham passes and the
+    # tensor-core GEMMs were timed
+    assert {"warp/levels", "warp/sequential", "warp/levels/y8", "warp/sequential/y8", "stockham/sequential",
+            "tensor/sequential"} <= set(ms)
+    # the fastest, or the size rule's choice when it is within 2% of the fastest
+    assert ms[tune["chosen"]] <= 1.02 * min(ms.values())
     info = L.IbInfo()
     assert lib.ib_get_info(s.handle, ctypes.byref(info)) == 0
-    form, order = tune["chosen"].split("/")
+    form, order = tune["chosen"].split("/")[:2]
     assert info.transform_form == {"stockham": L.IB_FORM_STOCKHAM, "warp": L.IB_FORM_WARP,
                                    "tensor": L.IB_FORM_TENSOR}[form]
     assert info.vort2flux_order == (L.IB_V2F_LEVELS if order == "levels" else L.IB_V2F_SEQUENTIAL)

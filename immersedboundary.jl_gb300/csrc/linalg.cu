@@ -196,43 +196,54 @@ __global__ void __launch_bounds__(256) k_gj_update(double* __restrict__ A, int n
 
 }  // namespace
 
-// y = A x for row-major A with an even row length (16-byte aligned rows): one warp per row,
-// 16-byte loads and four independent partial sums per lane (more loads in flight per warp, as
-// the ~n / 32 warps of this launch fill only part of the GPU), combined in a fixed order.
+// y = A x for row-major A with an even row length (16-byte aligned rows): two warps per row,
+// each over one half of the row with 16-byte loads and four independent partial sums per lane
+// (more loads in flight than one warp per row gives, with ~n/16 warps for the whole GPU),
+// combined in a fixed order: lanes, then the two halves.
 __global__ void k_gemv_rm2(const double* __restrict__ A, const double* __restrict__ x, double* __restrict__ y, int n) {
   pdl_begin();
-  const int lane = threadIdx.x & 31;
-  const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (row >= n) return;
-  const double2* a = reinterpret_cast<const double2*>(A + row * (int64_t)n);
-  const double2* xv = reinterpret_cast<const double2*>(x);
+  __shared__ double part[4][2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;  // 4 warps: 2 rows x 2 halves
+  const int64_t row = (int64_t)blockIdx.x * 2 + (w >> 1);
+  const int half = w & 1;
   const int n2 = n / 2;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  int j = lane;
-  for (; j + 96 < n2; j += 128) {
+  const int h0 = half ? n2 / 2 : 0, h1 = half ? n2 : n2 / 2;  // double2 index range of this half
+  double t = 0.0;
+  if (row < n) {
+    const double2* a = reinterpret_cast<const double2*>(A + row * (int64_t)n);
+    const double2* xv = reinterpret_cast<const double2*>(x);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    int j = h0 + lane;
+    for (; j + 96 < h1; j += 128) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const double2 av = __ldg(&a[j + 32 * u]), xw = __ldg(&xv[j + 32 * u]);
-      acc[u] = fma(av.x, xw.x, acc[u]);
-      acc[u] = fma(av.y, xw.y, acc[u]);
+      for (int u = 0; u < 4; ++u) {
+        const double2 av = __ldg(&a[j + 32 * u]), xw = __ldg(&xv[j + 32 * u]);
+        acc[u] = fma(av.x, xw.x, acc[u]);
+        acc[u] = fma(av.y, xw.y, acc[u]);
+      }
     }
-  }
-  for (int u = 0; j < n2; j += 32, ++u) {
-    const double2 av = __ldg(&a[j]), xw = __ldg(&xv[j]);
-    acc[u & 3] = fma(av.x, xw.x, acc[u & 3]);
-    acc[u & 3] = fma(av.y, xw.y, acc[u & 3]);
-  }
-  double t = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+    for (int u = 0; j < h1; j += 32, ++u) {
+      const double2 av = __ldg(&a[j]), xw = __ldg(&xv[j]);
+      acc[u & 3] = fma(av.x, xw.x, acc[u & 3]);
+      acc[u & 3] = fma(av.y, xw.y, acc[u & 3]);
+    }
+    t = (acc[0] + acc[1]) + (acc[2] + acc[3]);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  if (lane == 0) y[row] = t;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  if (lane == 0) part[w >> 1][half] = t;
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    const int64_t r = (int64_t)blockIdx.x * 2 + threadIdx.x;
+    if (r < n) y[r] = part[threadIdx.x][0] + part[threadIdx.x][1];
+  }
 }
 
 cudaError_t gemv_rowmajor(const double* A, const double* x, double* y, int n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t threads = (int64_t)n * 32;
   if (n % 2 == 0 && ((uintptr_t)A % 16) == 0 && ((uintptr_t)x % 16) == 0) {
-    return launch_k(k_gemv_rm2, dim3((int)((threads + 127) / 128)), dim3(128), 0, s, A, x, y, n);
+    return launch_k(k_gemv_rm2, dim3((n + 1) / 2), dim3(128), 0, s, A, x, y, n);
   }
   k_gemv_rm<<<(int)((threads + 255) / 256), 256, 0, s>>>(A, x, y, n);
   return cudaGetLastError();

@@ -62,7 +62,9 @@ __device__ __forceinline__ void load_line(float* U, const float* src, int nrow, 
 // y pass, spectrum only: S_y, multiply, store the spectrum in place, and the two quarter-row
 // sums of its inverse, vrow[b][s][k] = sum_l sin(pi (l+1)(J_s+1)/ny) spec[k][l].
 template <int P>
-__global__ void __launch_bounds__(kLines * 32)
+// 8 resident blocks per SM (64 registers), as the warp y pass the autotuner picks at the sizes
+// that use the all-levels Vort2Flux
+__global__ void __launch_bounds__(kLines * 32, 8)
 k_wy_spec(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, float* vrow) {
   pdl_begin();
   using Sh = Shape<float, P, 32>;
@@ -111,7 +113,7 @@ k_wy_spec(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, fl
 //   sin(pi (l+1)/ny) (Fb_k + (-1)^l Ft_k) + sin(pi (k+1)/nx) (Fl_l + (-1)^k Fr_l)
 // with Fb, Ft (Fl, Fr) the x (y) transforms of the bottom / top (left / right) ring sides.
 template <int P>
-__global__ void __launch_bounds__(kLines * 32)
+__global__ void __launch_bounds__(kLines * 32, 8)
 k_wy_ring(Geometry g, DstAxis<float> ax, float* w, const float* m, int batch, const float* sidex, const float* sidey,
           const float* sinx, const float* siny) {
   pdl_begin();

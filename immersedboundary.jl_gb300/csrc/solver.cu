@@ -1296,7 +1296,7 @@ double tune_time(ib_handle* h, double* gam, double* psi, double* q, double* q1, 
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return -1.0;
   double best = -1.0;
   bool ok = run() == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
-  for (int r = 0; ok && r < 3; ++r) {
+  for (int r = 0; ok && r < 5; ++r) {
     float ms = 0.0f;
     ok = cudaEventRecord(e0, s) == cudaSuccess && run() == cudaSuccess && cudaEventRecord(e1, s) == cudaSuccess &&
          cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess;
@@ -1419,9 +1419,9 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
     best = hit->second.best;
     for (int i = 0; i < 12; ++i) h->tune_ms[i] = hit->second.ms[i];
   } else {
-    // two interleaved rounds (so a clock ramp or a neighbour's burst does not favour one
-    // candidate), the fastest run of each candidate counts
-    for (int round = 0; round < 2; ++round)
+    // three interleaved rounds (so a clock ramp or a neighbour's burst does not favour one
+    // candidate), the fastest of each candidate's 15 runs counts
+    for (int round = 0; round < 3; ++round)
       for (const Cand& c : cands) {
         h->wdst = c.form == IB_FORM_WARP;
         h->gdst = c.form == IB_FORM_TENSOR;
@@ -1431,14 +1431,14 @@ int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
         const int idx = (c.form * 2 + (c.levels ? 1 : 0)) * 2 + (c.yalt ? 1 : 0);
         if (ms > 0 && (h->tune_ms[idx] < 0 || ms < h->tune_ms[idx])) h->tune_ms[idx] = ms;
       }
-    // the fastest, unless the size rule's choice is within 2% of it (timing noise)
+    // the fastest, unless the size rule's choice is within 1% of it (timing noise)
     const int rule = ((gdst0 ? IB_FORM_TENSOR : (wdst0 ? IB_FORM_WARP : IB_FORM_STOCKHAM)) * 2 + (lv0 ? 1 : 0)) * 2;
     for (int i = 0; i < 12; ++i)
       if (h->tune_ms[i] > 0 && (best < 0 || h->tune_ms[i] < best_ms)) {
         best = i;
         best_ms = h->tune_ms[i];
       }
-    if (best >= 0 && h->tune_ms[rule] > 0 && h->tune_ms[rule] <= 1.02 * best_ms) best = rule;
+    if (best >= 0 && h->tune_ms[rule] > 0 && h->tune_ms[rule] <= 1.01 * best_ms) best = rule;
     if (best >= 0) {
       TuneRecord rec;
       for (int i = 0; i < 12; ++i) rec.ms[i] = h->tune_ms[i];

@@ -1274,7 +1274,8 @@ int moving_step_mode(ib_handle* h, double t, double u, double v, const double* k
 // is the transform work a step repeats: the batched Crank-Nicolson solve over all levels, a
 // projection-size solve, a full Vort2Flux and a level-1-only Vort2Flux, run on scratch arrays
 // (the state is not touched); the stencil, body and Schur kernels are the same for every
-// candidate.  Each candidate runs once to warm up, then three times; the fastest run counts.
+// candidate.  Each candidate runs once to warm up, then five times in each of three rounds; the
+// fastest run counts.
 // IBGB300_DST / IBGB300_V2F pin a choice, IBGB300_AUTOTUNE=0 keeps the fixed size rules.
 template <typename S>
 cudaError_t tune_unit(ib_handle* h, double* gam, double* psi, double* q, double* q1, double* rings, double* in,

@@ -110,6 +110,8 @@ SIGNATURES = {
     "ib_get_schur": (C.c_int, [_vp, _dp, _dp]),
     # diagnostics
     "ib_get_info": (C.c_int, [_vp, C.POINTER(IbInfo)]),
+    "ib_checkpoint_save": (C.c_int, [_vp, C.c_char_p]),
+    "ib_checkpoint_load": (C.c_int, [_vp, C.c_char_p]),
     "ib_get_autotune": (C.c_int, [_vp, _dp, _ip]),
     "ib_advance_n_timed": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ib_profile_steps": (C.c_int, [_vp, C.c_int32, _dp, _dp, C.c_int32, _dp, C.POINTER(C.c_int64)]),

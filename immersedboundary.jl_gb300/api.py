@@ -31,6 +31,7 @@ lazily (only when a callback or the caller touches them).
 from __future__ import annotations
 
 import ctypes as C
+import os
 import math
 from dataclasses import dataclass
 from typing import Callable, Sequence
@@ -185,6 +186,22 @@ class StreamFcnFluid:
         u, v = (f(t) if callable(f) else f)
         return float(u), float(v)
 
+    def grid_flow(self, t: float):
+        """The uniform flow the base flux carries, in grid coordinates (``base_flux!``,
+        fluid-ops.jl:403-419).  LabFrame (or GridFrame) fluid: the freestream.  A fluid whose
+        grid translates with a ``RelativeFrame(LabFrame(), r, v, θ, Ω)`` (the reference's
+        "TODO: moving grid", :419): the freestream seen from the grid, U(t) - v(t); the grid
+        frame must not rotate (θ = Ω = 0), since a rotating grid would add fictitious terms the
+        scheme does not have."""
+        u, v = self.freestream(t)
+        fr = self.domain.frame
+        if isinstance(fr, RelativeFrame):
+            if fr.theta(t) != 0.0 or fr.omega(t) != 0.0:
+                raise NotImplementedError("a rotating grid frame is not supported (theta and Omega must be 0)")
+            gv = fr.v(t)
+            return u - float(gv[0]), v - float(gv[1])
+        return u, v
+
 
 # ---------------------------------------------------------------------------------------------
 # bodies (src/bodies)
@@ -276,7 +293,7 @@ def _base_flux(prob: Problem, t: float) -> np.ndarray:
     """``base_flux!`` (fluid-ops.jl:403-417) as a host array (nq x nlevels, column-major)."""
     d = prob.fluid.domain
     L = d.discrete.nlevels
-    u, v = prob.fluid.freestream(t)
+    u, v = prob.fluid.grid_flow(t)
     q0 = np.empty((L, d.nq))
     for lev in range(1, L + 1):
         hc = d.discrete.gridstep(lev)
@@ -407,8 +424,10 @@ class Solver:
                 raise NotImplementedError(f"unsupported body frame {type(b.frame).__name__}")
         # bodies in a RelativeFrame move rigidly (their xb are body-frame coordinates)
         self.moving = any(isinstance(b.frame, RelativeFrame) for b in prob.bodies)
-        if not isinstance(prob.fluid.domain.frame, LabFrame):
-            raise NotImplementedError("base_flux! is only defined for a LabFrame fluid")
+        fr = prob.fluid.domain.frame
+        if not isinstance(fr, (LabFrame, GridFrame)) and not (isinstance(fr, RelativeFrame)
+                                                             and isinstance(fr.base, LabFrame)):
+            raise NotImplementedError("the fluid frame must be LabFrame, GridFrame or a RelativeFrame of LabFrame")
         self.lib = _lib.load()
         self.prob = prob
         d = prob.fluid.domain
@@ -475,6 +494,22 @@ class Solver:
             self.handle, _lib.dptr(st._gamma), _lib.dptr(st._q), _lib.dptr(st._psi),
             _lib.dptr(st._nonlin[0]), _lib.dptr(st._nonlin[1]),
             _lib.dptr(st._fb) if st._fb.size else None, C.byref(t)))
+
+    def save_checkpoint(self, path) -> None:
+        """Write the state a restart needs (Gamma, q, psi, nonlin, Fb, t, step count) to a
+        checkpoint file (layout in include/ibgb300.h, ``ib_checkpoint_save``)."""
+        self._check(self.lib.ib_checkpoint_save(self.handle, os.fsencode(str(path))))
+
+    def load_checkpoint(self, path, state: "State | None" = None) -> None:
+        """Restore a checkpoint into this handle (same grid, levels, points and motion); the
+        bound state's host copies refresh from the device when next read."""
+        self._check(self.lib.ib_checkpoint_load(self.handle, os.fsencode(str(path))))
+        st = state if state is not None else getattr(self, "_bound_state", None)
+        if st is not None:
+            t = C.c_double()
+            self._check(self.lib.ib_get_state(self.handle, None, None, None, None, None, None, C.byref(t)))
+            st.t = t.value
+            st._stale = True
 
     _FORMS = ("stockham", "warp", "tensor")
 
@@ -623,7 +658,7 @@ class Solver:
         return xb[: 2 * n].reshape(2, n).T.copy(), vb[: 2 * n].reshape(2, n).T.copy()
 
     def advance(self, state: State, t: float):
-        u, v = self.prob.fluid.freestream(t)
+        u, v = self.prob.fluid.grid_flow(t)
         if self.moving:
             kin = np.ascontiguousarray(self.kinematics(t).reshape(-1))
             self._check(self.lib.ib_advance_kin(self.handle, float(t), u, v, _lib.dptr(kin)))
@@ -647,7 +682,7 @@ class Solver:
         ts = np.ascontiguousarray(np.asarray(ts, dtype=np.float64))
         if ts.size == 0:
             return
-        uv = np.ascontiguousarray(np.array([self.prob.fluid.freestream(t) for t in ts], dtype=np.float64).reshape(-1))
+        uv = np.ascontiguousarray(np.array([self.prob.fluid.grid_flow(t) for t in ts], dtype=np.float64).reshape(-1))
         if self.moving:
             kin = np.ascontiguousarray(np.concatenate([self.kinematics(t).reshape(-1) for t in ts]))
             self._check(self.lib.ib_advance_n_kin(self.handle, int(ts.size), _lib.dptr(ts), _lib.dptr(uv),
@@ -705,7 +740,7 @@ class Ensemble:
             ts = np.repeat(ts[:, None], n, axis=1)
         ts = np.ascontiguousarray(ts)
         if uv is None:
-            uv = np.array([[s.prob.fluid.freestream(float(ts[k, i])) for i, s in enumerate(self.solvers)]
+            uv = np.array([[s.prob.fluid.grid_flow(float(ts[k, i])) for i, s in enumerate(self.solvers)]
                            for k in range(ts.shape[0])], dtype=np.float64)
         uv = np.ascontiguousarray(uv, dtype=np.float64)
         ms = C.c_double()

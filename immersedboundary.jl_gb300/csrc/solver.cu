@@ -1894,6 +1894,98 @@ int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* no
   return check_status(h);
 }
 
+// ---- checkpoint files ------------------------------------------------------------------------
+// Layout (little-endian): 8-byte magic "IBGB300C", int32 version (1), int32 nx, ny, nlevels,
+// npoints, moving (1 if the F_{n-2} block follows), two int32 zeros, double t, int64 steps, then
+// FP64 arrays in the ABI's column-major layouts: Gamma, q, psi, nonlin[1], nonlin[2]
+// (nlevels x (nx-1)(ny-1) or nlevels x nq each), Fb (2 npoints) and, for moving bodies, the
+// previous step's Fb (the CG warm start's history).
+namespace {
+constexpr char kCkptMagic[8] = {'I', 'B', 'G', 'B', '3', '0', '0', 'C'};
+struct CkptHeader {
+  char magic[8];
+  int32_t version, nx, ny, nlevels, npoints, moving, reserved0, reserved1;
+  double t;
+  int64_t steps;
+};
+static_assert(sizeof(CkptHeader) == 56, "checkpoint header layout");
+}  // namespace
+
+int ib_checkpoint_save(ib_handle* h, const char* path) {
+  if (!h || !path) return IB_ERR_INVALID;
+  const Geometry& g = h->g;
+  const size_t nGL = (size_t)g.nlev * g.nG, nqL = (size_t)g.nlev * g.nq;
+  std::vector<double> buf(4 * nGL + nqL + 2 * (size_t)h->nf);
+  double* gam = buf.data();
+  double* q = gam + nGL;
+  double* psi = q + nqL;
+  double* n1 = psi + nGL;
+  double* n2 = n1 + nGL;
+  double* fb = n2 + nGL;
+  double t = 0.0;
+  int rc = ib_get_state(h, gam, q, psi, n1, n2, fb, &t);
+  if (rc != IB_OK) return rc;
+  const bool moving = h->motion == IB_MOTION_PRESCRIBED && h->nf > 0;
+  if (moving) {
+    DeviceGuard dev_guard_(h->device);
+    CK(dev_guard_.err);
+    CK(cudaMemcpy(fb + h->nf, h->fb_prev, sizeof(double) * h->nf, cudaMemcpyDeviceToHost));
+  }
+  CkptHeader hd{};
+  std::memcpy(hd.magic, kCkptMagic, 8);
+  hd.version = 1;
+  hd.nx = g.nx; hd.ny = g.ny; hd.nlevels = g.nlev; hd.npoints = h->nb; hd.moving = moving ? 1 : 0;
+  hd.t = t;
+  hd.steps = h->steps;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(h, IB_ERR_INVALID, "checkpoint: cannot open the file for writing");
+  const size_t nvals = 4 * nGL + nqL + (size_t)h->nf * (moving ? 2 : 1);
+  const bool ok = std::fwrite(&hd, sizeof(hd), 1, f) == 1 && std::fwrite(buf.data(), sizeof(double), nvals, f) == nvals;
+  const bool closed = std::fclose(f) == 0;
+  if (!ok || !closed) return fail(h, IB_ERR_INVALID, "checkpoint: write failed");
+  return IB_OK;
+}
+
+int ib_checkpoint_load(ib_handle* h, const char* path) {
+  if (!h || !path) return IB_ERR_INVALID;
+  const Geometry& g = h->g;
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(h, IB_ERR_INVALID, "checkpoint: cannot open the file");
+  CkptHeader hd{};
+  if (std::fread(&hd, sizeof(hd), 1, f) != 1 || std::memcmp(hd.magic, kCkptMagic, 8) != 0 || hd.version != 1) {
+    std::fclose(f);
+    return fail(h, IB_ERR_INVALID, "checkpoint: not a version-1 libibgb300 checkpoint");
+  }
+  const bool moving = h->motion == IB_MOTION_PRESCRIBED && h->nf > 0;
+  if (hd.nx != g.nx || hd.ny != g.ny || hd.nlevels != g.nlev || hd.npoints != h->nb || (hd.moving != 0) != moving) {
+    std::fclose(f);
+    return fail(h, IB_ERR_INVALID, "checkpoint: grid, levels, points or body motion differ from the handle's");
+  }
+  const size_t nGL = (size_t)g.nlev * g.nG, nqL = (size_t)g.nlev * g.nq;
+  const size_t nvals = 4 * nGL + nqL + (size_t)h->nf * (moving ? 2 : 1);
+  std::vector<double> buf(nvals);
+  const bool ok = std::fread(buf.data(), sizeof(double), nvals, f) == nvals;
+  std::fclose(f);
+  if (!ok) return fail(h, IB_ERR_INVALID, "checkpoint: file is shorter than its header says");
+  double* gam = buf.data();
+  double* q = gam + nGL;
+  double* psi = q + nqL;
+  double* n1 = psi + nGL;
+  double* n2 = n1 + nGL;
+  double* fb = n2 + nGL;
+  int rc = ib_set_state(h, gam, q, psi, n1, n2, h->nf ? fb : nullptr, hd.t);
+  if (rc != IB_OK) return rc;
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
+  if (moving) {
+    CK(cudaMemcpy(h->fb_prev, fb + h->nf, sizeof(double) * h->nf, cudaMemcpyHostToDevice));
+    for (auto& ge : h->mgexec)
+      if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  }
+  h->steps = hd.steps;
+  return IB_OK;
+}
+
 int ib_advance(ib_handle* h, double t, double u, double v) {
   if (!h) return IB_ERR_INVALID;
   DeviceGuard dev_guard_(h->device);

@@ -157,6 +157,13 @@ end
 "`advance!(state, solver, t)`: src/streamfcn/cnab/timestepping.jl:253-290 on the GPU."
 function ImmersedBoundary.advance!(state, solver::GB300Solver, t::Float64)
     u, v = fluidof(solver.prob).freestream(t)
+    # a grid translating with a RelativeFrame of the lab frame sees the freestream minus its
+    # velocity (base_flux! for a moving grid, the reference's TODO at fluid-ops.jl:419)
+    gframe = fluidof(solver.prob).domain.frame
+    if gframe isa RelativeFrame
+        gv = gframe.v(t)
+        u, v = u - gv[1], v - gv[2]
+    end
     st = if solver.moving
         # update_bodies! (src/bodies/body-points.jl:52-68): the frame closures at t, per body
         for (k, b) in enumerate(bodygroup(solver.prob))

@@ -106,6 +106,18 @@ int ib_set_state(ib_handle* h, const double* gamma, const double* q, const doubl
 int ib_get_state(ib_handle* h, double* gamma, double* q, double* psi, double* nonlin1,
                  double* nonlin2, double* fb, double* t);
 
+/* Checkpoint files for restarts and for cross-checking with other implementations.  The
+ * reference keeps snapshots in memory only (copy! of the state, src/streamfcn/states.jl:90-112,
+ * cnab/states.jl:23-27; solve! resumes from a given state, src/solve.jl:188).  The file holds
+ * what a restart needs: Gamma, q, psi, state.nonlin[1], state.nonlin[2], Fb, t, the step count
+ * and, for moving bodies, the previous step's Fb; FP64 in the column-major layouts above after
+ * a 56-byte header (magic "IBGB300C", int32 version 1, nx, ny, nlevels, npoints, moving flag,
+ * two zeros, double t, int64 steps).  Loading checks that the handle's grid, levels, points and motion match.  An FP64
+ * handle restarts to the same bits as an uninterrupted run; a mixed-precision one restarts its
+ * solves' predictors from zero and agrees to the refinement tolerance. */
+int ib_checkpoint_save(ib_handle* h, const char* path);
+int ib_checkpoint_load(ib_handle* h, const char* path);
+
 /* advance!(state, solver, t): src/streamfcn/cnab/timestepping.jl:253-290.  (u_inf, v_inf) is
  * fluid.freestream(t) (src/streamfcn/fluids.jl:82), evaluated by the caller; base_flux!
  * (src/streamfcn/fluid-ops.jl:403-417) runs on the device.  Synchronous: returns the step's

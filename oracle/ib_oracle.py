@@ -489,10 +489,18 @@ class Problem:
     body_npoints: list                  # points per body
     beta: tuple = (1.5, -0.5)           # SchemeCNAB(Val(2), dt), src/schemes.jl:22
     freestream: object = (1.0, 0.0)     # (u, v) constant or callable t -> (u, v)
+    grid_velocity: object = None        # translating grid: t -> (vx, vy) of the grid frame
 
     def uv(self, t):
+        """The uniform flow of base_flux! (fluid-ops.jl:403-417) in grid coordinates: the
+        freestream, minus the grid's velocity when the grid translates (the moving-grid case the
+        reference leaves as a TODO at fluid-ops.jl:419, restated as a Galilean change of frame)."""
         f = self.freestream
-        return tuple(f(t)) if callable(f) else tuple(f)
+        u, v = tuple(f(t)) if callable(f) else tuple(f)
+        if self.grid_velocity is not None:
+            gx, gy = self.grid_velocity(t)
+            u, v = u - gx, v - gy
+        return (u, v)
 
 
 @dataclass
@@ -799,3 +807,69 @@ class MovingSolver(Solver):
         st.psi, st.q = vort2flux(st.gamma, g, self.lam)
         st.t = float(t)
         st.points, st.velocities = xb, vb
+
+
+# ---------------------------------------------------------------------------
+# Checkpoint files of libibgb300 (ib_checkpoint_save / ib_checkpoint_load): the reference keeps
+# snapshots in memory only (copy! of the state, states.jl:90-112, cnab/states.jl:23-27); this
+# reader lets the oracle continue a run the GPU saved, and the writer makes files for tests.
+# Layout: 56-byte header (8-byte magic "IBGB300C", int32 version 1, nx, ny, nlevels, npoints,
+# moving flag, two int32 zeros, float64 t, int64 steps) then float64 arrays in the column-major
+# layouts: Gamma, q, psi, nonlin[1], nonlin[2], Fb [, previous Fb when moving].
+# ---------------------------------------------------------------------------
+_CKPT_HEADER = np.dtype([("magic", "S8"), ("version", "<i4"), ("nx", "<i4"), ("ny", "<i4"), ("nlevels", "<i4"),
+                         ("npoints", "<i4"), ("moving", "<i4"), ("r0", "<i4"), ("r1", "<i4"), ("t", "<f8"),
+                         ("steps", "<i8")])
+
+
+def write_checkpoint(path, g: Grid, st: State, steps: int = 0, fb_prev=None):
+    """Write an oracle State in the libibgb300 checkpoint layout."""
+    L = g.nlevels
+    hd = np.zeros(1, dtype=_CKPT_HEADER)
+    nb = st.fb.size // 2
+    hd[0] = (b"IBGB300C", 1, g.nx, g.ny, L, nb, 1 if fb_prev is not None else 0, 0, 0, st.t, steps)
+    parts = [st.gamma.reshape(L, -1), st.q.reshape(L, -1), st.psi.reshape(L, -1),
+             st.nonlin[0].reshape(L, -1), st.nonlin[1].reshape(L, -1), st.fb]
+    if fb_prev is not None:
+        parts.append(np.asarray(fb_prev))
+    with open(path, "wb") as f:
+        f.write(hd.tobytes())
+        for a in parts:
+            f.write(np.ascontiguousarray(a, dtype="<f8").tobytes())
+
+
+def read_checkpoint(path, g: Grid) -> dict:
+    """Read a libibgb300 checkpoint for grid g: header fields and the arrays, shaped like the
+    oracle's State fields (``nonlin`` as [older, newest] like ``State.nonlin``: the file's
+    nonlin[1] and nonlin[2] in the reference's 1-based order)."""
+    raw = open(path, "rb").read()
+    hd = np.frombuffer(raw[:_CKPT_HEADER.itemsize], dtype=_CKPT_HEADER)[0]
+    if hd["magic"] != b"IBGB300C" or hd["version"] != 1:
+        raise ValueError("not a version-1 libibgb300 checkpoint")
+    if (hd["nx"], hd["ny"], hd["nlevels"]) != (g.nx, g.ny, g.nlevels):
+        raise ValueError("checkpoint grid differs from the problem's")
+    L, nb = g.nlevels, int(hd["npoints"])
+    v = np.frombuffer(raw[_CKPT_HEADER.itemsize:], dtype="<f8")
+    sizes = [L * g.ngamma, L * g.nq, L * g.ngamma, L * g.ngamma, L * g.ngamma, 2 * nb]
+    if hd["moving"]:
+        sizes.append(2 * nb)
+    if v.size != sum(sizes):
+        raise ValueError("checkpoint size differs from its header")
+    out, o = [], 0
+    for n in sizes:
+        out.append(v[o:o + n].copy())
+        o += n
+    shp = (L,) + g.gshape
+    return {"t": float(hd["t"]), "steps": int(hd["steps"]), "gamma": out[0].reshape(shp),
+            "q": out[1].reshape(L, g.nq), "psi": out[2].reshape(shp),
+            "nonlin": [out[3].reshape(shp), out[4].reshape(shp)], "fb": out[5],
+            "fb_prev": out[6] if hd["moving"] else None}
+
+
+def state_from_checkpoint(prob: Problem, ck: dict) -> State:
+    """An oracle State continuing from a checkpoint (q0 is recomputed by the next advance)."""
+    st = init_state(prob, ck["t"])
+    st.gamma, st.q, st.psi = ck["gamma"].copy(), ck["q"].copy(), ck["psi"].copy()
+    st.nonlin = [a.copy() for a in ck["nonlin"]]
+    st.fb = ck["fb"].copy()
+    return st

@@ -119,3 +119,17 @@ def test_create_validates_arguments_without_a_gpu(lib):
     assert lib.ib_create(ctypes.byref(p), ctypes.byref(h)) == L.IB_ERR_INVALID
     assert lib.ib_status_string(3) == b"infinite flux"
     assert lib.ib_advance(None, 0.0, 1.0, 0.0) == L.IB_ERR_INVALID
+
+
+def test_grid_flow_of_a_translating_grid(ib):
+    """base_flux! in grid coordinates: the freestream, minus a translating grid's velocity."""
+    disc = ib.MultiLevel(ib.UniformGrid(0.05, (-1.0, 1.0), (-1.0, 1.0)), 2)
+    lab = ib.StreamFcnFluid(disc, lambda t: (1.0 + t, 0.5), 100.0)
+    assert lab.grid_flow(2.0) == (3.0, 0.5)
+    frame = ib.RelativeFrame(ib.LabFrame(), r=lambda t: (0.0, 0.0), v=lambda t: (0.25, -t),
+                             theta=lambda t: 0.0, omega=lambda t: 0.0)
+    moving = ib.StreamFcnFluid(ib.FluidDomain(disc, frame), lambda t: (1.0 + t, 0.5), 100.0)
+    assert moving.grid_flow(2.0) == (2.75, 2.5)
+    prob = ib.Problem(moving, ib.BodyGroup(), ib.SchemeCNAB(0.01))
+    q0 = ib.api._base_flux(prob, 2.0)
+    assert np.allclose(q0[0, : moving.domain.nu], 2.75 * 0.05) and np.allclose(q0[1, moving.domain.nu:], 2.5 * 0.1)

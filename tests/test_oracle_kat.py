@@ -255,3 +255,37 @@ def test_preconditioned_schur_solve_matches_dense_inverse(O):
     assert np.linalg.norm(a.fb - b.fb) / np.linalg.norm(a.fb) < 1e-11
     assert np.linalg.norm(a.gamma - b.gamma) / np.linalg.norm(a.gamma) < 1e-12
     assert 1 <= max(iters.refine_iterations) < 15
+
+
+def test_checkpoint_format_round_trip(O, tmp_path):
+    """The checkpoint layout (header + column-major FP64 arrays) read back field by field;
+    files of another grid, a wrong magic or a short body are refused."""
+    g = small_grid(O, 32, 24, 3)
+    prob = O.Problem(g, 0.01, 100.0, np.zeros((0, 2)), np.zeros(0), [])
+    st = O.init_state(prob, 0.37)
+    rng = np.random.default_rng(2)
+    st.gamma = rng.standard_normal(st.gamma.shape)
+    st.psi = rng.standard_normal(st.psi.shape)
+    st.q = rng.standard_normal(st.q.shape)
+    st.nonlin = [rng.standard_normal(st.gamma.shape), rng.standard_normal(st.gamma.shape)]
+    st.fb = rng.standard_normal(6)
+    path = tmp_path / "a.ckpt"
+    O.write_checkpoint(path, g, st, steps=12, fb_prev=np.arange(6.0))
+    raw = path.read_bytes()
+    assert raw[:8] == b"IBGB300C" and len(raw) == 56 + 8 * (4 * 3 * g.ngamma + 3 * g.nq + 12)
+    ck = O.read_checkpoint(path, g)
+    assert ck["t"] == 0.37 and ck["steps"] == 12
+    for k in ("gamma", "psi", "q", "fb"):
+        np.testing.assert_array_equal(ck[k], getattr(st, k))
+    np.testing.assert_array_equal(ck["nonlin"][0], st.nonlin[0])
+    np.testing.assert_array_equal(ck["nonlin"][1], st.nonlin[1])
+    np.testing.assert_array_equal(ck["fb_prev"], np.arange(6.0))
+    with pytest.raises(ValueError):
+        O.read_checkpoint(path, small_grid(O, 32, 32, 3))
+    bad = tmp_path / "b.ckpt"
+    bad.write_bytes(b"XXXXXXXX" + raw[8:])
+    with pytest.raises(ValueError):
+        O.read_checkpoint(bad, g)
+    bad.write_bytes(raw[:-8])
+    with pytest.raises(ValueError):
+        O.read_checkpoint(bad, g)

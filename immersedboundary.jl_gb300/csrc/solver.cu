@@ -1983,6 +1983,10 @@ int ib_checkpoint_load(ib_handle* h, const char* path) {
       if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
   }
   h->steps = hd.steps;
+  // the C_D / C_L history continues at the restored step (its earlier entries are not in the
+  // file)
+  const int counter = (int)(hd.steps % h->hist_cap);
+  CK(cudaMemcpy(h->d_counter, &counter, sizeof(int), cudaMemcpyHostToDevice));
   return IB_OK;
 }
 

@@ -263,6 +263,96 @@ def run_ensemble_config(ib, lib, n=96, K=20, W=3, moving=True):
     }
 
 
+def run_learned_protocol(ib, n_train=2000, n_eval=2000, f_train=0.2, f_unseen=(0.15, 0.25)):
+    """The learned warm start under the moving-plate protocol: the network trains on the
+    solver's own force history of steps 0..n_train-1 at f_train, then starts the CG solves of
+    steps n_train..n_train+n_eval-1 and, carried over to other handles, the solves of
+    n_eval steps at each unseen frequency; against linear extrapolation on the same steps.
+    Mixed precision, Schur-preconditioned CG to 1e-10 with a fixed re-assembly period (20 steps)
+    so that both arms see the same preconditioners."""
+    W = ib.workloads
+
+    def arm(f, nsteps, learned, train_at=None, import_buf=None):
+        wl = W.heaving_plate(nsteps=nsteps, f=f)
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision="mixed")
+        s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+        s.set_cg_preconditioner("schur_ref", refresh_steps=20)
+        s.vort2flux(st)
+        info = {}
+        if learned:
+            s.learn_init(hidden=256, layers=3, capacity=4096, seed=0)
+            if import_buf is not None:
+                s.learn_import(import_buf)
+                s.set_cg_options(tol=1e-10, warm_start="learned")
+            else:
+                s.learn_collect(True)
+        ts = [i * wl.dt for i in range(nsteps)]
+        t0 = time.perf_counter()
+        if train_at is not None:
+            s.advance_n(st, ts[:train_at])
+            a = time.perf_counter()
+            loss = s.learn_train(epochs=200, batch=64, lr=1e-3, seed=0)
+            blend, rel = s.learn_validation()
+            info = {"train_samples": s.learn_samples(), "train_loss": loss, "blend": blend,
+                    "held_out_rel_err_vs_extrapolation": rel, "train_s": time.perf_counter() - a}
+            s.learn_collect(False)
+            s.set_cg_options(tol=1e-10, warm_start="learned")
+            s.advance_n(st, ts[train_at:])
+        else:
+            s.advance_n(st, ts)
+        sec = time.perf_counter() - t0
+        it, res, r0 = s.cg_stats(nsteps, start=True)
+        buf = s.learn_export() if (learned and train_at is not None) else None
+        s.close()
+        return dict(it=np.asarray(it), res=np.asarray(res), r0=np.asarray(r0), info=info, buf=buf, sec=sec)
+
+    def summ(a, sl):
+        return {"cg_iterations_mean": float(np.mean(a["it"][sl])), "cg_iterations_max": int(np.max(a["it"][sl])),
+                "start_residual_mean": float(np.mean(a["r0"][sl])), "final_residual_max": float(np.max(a["res"][sl]))}
+    n = n_train + n_eval
+    lrn = arm(f_train, n, True, train_at=n_train)
+    ext = arm(f_train, n, False)
+    ev = slice(n_train, n)
+    out = {"workload": "heaving_plate 768x512x4, Re 1000, dt 0.0005, 201 points, heave 0.5 sin(2 pi f t), "
+                       "pitch 30 deg",
+           "training": lrn["info"],
+           "f_%g_steps_%d_%d" % (f_train, n_train, n): {"learned": summ(lrn, ev), "extrapolated": summ(ext, ev)}}
+    for f in f_unseen:
+        a = arm(f, n_eval, True, import_buf=lrn["buf"])
+        b = arm(f, n_eval, False)
+        sl = slice(2, n_eval)
+        out["f_%g_unseen_steps_0_%d" % (f, n_eval)] = {"learned": summ(a, sl), "extrapolated": summ(b, sl)}
+    return out
+
+
+def run_dt_probe(ib, dt=0.001, nsteps=40):
+    """Largest |Gamma| on the finest level per step of the moving plate at a given time step
+    (FP64 path, CG to 1e-10): the growth factor shows whether the step is stable."""
+    wl = ib.workloads.heaving_plate(nsteps=nsteps, dt=dt)
+    prob = wl.problem()
+    st = ib.initstate(prob)
+    st._gamma[:] = wl.initial_gamma()
+    s = ib.initsolver(prob, st, precision="fp64")
+    s.set_cg_options(tol=1e-10, warm_start="previous")
+    s.set_cg_preconditioner("schur_ref")
+    s.vort2flux(st)
+    gmax, err = [], None
+    try:
+        for i in range(nsteps):
+            ib.advance_(st, s, i * wl.dt)
+            gmax.append(float(np.max(np.abs(st.qty.gamma[0]))))
+    except Exception as e:  # a blown-up state ends the run with the library's status
+        err = str(e)
+    s.close()
+    g = np.array(gmax)
+    return {"dt": dt, "steps_run": len(gmax), "gamma_max": gmax,
+            "growth_per_step_last5": [float(x) for x in (g[-5:] / g[-6:-1])] if g.size > 6 else None,
+            "stopped_by": err}
+
+
 def run_precision_table(ib, wl, checkpoints=(100, 1000, 2000)):
     """Error of the mixed-precision solve against the FP64 GPU path at the given steps, with the
     sine transforms in FP32 (warp-per-line FFT passes) and as BF16x3 tensor-core GEMMs: relative
@@ -686,11 +776,22 @@ def main():
     ap.add_argument("--precision-table", action="store_true",
                     help="print the FP64 / FP32 / BF16x3 error table of the 2048^2 four-cylinder workload "
                          "at steps 100, 1000 and 2000 and exit")
+    ap.add_argument("--learned-protocol", action="store_true",
+                    help="print the learned warm start's moving-plate protocol (train on steps 0-2000 at f 0.2, "
+                         "evaluate on 2000-4000 and on f 0.15 / 0.25) and a dt 0.001 stability probe, and exit")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl != "reference" else args.warmup
     rank, world, local = dist_env()
+    if args.learned_protocol:
+        import __graft_entry__ as ge
+        ib = ge.package()
+        ge.build()
+        ib.load_library()
+        print(json.dumps({"learned_protocol": run_learned_protocol(ib),
+                          "dt_probe": [run_dt_probe(ib, 0.001), run_dt_probe(ib, 0.0005)]}), flush=True)
+        return
     if args.precision_table:
         import __graft_entry__ as ge
         ib = ge.package()

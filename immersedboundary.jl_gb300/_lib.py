@@ -111,6 +111,9 @@ SIGNATURES = {
     # diagnostics
     "ib_get_info": (C.c_int, [_vp, C.POINTER(IbInfo)]),
     "ib_checkpoint_save": (C.c_int, [_vp, C.c_char_p]),
+    "ib_learn_set_blend": (C.c_int, [_vp, C.c_double]),
+    "ib_learn_export": (C.c_int, [_vp, _fp, C.c_int64]),
+    "ib_learn_import": (C.c_int, [_vp, _fp, C.c_int64]),
     "ib_checkpoint_load": (C.c_int, [_vp, C.c_char_p]),
     "ib_get_autotune": (C.c_int, [_vp, _dp, _ip]),
     "ib_advance_n_timed": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),

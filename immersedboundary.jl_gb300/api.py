@@ -619,6 +619,25 @@ class Solver:
         self._check(self.lib.ib_learn_validation(self.handle, C.byref(b), C.byref(r)))
         return b.value, r.value
 
+    def learn_set_blend(self, blend: float):
+        """Weight of the network's correction in the warm start (0: plain extrapolation)."""
+        self._check(self.lib.ib_learn_set_blend(self.handle, float(blend)))
+
+    def learn_export(self) -> np.ndarray:
+        """The trained network with its normalisation and blend (``ib_learn_export``)."""
+        dims = self.learn_layout()
+        npar = C.c_int64()
+        self._check(self.lib.ib_learn_param_count(self.handle, C.byref(npar)))
+        n = int(npar.value) + 2 * dims[0] + 2 * dims[-1] + 1
+        buf = np.zeros(n, dtype=np.float32)
+        self._check(self.lib.ib_learn_export(self.handle, _lib.fptr(buf), n))
+        return buf
+
+    def learn_import(self, buf: np.ndarray):
+        """Load a network exported from a handle of the same layout; marks it trained."""
+        b = np.ascontiguousarray(buf, dtype=np.float32)
+        self._check(self.lib.ib_learn_import(self.handle, _lib.fptr(b), int(b.size)))
+
     def learn_layout(self):
         nl = C.c_int32()
         dims = np.zeros(16, dtype=np.int32)

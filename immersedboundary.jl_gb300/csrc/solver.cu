@@ -2561,6 +2561,59 @@ int ib_learn_set_params(ib_handle* h, const float* params) {
   return IB_OK;
 }
 
+int ib_learn_set_blend(ib_handle* h, double blend) {
+  if (!h || !h->mlp || !(blend >= 0.0 && blend <= 1.0)) return IB_ERR_INVALID;
+  h->mlp->blend = blend;
+  // the captured moving step holds the blend as a kernel argument: capture it again
+  for (auto& ge : h->mgexec)
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  return IB_OK;
+}
+
+int ib_learn_export(ib_handle* h, float* buf, int64_t n) {
+  if (!h || !h->mlp || !buf) return IB_ERR_INVALID;
+  learn::Mlp* m = h->mlp;
+  const int din = m->dims[0], dout = m->dims[m->nl];
+  if (n != m->nparam + 2 * (int64_t)din + 2 * (int64_t)dout + 1) return fail(h, IB_ERR_INVALID, "learn export: size");
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
+  cudaStream_t s = h->stream;
+  float* p = buf;
+  CK(cudaMemcpyAsync(p, m->master, sizeof(float) * m->nparam, cudaMemcpyDeviceToHost, s)); p += m->nparam;
+  CK(cudaMemcpyAsync(p, m->mu_x, sizeof(float) * din, cudaMemcpyDeviceToHost, s)); p += din;
+  CK(cudaMemcpyAsync(p, m->sd_x, sizeof(float) * din, cudaMemcpyDeviceToHost, s)); p += din;
+  CK(cudaMemcpyAsync(p, m->mu_y, sizeof(float) * dout, cudaMemcpyDeviceToHost, s)); p += dout;
+  CK(cudaMemcpyAsync(p, m->sd_y, sizeof(float) * dout, cudaMemcpyDeviceToHost, s)); p += dout;
+  CK(cudaStreamSynchronize(s));
+  *p = (float)m->blend;
+  return IB_OK;
+}
+
+int ib_learn_import(ib_handle* h, const float* buf, int64_t n) {
+  if (!h || !h->mlp || !buf) return IB_ERR_INVALID;
+  learn::Mlp* m = h->mlp;
+  const int din = m->dims[0], dout = m->dims[m->nl];
+  if (n != m->nparam + 2 * (int64_t)din + 2 * (int64_t)dout + 1) return fail(h, IB_ERR_INVALID, "learn import: size");
+  const double blend = buf[n - 1];
+  if (!(blend >= 0.0 && blend <= 1.0)) return fail(h, IB_ERR_INVALID, "learn import: blend outside [0, 1]");
+  DeviceGuard dev_guard_(h->device);
+  CK(dev_guard_.err);
+  cudaStream_t s = h->stream;
+  const float* p = buf;
+  CK(cudaMemcpyAsync(m->master, p, sizeof(float) * m->nparam, cudaMemcpyHostToDevice, s)); p += m->nparam;
+  CK(cudaMemcpyAsync(m->mu_x, p, sizeof(float) * din, cudaMemcpyHostToDevice, s)); p += din;
+  CK(cudaMemcpyAsync(m->sd_x, p, sizeof(float) * din, cudaMemcpyHostToDevice, s)); p += din;
+  CK(cudaMemcpyAsync(m->mu_y, p, sizeof(float) * dout, cudaMemcpyHostToDevice, s)); p += dout;
+  CK(cudaMemcpyAsync(m->sd_y, p, sizeof(float) * dout, cudaMemcpyHostToDevice, s)); p += dout;
+  CK(m->sync_bf16());
+  CK(cudaStreamSynchronize(s));
+  m->blend = blend;
+  m->trained = true;
+  for (auto& ge : h->mgexec)
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+  return IB_OK;
+}
+
 int ib_learn_gradients(ib_handle* h, int32_t rows, const float* x, const float* y, float* grad, double* loss) {
   if (!h || !h->mlp || !x || !y || rows < 1 || rows > learn::kMaxBatch) return IB_ERR_INVALID;
   DeviceGuard dev_guard_(h->device);

@@ -52,6 +52,16 @@ int ib_learn_param_count(ib_handle* h, int64_t* nparam);
 int ib_learn_get_params(ib_handle* h, float* params);
 int ib_learn_set_params(ib_handle* h, const float* params);
 
+/* weight of the network's correction in the warm start, in [0, 1] (0: plain extrapolation);
+ * replaces the validated value until the next training */
+int ib_learn_set_blend(ib_handle* h, double blend);
+
+/* a trained network with its normalisation, to reuse it on another handle of the same layout
+ * (another frequency, say): n = nparam + 2 dims[0] + 2 dims[last] + 1 floats: the parameters,
+ * mu_x, sd_x, mu_y, sd_y, then the blend.  Import marks the network trained. */
+int ib_learn_export(ib_handle* h, float* buf, int64_t n);
+int ib_learn_import(ib_handle* h, const float* buf, int64_t n);
+
 /* loss and parameter gradients of the network (normalisation not applied) on `rows` host rows
  * of inputs x [rows][dims[0]] and targets y [rows][dims[last]]: the training kernels, exposed
  * for gradient checks */

@@ -49,7 +49,7 @@ def test_gradients_match_oracle(ib):
     s.close()
 
 
-def run(ib, wl, warm, n_train, n_eval, train_kw):
+def run(ib, wl, warm, n_train, n_eval, train_kw, blend=None):
     prob = wl.problem()
     st = ib.initstate(prob)
     s = ib.initsolver(prob, st)
@@ -63,6 +63,8 @@ def run(ib, wl, warm, n_train, n_eval, train_kw):
         loss = s.learn_train(**train_kw)
         loss = (loss,) + s.learn_validation()
         s.set_cg_options(tol=1e-10, warm_start="learned")
+        if blend is not None:
+            s.learn_set_blend(blend)
     for i in range(n_train, n_train + n_eval):
         ib.advance_(st, s, i * wl.dt)
     it, res, r0 = s.cg_stats(n_eval, start=True)
@@ -87,3 +89,53 @@ def test_learned_warm_start_converges_and_does_not_regress_on_held_out_steps(ib)
     assert 0.0 <= loss[1] <= 1.0 and loss[2] <= 1.0
     assert np.mean(r0_l) <= 1.05 * np.mean(r0_e)
     assert it_l.sum() <= it_e.sum() * 1.01
+
+
+def test_zero_blend_start_is_extrapolation_on_the_same_trajectory(ib):
+    """With the network's correction weighted 0 the learned arm starts every CG solve exactly
+    where the extrapolating arm does (the same start residuals and iteration counts, step by
+    step): the learned arm's features and force history belong to the current step, so the
+    gap between the two arms' start residuals at the validated blend is the correction
+    itself.  That correction minimises the held-out error of F in the 2-norm, while the start
+    residual weighs it by B (cond ~1e4-1e5): a small blend of a correction that is rough along
+    the plate can still raise ||B x0 - rhs||."""
+    wl = heaving(ib)
+    n_train, n_eval = 200, 20
+    kw = dict(epochs=100, batch=32, lr=1e-3, seed=0)
+    it_e, res_e, r0_e, _, _ = run(ib, wl, "extrapolate", n_train, n_eval, kw)
+    it_0, res_0, r0_0, _, _ = run(ib, wl, "learned", n_train, n_eval, kw, blend=0.0)
+    np.testing.assert_array_equal(r0_0, r0_e)
+    np.testing.assert_array_equal(it_0, it_e)
+
+
+def test_network_export_import_reproduces_the_predictions(ib):
+    """A trained network moved to a second handle (ib_learn_export / ib_learn_import) gives that
+    handle the same warm starts: both continue the same run to the same bits."""
+    wl = heaving(ib)
+    arms = []
+    for k in range(2):
+        prob = wl.problem()
+        st = ib.initstate(prob)
+        s = ib.initsolver(prob, st)
+        s.set_cg_options(tol=1e-10, warm_start="extrapolate")
+        s.learn_init(hidden=64, layers=3, capacity=512, seed=0)
+        s.learn_collect(True)
+        arms.append((st, s))
+    for i in range(120):
+        for st, s in arms:
+            ib.advance_(st, s, i * wl.dt)
+    arms[0][1].learn_train(epochs=40, batch=32, lr=1e-3, seed=0)
+    arms[0][1].learn_set_blend(0.5)
+    buf = arms[0][1].learn_export()
+    arms[1][1].learn_import(buf)
+    np.testing.assert_array_equal(arms[1][1].learn_export(), buf)
+    for st, s in arms:
+        s.set_cg_options(tol=1e-10, warm_start="learned")
+    for i in range(120, 130):
+        for st, s in arms:
+            ib.advance_(st, s, i * wl.dt)
+    np.testing.assert_array_equal(arms[0][0].qty.Fb, arms[1][0].qty.Fb)
+    r0 = [s.cg_stats(10, start=True)[2] for _, s in arms]
+    np.testing.assert_array_equal(r0[0], r0[1])
+    for _, s in arms:
+        s.close()

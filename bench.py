@@ -321,10 +321,16 @@ def run_learned_protocol(ib, n_train=2000, n_eval=2000, f_train=0.2, f_unseen=(0
            "training": lrn["info"],
            "f_%g_steps_%d_%d" % (f_train, n_train, n): {"learned": summ(lrn, ev), "extrapolated": summ(ext, ev)}}
     for f in f_unseen:
-        a = arm(f, n_eval, True, import_buf=lrn["buf"])
-        b = arm(f, n_eval, False)
+        key = "f_%g_unseen_steps_0_%d" % (f, n_eval)
         sl = slice(2, n_eval)
-        out["f_%g_unseen_steps_0_%d" % (f, n_eval)] = {"learned": summ(a, sl), "extrapolated": summ(b, sl)}
+        res = {}
+        for name, learned in (("learned", True), ("extrapolated", False)):
+            try:
+                a = arm(f, n_eval, learned, import_buf=lrn["buf"] if learned else None)
+                res[name] = summ(a, sl)
+            except Exception as e:  # reported, not fatal: the other arms still run
+                res[name] = {"error": str(e)}
+        out[key] = res
     return out
 
 

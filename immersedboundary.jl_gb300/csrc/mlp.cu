@@ -269,12 +269,17 @@ __global__ void k_normalize(const float* __restrict__ x, const float* __restrict
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) xn[i] = (x[i] - mu[i]) / sd[i];
 }
 
-// warm start: fb = 2 f1 - f2 + blend * (yhat * sd_y + mu_y)
+// warm start: fb = 2 f1 - f2 + blend * (yhat * sd_y + mu_y); an entry whose correction is not
+// finite (a network far outside its training data) keeps the extrapolation, so a start never
+// brings a non-finite value into the CG
 __global__ void k_predict(const float* __restrict__ yh, const float* __restrict__ mu_y, const float* __restrict__ sd_y,
                           const double* __restrict__ f1, const double* __restrict__ f2, double* __restrict__ fb,
                           int nf, double blend) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x)
-    fb[i] = 2.0 * f1[i] - f2[i] + blend * ((double)yh[i] * (double)sd_y[i] + (double)mu_y[i]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += gridDim.x * blockDim.x) {
+    const double ex = 2.0 * f1[i] - f2[i];
+    const double c = blend * ((double)yh[i] * (double)sd_y[i] + (double)mu_y[i]);
+    fb[i] = isfinite(c) ? ex + c : ex;
+  }
 }
 
 int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096); }

@@ -29,6 +29,7 @@ IB_PREC_MIXED = 1
 IB_PREC_MIXED_TC = 2
 PRECISIONS = {"fp64": IB_PREC_FP64, "mixed": IB_PREC_MIXED, "mixed_tc": IB_PREC_MIXED_TC}
 IB_FORM_STOCKHAM, IB_FORM_WARP, IB_FORM_TENSOR = 0, 1, 2
+IB_SCHEME_CNAB, IB_SCHEME_RKC = 0, 1
 IB_MOTION_STATIC = 0
 IB_MOTION_PRESCRIBED = 1
 IB_WARM_PREVIOUS = 0
@@ -51,7 +52,7 @@ class IbInfo(C.Structure):
     _fields_ = [("kernels_per_step", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
                 ("nlevels", C.c_int32), ("nbodies", C.c_int32), ("npoints", C.c_int32),
                 ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("vort2flux_order", C.c_int32),
-                ("transform_form", C.c_int32)]
+                ("transform_form", C.c_int32), ("scheme", C.c_int32), ("rkc_stages", C.c_int32)]
 
 
 class IbProblem(C.Structure):
@@ -65,6 +66,7 @@ class IbProblem(C.Structure):
         ("nbodies", C.c_int32), ("body_npoints", _ip), ("xb", _dp), ("ds", _dp),
         ("motion", C.c_int32), ("precision", C.c_int32), ("device", C.c_int32),
         ("history_capacity", C.c_int32), ("refine_sweeps", C.c_int32),
+        ("scheme", C.c_int32), ("rkc_stages", C.c_int32),
     ]
 
 

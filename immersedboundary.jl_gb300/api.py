@@ -258,10 +258,15 @@ class SchemeCNAB:
 
 
 class SchemeRKC:
-    """``SchemeRKC(dt)`` (schemes.jl:8-12): declared by the reference, no solver exists for it."""
+    """``SchemeRKC(dt)`` (schemes.jl:3-12), which the reference declares without a solver.  Here
+    the s-stage second-order Runge-Kutta-Chebyshev method (damping 2/13) on the explicit
+    vorticity transport dGamma/dt = nu lap(Gamma) + N(Gamma), followed by the immersed-boundary
+    projection; ``stages`` = 0 picks the fewest stages whose stability interval covers
+    1.5 x dt x 8 / (Re h^2).  FP64, bodies fixed in the grid."""
 
-    def __init__(self, dt: float):
+    def __init__(self, dt: float, stages: int = 0):
         self.dt = float(dt)
+        self.stages = int(stages)
 
 
 def timestep(x) -> float:
@@ -395,7 +400,7 @@ class State:
 
 def initstate(prob: Problem, t: float = 0.0) -> State:
     """``initstate(prob, t)`` (src/ImmersedBoundary.jl:51)."""
-    if not isinstance(prob.scheme, SchemeCNAB):
+    if not isinstance(prob.scheme, (SchemeCNAB, SchemeRKC)):
         raise NotImplementedError(f"no state type for scheme {type(prob.scheme).__name__}")
     return State(prob, t)
 
@@ -417,7 +422,7 @@ class Solver:
 
     def __init__(self, prob: Problem, state: State, device: int = 0, history_capacity: int = 4096,
                  precision: str = "fp64", refine_sweeps: int = 0):
-        if not isinstance(prob.scheme, SchemeCNAB):
+        if not isinstance(prob.scheme, (SchemeCNAB, SchemeRKC)):
             raise NotImplementedError(f"no solver for scheme {type(prob.scheme).__name__}")
         for b in prob.bodies:
             if not isinstance(b.frame, (GridFrame, RelativeFrame)):
@@ -447,7 +452,13 @@ class Solver:
         p.nx, p.ny, p.nlevels = base.nx, base.ny, self.L
         p.x0, p.y0, p.h = float(base.xs[0]), float(base.ys[0]), base.h
         p.dt = prob.scheme.dt
-        p.beta0, p.beta1 = prob.scheme.beta
+        if isinstance(prob.scheme, SchemeRKC):
+            p.beta0, p.beta1 = 1.5, -0.5
+            p.scheme = _lib.IB_SCHEME_RKC
+            p.rkc_stages = prob.scheme.stages
+        else:
+            p.beta0, p.beta1 = prob.scheme.beta
+            p.scheme = _lib.IB_SCHEME_CNAB
         p.re = prob.fluid.Re
         p.nbodies = self.nbodies
         p.body_npoints = _lib.iptr(self._npts) if self.nbodies else None

@@ -261,12 +261,15 @@ struct NonlinArgs {
 };
 template <typename T>
 cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s);
+// one stage of the Runge-Kutta-Chebyshev scheme (stencil.cu: k_rkc_stage)
+cudaError_t rkc_stage(int64_t n, double* Y, const double* Y0, const double* Ym1, const double* Ym2, const double* G,
+                      double* F0, double a0, double a1, double a2, double c1, double c0, bool store_f0, cudaStream_t s);
 
 // Trial-step boundary rings: bcn[l] (nonlinear ring, already x0.25x0.25) for l < nlev-1 and
 // the accumulated rhsbc edge vectors of every level (reference quirk: never reset).
 template <typename T>
 cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac,
-                        cudaStream_t s);
+                        cudaStream_t s, bool accumulate = true);
 
 // ----------------------------------------------------------------------------------------------
 // bodies (body.cu)

@@ -82,6 +82,12 @@ struct ib_handle {
   int coarse_from = 2;                          // first (0-based) level counted as coarse
   bool wdst = false;                            // both axes use the warp-per-line passes
   bool gdst = false;                            // mixed precision: transforms as tensor-core GEMMs
+  int scheme = IB_SCHEME_CNAB;                  // time stepping (IB_SCHEME_*)
+  int rkc_s = 0;                                // Runge-Kutta-Chebyshev: stages and their
+  std::vector<double> rkc_mu, rkc_nu, rkc_mut, rkc_gamt;  // coefficients (index = stage)
+  double* rkY[2] = {nullptr, nullptr};          // stage values (rotating)
+  double* rkF0 = nullptr;                       // F(Y0)
+  double *d_alpha_rkc = nullptr, *d_fac_rkc = nullptr;  // per level 1 / (Re hc^2)
   bool cn_pred = false;                         // mixed: trial CN solve refined from Gamma_n,
   double* cprev = nullptr;                      //   the projection from its previous correction
   cudaEvent_t stress_ev[2] = {nullptr, nullptr};  // fork / join of the stress branch
@@ -681,8 +687,101 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
   return enqueue_project<S>(h, p);
 }
 
+// One step of the Runge-Kutta-Chebyshev scheme (FP64, bodies fixed in the grid), buffer parity p:
+//   Y0 = Gamma_n;  Y1 = Y0 + mut_1 dt F(Y0);
+//   Y_j = (1 - mu_j - nu_j) Y0 + mu_j Y_{j-1} + nu_j Y_{j-2} + mut_j dt F(Y_{j-1}) + gamt_j dt F(Y0)
+//   F(Y) = N(Y) + (1/(Re hc^2)) (ring edges - lap5 Y) per level: the CNAB scheme's nonlinear
+//   term (with its rings) and the explicit viscous term, whose missing neighbours at a level's
+//   edges are the next coarser level's values (get_bc!); N and the fluxes of Y_{j-1} from a
+//   Vort2Flux of every level (which coarsifies Y_{j-1} in place, as the reference's does to Gamma)
+//   Fb = B'^-1 E(q(Y_s) + q0), B' = E C Lap^-1 C^T E^T;  Gamma_{n+1} = Y_s - C^T E^T Fb on level 1
+cudaError_t enqueue_rkc_step(ib_handle* h, int p) {
+  const Geometry& g = h->g;
+  const int L = g.nlev;
+  const int64_t n = (int64_t)L * g.nG;
+  cudaStream_t s = h->stream;
+  double* Y0 = h->G[p];
+  double* out = h->G[p ^ 1];
+  const double dt = h->dt;
+  // rhs = Y + F(Y), from the fluxes q of Y
+  auto evalG = [&](const double* Y, const double* q) -> cudaError_t {
+    CE(trial_rings<double>(g, Y, h->bcn, h->edges, h->d_fac_rkc, s, false));
+    NonlinArgs<double> na{};
+    na.q = q;
+    na.gamma = Y;
+    na.bcn = h->bcn;
+    na.nl_old = h->N[p];      // weight 0
+    na.edges = h->edges;
+    na.nl_new = h->N[p ^ 1];  // N(Y) (not kept: the scheme has no history)
+    na.rhs = h->rhs;
+    na.q0 = h->d_q0;
+    na.inv_hc2 = h->d_inv_hc2;
+    na.alpha = h->d_alpha_rkc;
+    na.dtb0 = 1.0;
+    na.dtb1 = 0.0;
+    return nonlin_rhs<double>(g, na, s);
+  };
+  const int S = h->rkc_s;
+  CE(evalG(Y0, h->q));
+  double* first = S == 1 ? out : h->rkY[0];
+  CE(rkc_stage(n, first, Y0, Y0, nullptr, h->rhs, h->rkF0, 1.0, 0.0, 0.0, h->rkc_mut[1] * dt, 0.0, true, s));
+  double *Ym1 = first, *Ym2 = Y0;
+  for (int j = 2; j <= S; ++j) {
+    CE(vort2flux<double>(h, Ym1, h->psi, h->q, nullptr, h->rings));
+    CE(evalG(Ym1, h->q));
+    double* dst = (j == S) ? out : (j == 2 ? h->rkY[1] : Ym2);
+    const double mu = h->rkc_mu[j], nu = h->rkc_nu[j];
+    CE(rkc_stage(n, dst, Y0, Ym1, Ym2, h->rhs, h->rkF0, 1.0 - mu - nu, mu, nu, h->rkc_mut[j] * dt,
+                 h->rkc_gamt[j] * dt, false, s));
+    Ym2 = Ym1;
+    Ym1 = dst;
+  }
+  if (h->nb > 0) {
+    CE(vort2flux<double>(h, out, h->psi, nullptr, h->qs1, h->rings));
+    CE(reg_gather<double>(g, h->qs1, h->d_q0, h->body_idx, h->weight, h->nb, h->ftmp, 1, g.nq, h->nf, s));
+    CE(gemv_rowmajor(h->binv_rm, h->ftmp, h->fb, h->nf, s));
+    CE(enqueue_stress(h));
+    CE(reg_scatter_rot<double>(g, h->fb, h->body_idx, h->weight, h->nb, h->qtmp, h->gtmp, 1, h->nf, h->status + 1,
+                               h->d_box, h->box_ready, s));
+    CE(axpby<double>(out, h->gtmp, -1.0, 1.0, g.nG, s));
+  }
+  return vort2flux<double>(h, out, h->psi, h->q, nullptr, h->rings);
+}
+
 cudaError_t enqueue_step_mode(ib_handle* h, int p) {
+  if (h->scheme == IB_SCHEME_RKC) return enqueue_rkc_step(h, p);
   return h->precision == IB_PREC_MIXED ? enqueue_step<df64>(h, p) : enqueue_step<double>(h, p);
+}
+
+// Second-order Runge-Kutta-Chebyshev coefficients with damping eps = 2/13 (Sommeijer, Shampine
+// and Verwer, "RKC: an explicit solver for parabolic PDEs", 1998), from the Chebyshev
+// polynomials T_j and their derivatives at w0 = 1 + eps / s^2.  Returns the length beta(s) of
+// the stability interval on the negative real axis.
+double rkc_coefficients(int S, std::vector<double>& mu, std::vector<double>& nu, std::vector<double>& mut,
+                        std::vector<double>& gamt) {
+  const double eps = 2.0 / 13.0, w0 = 1.0 + eps / ((double)S * S);
+  std::vector<double> T(S + 1), T1(S + 1), T2(S + 1);
+  T[0] = 1.0; T[1] = w0;
+  T1[0] = 0.0; T1[1] = 1.0;
+  T2[0] = 0.0; T2[1] = 0.0;
+  for (int j = 2; j <= S; ++j) {
+    T[j] = 2.0 * w0 * T[j - 1] - T[j - 2];
+    T1[j] = 2.0 * T[j - 1] + 2.0 * w0 * T1[j - 1] - T1[j - 2];
+    T2[j] = 4.0 * T1[j - 1] + 2.0 * w0 * T2[j - 1] - T2[j - 2];
+  }
+  const double w1 = T1[S] / T2[S];
+  std::vector<double> b(S + 1);
+  for (int j = 2; j <= S; ++j) b[j] = T2[j] / (T1[j] * T1[j]);
+  b[0] = b[1] = b[2];
+  mu.assign(S + 1, 0.0); nu.assign(S + 1, 0.0); mut.assign(S + 1, 0.0); gamt.assign(S + 1, 0.0);
+  mut[1] = b[1] * w1;
+  for (int j = 2; j <= S; ++j) {
+    mu[j] = 2.0 * b[j] * w0 / b[j - 1];
+    nu[j] = -b[j] / b[j - 2];
+    mut[j] = 2.0 * b[j] * w1 / b[j - 1];
+    gamt[j] = -(1.0 - b[j - 1] * T[j - 1]) * mut[j];
+  }
+  return (w0 + 1.0) * T2[S] / T1[S];
 }
 
 // B z for the current weights (B_Times, cnab/ops.jl:125-143): E q1(Vort2Flux(Ainv_1 C^T E^T z)).
@@ -759,7 +858,10 @@ cudaError_t schur_columns(ib_handle* h, int c0, int n, double* Wa, double* Gb, d
   };
   S *A = view<S>(Wa), *G = view<S>(Gb), *P = view<S>(Pb), *Q = view<S>(Qb), *R = view<S>(Rb);
   CE(unit_scatter_rot<S>(g, h->body_idx, h->weight, h->nb, c0, n, A, s));
-  CE(psolve(A, G, nullptr, op_cn1(h)));
+  if (h->scheme == IB_SCHEME_RKC)  // explicit scheme: B' = E C Lap^-1 C^T E^T, no implicit operator
+    CE(cudaMemcpyAsync(G, A, sizeof(S) * n * nG, cudaMemcpyDeviceToDevice, s));
+  else
+    CE(psolve(A, G, nullptr, op_cn1(h)));
   if (L > 1) CE(cudaMemsetAsync(G + (int64_t)n * nG, 0, sizeof(S) * (L - 1) * n * nG, s));
   for (int l = 1; l < L; ++l) CE(coarsify<S>(g, G + (int64_t)l * n * nG, G + (int64_t)(l - 1) * n * nG, n, nG, s));
   CE(psolve(G + (int64_t)(L - 1) * n * nG, P + (int64_t)(L - 1) * n * nG, nullptr, op_lap(h)));
@@ -1585,6 +1687,26 @@ int ib_create(const ib_problem* p, ib_handle** out) {
   h->nbodies = p->nbodies;
   h->nb = nb;
   h->nf = 2 * nb;
+  if (p->scheme != IB_SCHEME_CNAB && p->scheme != IB_SCHEME_RKC) return bail(fail(h, IB_ERR_INVALID, "unknown scheme"));
+  h->scheme = p->scheme;
+  if (h->scheme == IB_SCHEME_RKC) {
+    if (p->precision != IB_PREC_FP64)
+      return bail(fail(h, IB_ERR_UNSUPPORTED, "the Runge-Kutta-Chebyshev scheme is FP64 only"));
+    if (p->motion != IB_MOTION_STATIC)
+      return bail(fail(h, IB_ERR_UNSUPPORTED, "the Runge-Kutta-Chebyshev scheme takes bodies fixed in the grid"));
+    if (p->rkc_stages < 0 || p->rkc_stages == 1 || p->rkc_stages > 64)
+      return bail(fail(h, IB_ERR_INVALID, "rkc_stages must be 0 (automatic) or 2..64"));
+    // the fewest stages whose stability interval covers 1.5 x dt x the finest level's viscous
+    // spectral radius 8 / (Re h^2)
+    const double need = 1.5 * p->dt * 8.0 / (p->re * p->h * p->h);
+    int S = p->rkc_stages;
+    if (S == 0) {
+      S = 2;
+      while (S < 64 && rkc_coefficients(S, h->rkc_mu, h->rkc_nu, h->rkc_mut, h->rkc_gamt) < need) ++S;
+    }
+    rkc_coefficients(S, h->rkc_mu, h->rkc_nu, h->rkc_mut, h->rkc_gamt);
+    h->rkc_s = S;
+  }
   // IB_PREC_MIXED_TC is the mixed-precision solve with the tensor-core transform passes
   h->precision = p->precision == IB_PREC_FP64 ? IB_PREC_FP64 : IB_PREC_MIXED;
   const bool want_tc = p->precision == IB_PREC_MIXED_TC;
@@ -1682,6 +1804,10 @@ int ib_create(const ib_problem* p, ib_handle** out) {
       return bail(fail(h, IB_ERR_CUDA, "ring transfer tables", e));
   }
   AL(h->status, 4); AL(h->d_counter, 1); AL(h->d_box, 4);
+  if (h->scheme == IB_SCHEME_RKC) {
+    AL(h->rkY[0], L * nG); AL(h->rkY[1], L * nG); AL(h->rkF0, L * nG);
+    AL(h->d_alpha_rkc, L); AL(h->d_fac_rkc, L);
+  }
   if (h->precision == IB_PREC_MIXED && h->cn_pred) AL(h->cprev, nG);
   for (auto& ev : h->stress_ev)
     if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) {
@@ -1715,6 +1841,17 @@ int ib_create(const ib_problem* p, ib_handle** out) {
     std::vector<double> ones(L, 1.0);
     if ((e = cudaMemcpy(h->d_one, ones.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
       return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    if (h->scheme == IB_SCHEME_RKC) {
+      // explicit viscous term nu lap / hc^2 and its ring weight, per level
+      std::vector<double> visc(L);
+      for (int l = 0; l < L; ++l) {
+        const double hc = g.h * std::ldexp(1.0, l);
+        visc[l] = 1.0 / (h->re * hc * hc);
+      }
+      if ((e = cudaMemcpy(h->d_alpha_rkc, visc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaMemcpy(h->d_fac_rkc, visc.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return bail(fail(h, IB_ERR_CUDA, "parameter upload", e));
+    }
     if (h->precision == IB_PREC_MIXED) {
       std::vector<float> l32(lap.begin(), lap.end()), c32(cn1.begin(), cn1.end());
       if ((e = cudaMemcpy(h->mLap32, l32.data(), sizeof(float) * l32.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -2189,6 +2326,8 @@ int ib_get_info(ib_handle* h, ib_info* info) {
   info->setup_ms = h->setup_ms;
   info->vort2flux_order = h->v2f_levels ? IB_V2F_LEVELS : IB_V2F_SEQUENTIAL;
   info->transform_form = h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM);
+  info->scheme = h->scheme;
+  info->rkc_stages = h->rkc_s;
   return IB_OK;
 }
 

@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kNTX * kNTY) k_nonlin_rhs(Geometry g, NonlinAr
 // edges[l] = sum_{l' = l}^{nlev-2} fac[l'] * get_bc(gamma[l'+1]) on the four edges.
 template <typename T>
 __global__ void k_trial_rings(Geometry g, const T* __restrict__ gamma, T* __restrict__ bcn, T* __restrict__ edges,
-                              const double* __restrict__ fac) {
+                              const double* __restrict__ fac, int accumulate) {
   pdl_begin();
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int ne = 2 * ncol + 2 * nrow;
@@ -324,9 +324,31 @@ __global__ void k_trial_rings(Geometry g, const T* __restrict__ gamma, T* __rest
       else if (e < 2 * ncol + nrow) ridx = g.L + 1 + (e - 2 * ncol);
       else ridx = g.R + 1 + (e - 2 * ncol - nrow);
       T acc = T(0);
-      for (int lp = nl - 2; lp >= l; --lp) acc += (T)fac[lp] * ring_value(g, gamma + (int64_t)(lp + 1) * g.nG, ridx);
+      if (accumulate) {
+        for (int lp = nl - 2; lp >= l; --lp) acc += (T)fac[lp] * ring_value(g, gamma + (int64_t)(lp + 1) * g.nG, ridx);
+      } else if (l < nl - 1) {
+        acc = (T)fac[l] * ring_value(g, gamma + (int64_t)(l + 1) * g.nG, ridx);
+      }
       edges[u] = acc;
     }
+  }
+}
+
+// One Runge-Kutta-Chebyshev stage, elementwise over n values:
+//   Y = a0 Y0 + a1 Ym1 + a2 Ym2 + c1 (G - Ym1) + c0 F0,   G = Ym1 + F(Ym1)
+// (Ym2 may be null when a2 = 0; Y may alias Ym2).  With store_f0, F0 = G - Ym1 is also written.
+__global__ void k_rkc_stage(int64_t n, double* __restrict__ Y, const double* __restrict__ Y0, const double* Ym1,
+                            const double* Ym2, const double* __restrict__ G, double* F0, double a0, double a1,
+                            double a2, double c1, double c0, int store_f0) {
+  pdl_begin();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double ym1 = Ym1[i];
+    const double f = G[i] - ym1;
+    if (store_f0) F0[i] = f;
+    double y = a0 * Y0[i] + a1 * ym1 + c1 * f;
+    if (Ym2) y += a2 * Ym2[i];
+    if (!store_f0) y += c0 * F0[i];
+    Y[i] = y;
   }
 }
 
@@ -383,10 +405,18 @@ cudaError_t nonlin_rhs(const Geometry& g, const NonlinArgs<T>& a, cudaStream_t s
   return launch_k(k_nonlin_rhs<T>, dim3(tiles < 65535 * 8 ? tiles : 65535 * 8), dim3(kNTX * kNTY), 0, s, g, a);
 }
 template <typename T>
-cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac, cudaStream_t s) {
+cudaError_t trial_rings(const Geometry& g, const T* gamma, T* bcn, T* edges, const double* fac, cudaStream_t s,
+                        bool accumulate) {
   const int64_t n = (int64_t)g.nlev * g.nbc + (int64_t)g.nlev * (2 * (g.nx - 1) + 2 * (g.ny - 1));
-  return launch_k(k_trial_rings<T>, dim3(blocks_for(n)), dim3(kThreads), 0, s, g, gamma, bcn, edges, fac);
+  return launch_k(k_trial_rings<T>, dim3(blocks_for(n)), dim3(kThreads), 0, s, g, gamma, bcn, edges, fac,
+                  accumulate ? 1 : 0);
 }
+cudaError_t rkc_stage(int64_t n, double* Y, const double* Y0, const double* Ym1, const double* Ym2, const double* G,
+                      double* F0, double a0, double a1, double a2, double c1, double c0, bool store_f0, cudaStream_t s) {
+  return launch_k(k_rkc_stage, dim3(blocks_for(n)), dim3(kThreads), 0, s, n, Y, Y0, Ym1, Ym2, G, F0, a0, a1, a2, c1, c0,
+                  store_f0 ? 1 : 0);
+}
+
 template <typename T>
 cudaError_t fill(T* p, T v, int64_t n, cudaStream_t s) {
   k_fill<T><<<blocks_for(n), kThreads, 0, s>>>(p, v, n);
@@ -404,7 +434,7 @@ cudaError_t axpby(T* y, const T* x, T a, T b, int64_t n, cudaStream_t s) {
   template cudaError_t curl<T>(const Geometry&, const T*, const T*, T*, int, cudaStream_t);          \
   template cudaError_t rot<T>(const Geometry&, const T*, T*, int, cudaStream_t);                     \
   template cudaError_t nonlin_rhs<T>(const Geometry&, const NonlinArgs<T>&, cudaStream_t);           \
-  template cudaError_t trial_rings<T>(const Geometry&, const T*, T*, T*, const double*, cudaStream_t); \
+  template cudaError_t trial_rings<T>(const Geometry&, const T*, T*, T*, const double*, cudaStream_t, bool); \
   template cudaError_t fill<T>(T*, T, int64_t, cudaStream_t);                                        \
   template cudaError_t axpby<T>(T*, const T*, T, T, int64_t, cudaStream_t);
 IB_INST(double)

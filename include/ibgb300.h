@@ -50,6 +50,14 @@ extern "C" {
                                GEMM against the sine matrix on the tensor cores (FP32 accumulation);
                                both axes a multiple of 128 cells; Vort2Flux level by level */
 
+/* time-stepping scheme (ib_problem.scheme) */
+#define IB_SCHEME_CNAB 0  /* SchemeCNAB(dt), src/schemes.jl:19-26: the default */
+#define IB_SCHEME_RKC 1   /* SchemeRKC(dt), src/schemes.jl:3-12: declared by the reference but given no
+                             solver there; here the s-stage second-order Runge-Kutta-Chebyshev method
+                             (damping 2/13) on dGamma/dt = nu lap(Gamma) + N(Gamma), explicit, then the
+                             immersed-boundary projection with B' = E C Lap^-1 C^T E^T; FP64, bodies
+                             fixed in the grid */
+
 /* body motion */
 #define IB_MOTION_STATIC 0          /* RigidBody{GridFrame}: E and B inverse built once */
 #define IB_MOTION_PRESCRIBED 1      /* RigidBody{RelativeFrame}: xb in the body frame, rigid
@@ -83,6 +91,10 @@ typedef struct ib_problem {
   int32_t refine_sweeps;        /* IB_PREC_MIXED: residual sweeps per solve: 1 or 2 everywhere, or
                                    0 (default): 2, except 1 for the Vort2Flux solves of the third
                                    and coarser levels (they only feed boundary rings) */
+  int32_t scheme;               /* IB_SCHEME_* (0: CNAB) */
+  int32_t rkc_stages;           /* IB_SCHEME_RKC: stages s >= 2, or 0: the fewest whose stability
+                                   interval covers 1.5 x dt x the finest level's viscous spectral
+                                   radius 8 / (Re h^2) */
 } ib_problem;
 
 typedef struct ib_handle ib_handle;

@@ -22,6 +22,8 @@ typedef struct ib_info {
   double setup_ms;           /* wall time of ib_create (tables, delta weights, Schur inverse) */
   int32_t vort2flux_order;   /* the order in effect: IB_V2F_LEVELS or IB_V2F_SEQUENTIAL */
   int32_t transform_form;    /* the sine-transform passes in effect: IB_FORM_* */
+  int32_t scheme;            /* IB_SCHEME_* */
+  int32_t rkc_stages;        /* stages of the Runge-Kutta-Chebyshev scheme (0 for CNAB) */
 } ib_info;
 
 #define IB_FORM_STOCKHAM 0   /* shared-memory Stockham FFT passes, 64 threads per line */

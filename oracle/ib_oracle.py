@@ -873,3 +873,122 @@ def state_from_checkpoint(prob: Problem, ck: dict) -> State:
     st.nonlin = [a.copy() for a in ck["nonlin"]]
     st.fb = ck["fb"].copy()
     return st
+
+
+# ---------------------------------------------------------------------------
+# SchemeRKC (src/schemes.jl:3-12, "Runge-Kutta-Chebyshev scheme"): declared by the reference,
+# which defines no state or solver for it.  This is the definition libibgb300 implements
+# (IB_SCHEME_RKC), restated: the s-stage second-order RKC method with damping eps = 2/13
+# (Sommeijer, Shampine & Verwer 1998) on dGamma/dt = F(Gamma), per level
+#   F_l = N_l(Gamma) + (1 / (Re hc_l^2)) (apply_bc(get_bc(Gamma_{l+1})) - lap5(Gamma_l)),
+# N_l the CNAB scheme's nonlinear term with its rings (cnab/ops.jl:151-167, timestepping.jl:
+# 48-58), then the projection Gamma_1 -= C^T E^T Fb with Fb = B'^-1 E(q1 + q0),
+# B' = E C Lap^-1 C^T E^T (B_Times without the implicit operator).
+# ---------------------------------------------------------------------------
+def rkc_coefficients(S: int):
+    """(mu, nu, mut, gamt, beta): stage coefficients indexed 1..S and the stability interval."""
+    eps = 2.0 / 13.0
+    w0 = 1.0 + eps / (S * S)
+    T, T1, T2 = [1.0, w0], [0.0, 1.0], [0.0, 0.0]
+    for j in range(2, S + 1):
+        T.append(2 * w0 * T[j - 1] - T[j - 2])
+        T1.append(2 * T[j - 1] + 2 * w0 * T1[j - 1] - T1[j - 2])
+        T2.append(4 * T1[j - 1] + 2 * w0 * T2[j - 1] - T2[j - 2])
+    w1 = T1[S] / T2[S]
+    b = [0.0] * (S + 1)
+    for j in range(2, S + 1):
+        b[j] = T2[j] / T1[j] ** 2
+    b[0] = b[1] = b[2]
+    mu, nu, mut, gamt = [0.0] * (S + 1), [0.0] * (S + 1), [0.0] * (S + 1), [0.0] * (S + 1)
+    mut[1] = b[1] * w1
+    for j in range(2, S + 1):
+        mu[j] = 2 * b[j] * w0 / b[j - 1]
+        nu[j] = -b[j] / b[j - 2]
+        mut[j] = 2 * b[j] * w1 / b[j - 1]
+        gamt[j] = -(1 - b[j - 1] * T[j - 1]) * mut[j]
+    return mu, nu, mut, gamt, (w0 + 1) * T2[S] / T1[S]
+
+
+def lap5(Y):
+    """4 Y - (its four neighbours), zero outside the array (rot o curl with zero ring)."""
+    out = 4.0 * Y
+    out[..., :, 1:] -= Y[..., :, :-1]
+    out[..., :, :-1] -= Y[..., :, 1:]
+    out[..., 1:, :] -= Y[..., :-1, :]
+    out[..., :-1, :] -= Y[..., 1:, :]
+    return out
+
+
+def b_times_explicit(z, reg: Reg, g: Grid, lam):
+    """B' z = E q1(vort2flux(C^T E^T z)) (B_Times, cnab/ops.jl:125-143, without Ainv)."""
+    z = np.asarray(z, dtype=np.float64)
+    lead = z.shape[:-1]
+    G = np.zeros(lead + (g.nlevels,) + g.gshape)
+    G[..., 0, :, :] = rot(reg_scatter(z, reg, g), g)
+    _, q = vort2flux(G, g, lam)
+    return reg_gather(q[..., 0, :], reg, g)
+
+
+class RKCSolver(Solver):
+    """SchemeRKC restated (see above): bodies fixed in the grid, FP64."""
+
+    def __init__(self, prob: Problem, stages: int = 0, batch: int = 64):
+        g = prob.grid
+        self.prob, self.g = prob, g
+        self.lam = lap_eigs(g)
+        self.reg = reg_update(prob.xb, g)
+        nf = 2 * self.reg.body_idx.shape[0]
+        if nf:
+            B = np.empty((nf, nf))
+            for c0 in range(0, nf, batch):
+                c1 = min(nf, c0 + batch)
+                E = np.zeros((c1 - c0, nf))
+                E[np.arange(c1 - c0), np.arange(c0, c1)] = 1.0
+                B[:, c0:c1] = b_times_explicit(E, self.reg, g, self.lam).T
+            self.Bmat, self.Binv = B, np.linalg.inv(B)
+        else:
+            self.Bmat = self.Binv = np.zeros((0, 0))
+        if stages == 0:
+            need = 1.5 * prob.dt * 8.0 / (prob.Re * g.h * g.h)
+            stages = 2
+            while stages < 64 and rkc_coefficients(stages)[4] < need:
+                stages += 1
+        self.stages = stages
+        self.coef = rkc_coefficients(stages)
+
+    def F(self, Y, q, q0):
+        g, prob = self.g, self.prob
+        L = g.nlevels
+        out = np.empty_like(Y)
+        for lev in range(1, L + 1):
+            bcv = get_bc(Y[lev], g) if lev < L else np.zeros(g.nbc)
+            nl = nonlinear(q[lev - 1], q0[lev - 1], Y[lev - 1], 0.25 * bcv, lev, g)
+            visc = -lap5(Y[lev - 1])
+            apply_bc(visc, bcv, 1.0, g)
+            hc = g.hc(lev)
+            out[lev - 1] = nl + visc / (prob.Re * hc * hc)
+        return out
+
+    def advance(self, st: State, t: float):
+        g, prob = self.g, self.prob
+        dt = prob.dt
+        mu, nu, mut, gamt, _ = self.coef
+        st.q0 = base_flux(g, *prob.uv(t))
+        Y0 = st.gamma.copy()
+        F0 = self.F(Y0, st.q, st.q0)
+        Ym2, Ym1 = Y0, Y0 + mut[1] * dt * F0
+        for j in range(2, self.stages + 1):
+            _, q = vort2flux(Ym1, g, self.lam)
+            Fj = self.F(Ym1, q, st.q0)
+            Yj = (1 - mu[j] - nu[j]) * Y0 + mu[j] * Ym1 + nu[j] * Ym2 + mut[j] * dt * Fj + gamt[j] * dt * F0
+            Ym2, Ym1 = Ym1, Yj
+        out = Ym1
+        if self.Binv.size:
+            _, qs = vort2flux(out, g, self.lam)
+            ftmp = reg_gather(qs[0] + st.q0[0], self.reg, g)
+            st.fb = self.Binv @ ftmp
+            update_stress(st, prob)
+            out[0] -= rot(reg_scatter(st.fb, self.reg, g), g)
+        st.gamma = out
+        st.psi, st.q = vort2flux(st.gamma, g, self.lam)
+        st.t = float(t)

@@ -82,10 +82,16 @@ def test_workloads(ib):
 
 
 def test_schemes_without_solver_raise(ib):
+    """SchemeCNAB and SchemeRKC have solvers; another scheme type has no state type."""
     g = ib.MultiLevel(ib.UniformGrid(0.1, (-1.0, 2.2), (-1.6, 1.6)), 2)
-    prob = ib.Problem(ib.StreamFcnFluid(g, (1.0, 0.0), 100.0), ib.BodyGroup(), ib.SchemeRKC(0.01))
+
+    class SchemeOther:
+        dt = 0.01
+    prob = ib.Problem(ib.StreamFcnFluid(g, (1.0, 0.0), 100.0), ib.BodyGroup(), SchemeOther())
     with pytest.raises(NotImplementedError):
         ib.initstate(prob)
+    prob = ib.Problem(ib.StreamFcnFluid(g, (1.0, 0.0), 100.0), ib.BodyGroup(), ib.SchemeRKC(0.01))
+    assert ib.initstate(prob).t == 0.0
 
 
 def _declared_symbols():

@@ -289,3 +289,43 @@ def test_checkpoint_format_round_trip(O, tmp_path):
     bad.write_bytes(raw[:-8])
     with pytest.raises(ValueError):
         O.read_checkpoint(bad, g)
+
+
+def test_rkc_coefficients_and_stability_interval(O):
+    """RKC with 2/13 damping: the stability interval grows like s^2 toward the published
+    ~0.653 s^2, and the stage coefficients are consistent (exact for dY/dt = 1)."""
+    prev = 0.0
+    for S in (2, 3, 5, 10, 20):
+        mu, nu, mut, gamt, beta = O.rkc_coefficients(S)
+        assert 0.45 * S * S < beta < 0.66 * S * S and beta / (S * S) > prev
+        prev = beta / (S * S)
+        # integrate dy/dt = 1 from 0 over dt = 1: every stage's y equals its stage time c_j,
+        # and the last one reaches 1
+        y = [0.0, mut[1]]
+        for j in range(2, S + 1):
+            y.append((1 - mu[j] - nu[j]) * 0.0 + mu[j] * y[j - 1] + nu[j] * y[j - 2] + mut[j] + gamt[j])
+        assert abs(y[S] - 1.0) < 1e-12
+
+
+def test_rkc_is_second_order_in_time(O):
+    """No body, smooth vorticity on a 2-level grid: halving dt quarters the error at a fixed time."""
+    g = small_grid(O, 32, 32, 2)
+    prob0 = O.Problem(g, 0.02, 50.0, np.zeros((0, 2)), np.zeros(0), [], freestream=(0.3, 0.1))
+    xs = (np.arange(1, g.nx) - g.nx / 2) / (g.nx / 6)
+    ys = (np.arange(1, g.ny) - g.ny / 2) / (g.ny / 6)
+    omega = np.exp(-(xs[None, :] ** 2 + ys[:, None] ** 2))
+
+    def run(dt, n):
+        prob = O.Problem(g, dt, prob0.Re, prob0.xb, prob0.ds, [], freestream=prob0.freestream)
+        st = O.init_state(prob)
+        st.gamma[0] = 1e-2 * omega * g.h ** 2
+        st.psi, st.q = O.vort2flux(st.gamma, g, O.lap_eigs(g))
+        sol = O.RKCSolver(prob, stages=3)
+        for i in range(n):
+            sol.advance(st, i * dt)
+        return st.gamma[0].copy()
+    ref = run(0.0025, 32)
+    e1 = np.linalg.norm(run(0.02, 4) - ref)
+    e2 = np.linalg.norm(run(0.01, 8) - ref)
+    e3 = np.linalg.norm(run(0.005, 16) - ref)
+    assert 3.0 < e1 / e2 < 5.0 and 3.0 < e2 / e3 < 5.5, (e1, e2, e3)

@@ -921,20 +921,40 @@ def solve_(state: State, prob: Problem, tlims, save=(), call=(), solver: Solver 
         return p
 
     pushers = [pusher(cb, r) for cb, r in zip(save, results)]
-    if not callers and not pushers:
-        for c0 in range(0, len(ts), 1024):
-            solver.advance_n(state, ts[c0:c0 + 1024])
-        return results
-    for i, t in enumerate(ts, start=1):
-        solver.advance(state, float(t))
+    # Steps at which some callback fires, known before stepping: every caller's decision is a
+    # function of the step index and time alone.  The steps in between run as batches of
+    # captured-graph replays without a host round trip.
+    fire = sorted(set().union(*(_fire_steps(cb, ts, dt) for cb in (*save, *call))))
+    done = 0
+    for k in fire:
+        for c0 in range(done, k, 1024):
+            solver.advance_n(state, ts[c0:min(k, c0 + 1024)])
+        done = k
         for p in pushers:
-            p(i, state)
+            p(k, state)
         stop = False
         for f in callers:
-            stop |= f(i, state) == StopIteration()
+            stop |= f(k, state) == StopIteration()
         if stop:
-            break
+            return results
+    for c0 in range(done, len(ts), 1024):
+        solver.advance_n(state, ts[c0:c0 + 1024])
     return results
+
+
+def _fire_steps(cb: StateCallback, ts: np.ndarray, dt: float) -> set:
+    """The 1-based step indices at which ``cb``'s caller calls it over the time range ``ts``."""
+    caller = _callback_caller(dt, StateCallback(lambda s: True, cb.timesteps))
+
+    class _At:
+        t = 0.0
+    at = _At()
+    out = set()
+    for i, t in enumerate(ts, start=1):
+        at.t = float(t)
+        if caller(i, at) is not None:
+            out.add(i)
+    return out
 
 
 def solve(prob: Problem, tlims, save=(), call=(), **kw):

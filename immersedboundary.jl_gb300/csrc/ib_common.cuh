@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <cstdint>
 
 #include "df64.cuh"
@@ -465,6 +466,17 @@ struct DeviceGuard {
   }
   DeviceGuard(const DeviceGuard&) = delete;
   DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
+// An NVTX range over a host scope, so that setup, eager steps and their phases (trial state,
+// forcing, projection, CG) show by name on a profiler's timeline.  Inside stream capture a
+// range marks when the phase was captured, not its replays.  Without a profiler attached a
+// range costs a test of a null function pointer.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
 };
 
 // ----------------------------------------------------------------------------------------------

@@ -595,6 +595,7 @@ int conv_blocks(int64_t n) {
 // psi on every level and the trial flux on level 1 (the only level the step reads)
 template <typename S>
 cudaError_t enqueue_trial(ib_handle* h, int p) {
+  ib::Range nvtx_range("trial state");
   const Geometry& g = h->g;
   const int L = g.nlev;
   cudaStream_t s = h->stream;
@@ -630,6 +631,7 @@ cudaError_t enqueue_trial(ib_handle* h, int p) {
 
 // f. update_stress! (states.jl:53-84) and the device C_D / C_L history
 cudaError_t enqueue_stress(ib_handle* h) {
+  ib::Range nvtx_range("stress");
   cudaStream_t s = h->stream;
   CE(update_stress_hd(h->fb, h->nb, h->nbodies, h->body_start, h->ds, h->g.h, h->dt, h->cdcl, h->stress, s));
   return launch_k(k_hist_append, dim3(1), dim3(64), 0, s, (const double*)h->cdcl, h->hist, h->hist_cap, 2 * h->nbodies,
@@ -640,6 +642,7 @@ cudaError_t enqueue_stress(ib_handle* h) {
 // h. Vort2Flux on the new state (timestepping.jl:285); the trial buffer becomes Gamma
 template <typename S>
 cudaError_t enqueue_project(ib_handle* h, int p) {
+  ib::Range nvtx_range("projection");
   const Geometry& g = h->g;
   S* gs = view<S>(h->G[p ^ 1]);
   if (h->nb > 0) {
@@ -696,6 +699,7 @@ cudaError_t enqueue_step(ib_handle* h, int p) {
 //   Vort2Flux of every level (which coarsifies Y_{j-1} in place, as the reference's does to Gamma)
 //   Fb = B'^-1 E(q(Y_s) + q0), B' = E C Lap^-1 C^T E^T;  Gamma_{n+1} = Y_s - C^T E^T Fb on level 1
 cudaError_t enqueue_rkc_step(ib_handle* h, int p) {
+  ib::Range nvtx_range("RKC step");
   const Geometry& g = h->g;
   const int L = g.nlev;
   const int64_t n = (int64_t)L * g.nG;
@@ -879,6 +883,7 @@ cudaError_t schur_columns(ib_handle* h, int c0, int n, double* Wa, double* Gb, d
 // bodies B^-1 only preconditions CG on the exact operator, and a mixed-precision handle
 // assembles it with FP32 transforms.
 int assemble_schur(ib_handle* h) {
+  ib::Range nvtx_range("assemble Schur inverse");
   const Geometry& g = h->g;
   const int L = g.nlev, nf = h->nf;
   const int64_t nG = g.nG;
@@ -959,6 +964,7 @@ int prime_kernels(ib_handle* h) {
 }
 
 int capture_graphs(ib_handle* h) {
+  ib::Range nvtx_range("capture step graphs");
   for (int p = 0; p < 2; ++p) {
     if (h->gexec[p]) { cudaGraphExecDestroy(h->gexec[p]); h->gexec[p] = nullptr; }
     cudaGraph_t graph = nullptr;
@@ -1051,6 +1057,7 @@ int stage_q0(ib_handle* h, double u, double v, const double* kin = nullptr) {
 // Scalars: sc[0] = r.z, sc[1] = p.Ap, sc[2] = new r.z, sc[3] = rhs.rhs, sc[4] = r.r.
 template <typename S>
 int cg_solve(ib_handle* h) {
+  ib::Range nvtx_range("CG solve");
   const int nf = h->nf;
   cudaStream_t s = h->stream;
   double *x = h->fb, *r = h->cg_r, *p = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
@@ -1168,6 +1175,7 @@ void pc_account(ib_handle* h, int64_t solve_step) {
 // step's kinematics, the trial state, Fb by CG, stress, projection and Vort2Flux.
 template <typename S>
 int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
+  ib::Range nvtx_range("moving step");
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   const int p = h->parity;
@@ -1325,6 +1333,7 @@ uint64_t moving_graph_key(const ib_handle* h) {
 
 template <typename S>
 int moving_step_graph(ib_handle* h, double t, double u, double v, const double* kin) {
+  ib::Range nvtx_range("moving step (graph)");
   const Geometry& g = h->g;
   // base flux and kinematics of this step into the pinned slot the graphs copy from (the
   // previous launch is complete: every step ends with a synchronisation)
@@ -1426,6 +1435,7 @@ std::mutex g_tune_mu;
 std::map<std::string, TuneRecord> g_tune_cache;
 
 int autotune(ib_handle* h, bool tune_form, bool tune_v2f, bool lv_base) {
+  ib::Range nvtx_range("autotune");
   const Geometry& g = h->g;
   const int L = g.nlev;
   char keybuf[160];
@@ -1634,6 +1644,7 @@ const char* ib_last_error(const ib_handle* h) {
 }
 
 int ib_create(const ib_problem* p, ib_handle** out) {
+  ib::Range nvtx_range("ib_create");
   const auto t_start = std::chrono::steady_clock::now();
   ib_handle* h = nullptr;
   if (!p || !out) return fail(nullptr, IB_ERR_INVALID, "null argument");
@@ -2049,6 +2060,7 @@ static_assert(sizeof(CkptHeader) == 56, "checkpoint header layout");
 }  // namespace
 
 int ib_checkpoint_save(ib_handle* h, const char* path) {
+  ib::Range nvtx_range("ib_checkpoint_save");
   if (!h || !path) return IB_ERR_INVALID;
   const Geometry& g = h->g;
   const size_t nGL = (size_t)g.nlev * g.nG, nqL = (size_t)g.nlev * g.nq;
@@ -2084,6 +2096,7 @@ int ib_checkpoint_save(ib_handle* h, const char* path) {
 }
 
 int ib_checkpoint_load(ib_handle* h, const char* path) {
+  ib::Range nvtx_range("ib_checkpoint_load");
   if (!h || !path) return IB_ERR_INVALID;
   const Geometry& g = h->g;
   FILE* f = std::fopen(path, "rb");
@@ -2137,6 +2150,7 @@ int ib_advance(ib_handle* h, double t, double u, double v) {
 }
 
 int ib_advance_n(ib_handle* h, int32_t n, const double* t, const double* uv) {
+  ib::Range nvtx_range("ib_advance_n");
   if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
   DeviceGuard dev_guard_(h->device);
   CK(dev_guard_.err);
@@ -2160,6 +2174,7 @@ int ib_advance_kin(ib_handle* h, double t, double u, double v, const double* kin
 }
 
 int ib_advance_n_kin(ib_handle* h, int32_t n, const double* t, const double* uv, const double* kin) {
+  ib::Range nvtx_range("ib_advance_n_kin");
   if (!h || n < 0 || (n > 0 && (!t || !uv))) return IB_ERR_INVALID;
   if (h->motion != IB_MOTION_PRESCRIBED) return ib_advance_n(h, n, t, uv);
   if (n > 0 && !kin) return fail(h, IB_ERR_INVALID, "moving bodies need kinematics");
@@ -2250,6 +2265,7 @@ int ib_get_body_points(ib_handle* h, double* xb, double* vb) {
 }
 
 int ib_vort2flux(ib_handle* h) {
+  ib::Range nvtx_range("ib_vort2flux");
   if (!h) return IB_ERR_INVALID;
   DeviceGuard dev_guard_(h->device);
   CK(dev_guard_.err);
@@ -2649,6 +2665,7 @@ int ib_learn_sample_count(ib_handle* h, int32_t* count) {
 }
 
 int ib_learn_train(ib_handle* h, int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss) {
+  ib::Range nvtx_range("ib_learn_train");
   if (!h || !h->mlp) return h ? fail(h, IB_ERR_INVALID, "no network (ib_learn_init)") : IB_ERR_INVALID;
   if (epochs < 1 || batch < 1 || batch > learn::kMaxBatch || !(lr > 0))
     return fail(h, IB_ERR_INVALID, "epochs, batch (1..512) and learning rate must be positive");
@@ -2965,12 +2982,14 @@ int ib_ensemble_destroy(ib_ensemble* e) {
 }
 
 int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, double* device_ms) {
+  ib::Range nvtx_range("ib_ensemble_advance_n");
   if (e && e->any_moving) return efail(e, IB_ERR_INVALID, "moving members need kinematics (ib_ensemble_advance_n_kin)");
   return ib_ensemble_advance_n_kin(e, nsteps, t, uv, nullptr, device_ms);
 }
 
 int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, const double* kin,
                               double* device_ms) {
+  ib::Range nvtx_range("ib_ensemble_advance_n_kin");
   if (!e || nsteps < 0 || (nsteps > 0 && (!t || !uv))) return IB_ERR_INVALID;
   if (e->any_moving && nsteps > 0 && !kin) return efail(e, IB_ERR_INVALID, "moving members need kinematics");
   DeviceGuard dev_guard_(e->device);

@@ -25,6 +25,9 @@ const libibgb300 = joinpath(@__DIR__, "..", "libibgb300.so")
 
 const IB_PREC_FP64 = Int32(0)
 const IB_PREC_MIXED = Int32(1)
+const IB_PREC_MIXED_TC = Int32(2)
+const IB_SCHEME_CNAB = Int32(0)
+const IB_SCHEME_RKC = Int32(1)
 const IB_MOTION_STATIC = Int32(0)
 const IB_MOTION_PRESCRIBED = Int32(1)
 const IB_PC_SCHUR_REF = Int32(1)
@@ -56,6 +59,8 @@ struct IbProblem
     device::Int32
     history_capacity::Int32
     refine_sweeps::Int32
+    scheme::Int32       # IB_SCHEME_*
+    rkc_stages::Int32   # SchemeRKC: 0 picks the fewest stable stages
 end
 
 struct IBError <: Exception
@@ -82,7 +87,7 @@ end
 ImmersedBoundary.problemof(s::GB300Solver) = s.prob
 
 function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, sync=:all, precondition=true,
-                     vort2flux_order=IB_V2F_AUTO)
+                     vort2flux_order=IB_V2F_AUTO, rkc_stages=0)
     fluid = fluidof(prob)
     grid = discretize(fluid)
     base = baselevel(grid)
@@ -92,13 +97,17 @@ function GB300Solver(prob::Problem, state; precision=IB_PREC_FP64, device=0, syn
     xb = vcat((b.xb for b in bodies)...)          # nb x 2, column-major
     ds = vcat((b.ds for b in bodies)...)
     scheme = schemeof(prob)
+    # SchemeRKC (src/schemes.jl:8-10) carries only dt; the beta fields are CNAB's
+    rkc = scheme isa SchemeRKC
+    beta = rkc ? (1.5, -0.5) : (scheme.β[1], scheme.β[2])
     mv = moving(bodies)
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve npts xb ds begin
         p = IbProblem(fluid.domain.nx, fluid.domain.ny, nlevels(grid), first(xs), first(ys),
-                      gridstep(base), scheme.dt, scheme.β[1], scheme.β[2], fluid.Re,
+                      gridstep(base), scheme.dt, beta[1], beta[2], fluid.Re,
                       length(npts), pointer(npts), pointer(xb), pointer(ds),
-                      mv ? IB_MOTION_PRESCRIBED : IB_MOTION_STATIC, precision, device, 4096, 0)
+                      mv ? IB_MOTION_PRESCRIBED : IB_MOTION_STATIC, precision, device, 4096, 0,
+                      rkc ? IB_SCHEME_RKC : IB_SCHEME_CNAB, rkc_stages)
         st = ccall((:ib_create, libibgb300), Cint, (Ref{IbProblem}, Ref{Ptr{Cvoid}}), p, handle)
         check(st, C_NULL)
     end
@@ -161,6 +170,8 @@ function ImmersedBoundary.advance!(state, solver::GB300Solver, t::Float64)
     # velocity (base_flux! for a moving grid, the reference's TODO at fluid-ops.jl:419)
     gframe = fluidof(solver.prob).domain.frame
     if gframe isa RelativeFrame
+        # a rotating grid would add fictitious terms the stream-function step does not model
+        (gframe.θ(t) == 0 && gframe.Ω(t) == 0) || error("a rotating grid frame is not supported")
         gv = gframe.v(t)
         u, v = u - gv[1], v - gv[2]
     end
@@ -184,14 +195,39 @@ function ImmersedBoundary.advance!(state, solver::GB300Solver, t::Float64)
     return nothing
 end
 
-"Make `solve` / `solve!` use the GB300 solver for stream-function / CNAB problems."
+"""
+Make `solve` / `solve!` use the GB300 solver for stream-function problems: CNAB, and
+SchemeRKC, which the reference declares without a state or solver type (its state here is
+CNAB's: `qty`, `nonlin` (unused by RKC) and `t`).
+"""
 function use_gb300!(; precision=IB_PREC_FP64, device=0, sync=:all)
     @eval function ImmersedBoundary.solvertype(
-        ::Problem{<:StreamFcnFluid{<:StreamFcnGrid},<:Any,<:SchemeCNAB}
+        ::Problem{<:StreamFcnFluid{<:StreamFcnGrid},<:Any,<:Union{SchemeCNAB,SchemeRKC}}
     )
         return (prob, state) -> GB300Solver(prob, state; precision=$precision, device=$device, sync=$(QuoteNode(sync)))
     end
+    @eval ImmersedBoundary.statetype(::Problem{<:StreamFcnFluid{<:StreamFcnGrid},<:Any,<:SchemeRKC}) =
+        ImmersedBoundary.StreamFcn.CNAB.State
     return nothing
+end
+
+"Write the solver's state to a checkpoint file (`ib_checkpoint_save`)."
+function save_checkpoint(s::GB300Solver, path::AbstractString)
+    check(ccall((:ib_checkpoint_save, libibgb300), Cint, (Ptr{Cvoid}, Cstring), s.handle, path), s.handle)
+end
+
+"Restore the solver from a checkpoint file of the same problem and refresh `state` from it."
+function load_checkpoint!(s::GB300Solver, state, path::AbstractString)
+    check(ccall((:ib_checkpoint_load, libibgb300), Cint, (Ptr{Cvoid}, Cstring), s.handle, path), s.handle)
+    pull_state!(s, state)
+    pull_stress!(s, state)
+    tref = Ref{Cdouble}(0.0)
+    check(ccall((:ib_get_state, libibgb300), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                 Ptr{Float64}, Ref{Cdouble}),
+                s.handle, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, C_NULL, tref), s.handle)
+    state.t = tref[]
+    return state
 end
 
 end # module

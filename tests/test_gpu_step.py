@@ -128,6 +128,25 @@ def test_stop_iteration_and_at_indices(ib):
     assert list(res[0]) == pytest.approx([wl.dt, 2 * wl.dt])
 
 
+def test_sparse_callbacks_run_batched_and_match_single_steps(ib):
+    """at_indices / at_times callbacks: the steps between firings run as graph-replay batches
+    and the samples equal those of a per-step run."""
+    wl = ib.workloads.scaled(ib.workloads.cylinder_small(), 64, 64, nlevels=2)
+    prob = wl.problem()
+    every = ib.solve(prob, (0.0, 29 * wl.dt), save=(ib.each_timestep(lambda s: s.qty.gamma.copy()),))[0]
+    idx = [1, 7, 20, 30]
+    times = [0.0, 4.6 * wl.dt, 12.2 * wl.dt]
+    res = ib.solve(prob, (0.0, 29 * wl.dt),
+                   save=(ib.at_indices(lambda s: s.qty.gamma.copy(), idx),
+                         ib.at_times(lambda s: s.qty.gamma.copy(), times)))
+    assert len(res[0]) == 4 and len(res[1]) == 3
+    for got, i in zip(res[0], idx):
+        np.testing.assert_array_equal(got, every[i - 1])
+    for got, i in zip(res[1], [1, 6, 13]):
+        np.testing.assert_array_equal(got, every[i - 1])
+    assert res[1].t == pytest.approx([0.0, 5 * wl.dt, 12 * wl.dt])
+
+
 def test_errors_are_reported_not_faulted(ib):
     """A body too close to the edge and a non-finite state come back as status codes."""
     grid = ib.MultiLevel(ib.UniformGrid(0.05, (-1.0, 2.2), (-1.6, 1.6)), 2)

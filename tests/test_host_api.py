@@ -53,6 +53,17 @@ def test_callback_callers(ib):
     assert ib.StopIteration() == ib.StopIteration()
 
 
+def test_fire_steps_schedule_matches_the_callers(ib):
+    """solve_ batches the steps between firings; the schedule is the callers' own decisions."""
+    from ibgb300.api import _fire_steps, _time_range
+    dt = 0.1
+    ts = _time_range(0.0, 1.0, dt)
+    assert _fire_steps(ib.at_indices(None, [2, 4, 4, 20]), ts, dt) == {2, 4}
+    assert _fire_steps(ib.at_indices(None, [4, 2]), ts, dt) == {4}
+    assert _fire_steps(ib.at_times(None, [0.0, 0.11, 0.12, 0.35, 5.0]), ts, dt) == {1, 2, 4}
+    assert _fire_steps(ib.each_timestep(None), ts, dt) == set(range(1, 12))
+
+
 def test_circle_and_bodies(ib):
     c = ib.circle((0.0, 0.0), 0.5, 0.02)
     assert c.npoints() == int(np.floor(np.pi * 0.5 / 0.02))

@@ -142,6 +142,7 @@ SIGNATURES = {
     "ib_ensemble_advance_n": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp]),
     "ib_ensemble_advance_n_kin": (C.c_int, [_vp, C.c_int32, _dp, _dp, _dp, _dp]),
     "ib_ensemble_info": (C.c_int, [_vp, _ip, _ip]),
+    "ib_ensemble_set_steps_per_launch": (C.c_int, [_vp, C.c_int32]),
     "ib_ensemble_last_error": (C.c_char_p, [_vp]),
 }
 

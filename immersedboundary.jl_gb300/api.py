@@ -740,7 +740,7 @@ class Ensemble:
     first two steps.  Members keep their own state; ``state`` objects are refreshed lazily like
     after ``advance_``."""
 
-    def __init__(self, solvers: Sequence[Solver]):
+    def __init__(self, solvers: Sequence[Solver], steps_per_launch: int = 1):
         self.solvers = list(solvers)
         self.lib = self.solvers[0].lib
         arr = (C.c_void_p * len(self.solvers))(*[s.handle for s in self.solvers])
@@ -749,6 +749,8 @@ class Ensemble:
         if st != _lib.IB_OK:
             raise _lib.IBError(st, (self.lib.ib_ensemble_last_error(None) or b"").decode())
         self.handle = h
+        if steps_per_launch != 1:
+            self.set_steps_per_launch(steps_per_launch)
 
     def _check(self, st):
         if st != _lib.IB_OK:
@@ -758,6 +760,12 @@ class Ensemble:
         n, k = C.c_int32(), C.c_int32()
         self._check(self.lib.ib_ensemble_info(self.handle, C.byref(n), C.byref(k)))
         return n.value, k.value
+
+    def set_steps_per_launch(self, k: int):
+        """Carry ``k`` consecutive steps of every member per graph launch (1..8): within a
+        launch a member goes on with its next step without waiting for the slowest member.
+        Results are bitwise those of one step per launch."""
+        self._check(self.lib.ib_ensemble_set_steps_per_launch(self.handle, int(k)))
 
     def advance_n(self, ts, uv=None, states: Sequence[State] | None = None) -> float:
         """Advance every member through the times ``ts``: [nsteps] (the same times for every

@@ -246,6 +246,16 @@ __global__ void k_val_sums(const float* __restrict__ yb, const float* __restrict
 }
 
 // minibatch rows idx[0..b): normalised features and targets
+__global__ void k_denorm(const float* __restrict__ yb, const float* __restrict__ yh, const float* __restrict__ mu_y,
+                         const float* __restrict__ sd_y, int b, int nf, double* __restrict__ q, double* __restrict__ t) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)b * nf;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nf);
+    t[i] = (double)yb[i] * sd_y[k] + mu_y[k];
+    q[i] = (double)yh[i] * sd_y[k] + mu_y[k];
+  }
+}
+
 __global__ void k_gather(const float* __restrict__ xs, const float* __restrict__ ys, const int* __restrict__ idx, int b,
                          int din, int nkin, int nf, const float* __restrict__ mu_x, const float* __restrict__ sd_x,
                          const float* __restrict__ mu_y, const float* __restrict__ sd_y, float* __restrict__ xb,
@@ -512,6 +522,7 @@ cudaError_t Mlp::train(int epochs, int batch, float lr, uint64_t seed, double* f
   // validation: blend = argmin over [0, 1] of |t - blend q|^2 on the held-out rows
   blend = 1.0;
   val_rel = -1.0;
+  val_rows.assign(order.begin() + ntr, order.end());
   if (nval > 0) {
     if ((e = cudaMemcpyAsync(idx, order.data() + ntr, sizeof(int) * nval, cudaMemcpyHostToDevice, stream)) !=
         cudaSuccess)
@@ -536,6 +547,28 @@ cudaError_t Mlp::train(int epochs, int batch, float lr, uint64_t seed, double* f
   if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
   trained = true;
   if (final_loss) *final_loss = last;
+  return cudaSuccess;
+}
+
+cudaError_t Mlp::heldout(double* q, double* t, int max_rows, int* rows) {
+  const int din = dims[0], nf = dims[nl];
+  const int nkin = din - 2 * nf;
+  const int n = std::min<int>(max_rows, (int)val_rows.size());
+  *rows = n;
+  if (n == 0) return cudaSuccess;
+  const int* first = val_rows.data() + val_rows.size() - n;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(idx, first, sizeof(int) * n, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+  for (int s0 = 0; s0 < n; s0 += kMaxBatch) {
+    const int b = std::min(kMaxBatch, n - s0);
+    k_gather<<<blocks_for((int64_t)b * (din + nf)), 256, 0, stream>>>(xs, ys, idx + s0, b, din, nkin, nf, mu_x, sd_x,
+                                                                       mu_y, sd_y, act[0], ybatch);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = forward(b)) != cudaSuccess) return e;
+    k_denorm<<<blocks_for((int64_t)b * nf), 256, 0, stream>>>(ybatch, act[nl], mu_y, sd_y, b, nf,
+                                                                q + (int64_t)s0 * nf, t + (int64_t)s0 * nf);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   return cudaSuccess;
 }
 

@@ -36,6 +36,7 @@ struct Mlp {
   bool trained = false;
   double blend = 1.0;    // weight of the network's correction (validated at training)
   double val_rel = -1;   // held-out squared error relative to plain extrapolation's (-1: none)
+  std::vector<int> val_rows;  // sample slots of the held-out rows of the last training, oldest first
   int adam_t = 0;
   cudaStream_t stream = nullptr;
   std::vector<void*> allocs;
@@ -54,6 +55,9 @@ struct Mlp {
   void record_commit();                         // the host mirror of count / next
   cudaError_t predict(const double* f1, const double* f2, double* fb);
   cudaError_t train(int epochs, int batch, float lr, uint64_t seed, double* final_loss);
+  // the network's corrections q and the targets t (F_n minus its extrapolation) of the most
+  // recent held-out rows, denormalised, row-major [rows][nf] in FP64; at most max_rows rows
+  cudaError_t heldout(double* q, double* t, int max_rows, int* rows);
   // loss and parameter gradients of the raw network on host rows (normalised inputs/targets)
   cudaError_t gradients(int b, const float* x_host, const float* y_host, float* grad_host, double* loss_host);
 };

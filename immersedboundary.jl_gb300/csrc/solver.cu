@@ -47,6 +47,9 @@ constexpr int kQ0Slots = 1024;  // pinned staging slots of per-step base flux
 
 }  // namespace
 
+// steps of every member one ensemble graph launch can carry (ib_ensemble_set_steps_per_launch)
+constexpr int kMaxStepsPerLaunch = 8;
+
 struct ib_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -118,8 +121,9 @@ struct ib_handle {
   cudaGraphExec_t mgexec[2] = {nullptr, nullptr};
   uint64_t mg_key = 0;
   cudaStream_t loop_stream = nullptr;             // capture stream of the CG loop body
-  double* h_mslot = nullptr;                      // pinned: base flux [2L] and kinematics [6 nbodies]
-  double* h_cgout = nullptr;                      // pinned: CG statistics of the last captured step
+  double* h_mslot = nullptr;                      // pinned: per step of a launch, base flux [2L] and
+                                                  // kinematics [6 nbodies] (kMaxStepsPerLaunch slots)
+  double* h_cgout = nullptr;                      // pinned: CG statistics [4] per step of the last launch
   double *d_cgctl = nullptr, *d_cgout = nullptr;
   bool collect = false;                           // record (features, F_n) every moving step
   std::vector<double> cg_res0;                    // initial relative residual of each CG solve
@@ -1111,6 +1115,72 @@ int cg_solve(ib_handle* h) {
   return IB_OK;
 }
 
+// The training's blend minimises the held-out force error in the 2-norm.  The CG start residual
+// is that error times the Schur operator B (condition number ~1e4-1e5), which amplifies a
+// correction that is rough from point to point, so a blend that barely lowers the 2-norm error
+// can raise ||B x0 - rhs||.  This re-fits the blend in the norm CG sees: over the most recent
+// held-out rows j (at most 256), blend = argmin over [0, 1] of sum_j |B (blend q_j - t_j)|^2,
+// with q_j the network's correction, t_j the extrapolation's error and B the operator of the
+// current configuration.  The B products run on the Schur scratch arrays; the two a later
+// product starts from (Pw, rings_w: the previous call's psi and rings) are saved and restored,
+// so the run's later CG iterates are those it would have had without this validation.
+template <typename S>
+int learn_validate_schur(ib_handle* h) {
+  learn::Mlp& m = *h->mlp;
+  const int nf = h->nf;
+  const Geometry& g = h->g;
+  cudaStream_t s = h->stream;
+  constexpr int kRows = 256;
+  const size_t npw = (size_t)g.nlev * g.nG, nrw = (size_t)g.nlev * g.nbc;  // 8-byte elements either way
+  double *q = nullptr, *t = nullptr, *bq = nullptr, *bt = nullptr, *dots = nullptr, *save = nullptr;
+  auto release = [&]() {
+    for (double* p : {q, t, bq, bt, dots, save})
+      if (p) cudaFree(p);
+  };
+  auto al = [&](double** p, size_t n) { return cudaMalloc(p, sizeof(double) * std::max<size_t>(n, 1)); };
+  cudaError_t e;
+  if ((e = al(&q, (size_t)kRows * nf)) != cudaSuccess || (e = al(&t, (size_t)kRows * nf)) != cudaSuccess ||
+      (e = al(&bq, nf)) != cudaSuccess || (e = al(&bt, nf)) != cudaSuccess || (e = al(&dots, 3 * kRows)) != cudaSuccess ||
+      (e = al(&save, npw + nrw)) != cudaSuccess) {
+    release();
+    return fail(h, IB_ERR_CUDA, "learned-start validation buffers", e);
+  }
+  int rows = 0;
+  e = m.heldout(q, t, kRows, &rows);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(save, h->Pw, sizeof(double) * npw, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(save + npw, h->rings_w, sizeof(double) * nrw, cudaMemcpyDeviceToDevice, s);
+  for (int j = 0; j < rows && e == cudaSuccess; ++j) {
+    if ((e = schur_apply<S>(h, q + (size_t)j * nf, bq)) != cudaSuccess) break;
+    if ((e = schur_apply<S>(h, t + (size_t)j * nf, bt)) != cudaSuccess) break;
+    if ((e = vec_dot(bq, bt, nf, dots + 3 * j, s)) != cudaSuccess) break;
+    if ((e = vec_dot(bq, bq, nf, dots + 3 * j + 1, s)) != cudaSuccess) break;
+    e = vec_dot(bt, bt, nf, dots + 3 * j + 2, s);
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->Pw, save, sizeof(double) * npw, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->rings_w, save + npw, sizeof(double) * nrw, cudaMemcpyDeviceToDevice, s);
+  std::vector<double> hd(3 * (size_t)std::max(rows, 1));
+  if (e == cudaSuccess && rows > 0)
+    e = cudaMemcpyAsync(hd.data(), dots, sizeof(double) * 3 * rows, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  release();
+  if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "learned-start validation", e);
+  if (rows == 0) return check_status(h);
+  double tq = 0.0, qq = 0.0, tt = 0.0;
+  for (int j = 0; j < rows; ++j) {
+    tq += hd[3 * j];
+    qq += hd[3 * j + 1];
+    tt += hd[3 * j + 2];
+  }
+  if (!std::isfinite(tq) || !std::isfinite(qq)) {
+    m.blend = 0.0;
+    m.val_rel = 1.0;
+  } else {
+    m.blend = qq > 0.0 ? std::min(1.0, std::max(0.0, tq / qq)) : 0.0;
+    m.val_rel = tt > 0.0 ? (tt - 2.0 * m.blend * tq + m.blend * m.blend * qq) / tt : 0.0;
+  }
+  return check_status(h);
+}
+
 // warm start (h->fb holds F_{n-1}, h->fb_prev F_{n-2}): the previous Fb (the reference's cg! on
 // qty.Fb), its linear extrapolation, zero, or the learned prediction (extrapolation until a
 // network is trained); keeps F_{n-1} in h->fb_last and the network's features
@@ -1215,19 +1285,22 @@ int moving_step(ib_handle* h, double t, double u, double v, const double* kin) {
 // preconditioner policy and the error reporting of the eager step.
 
 // Records the moving step for buffer parity p into the capture h->stream belongs to (its own,
-// or an ensemble's that it joined).
+// or an ensemble's that it joined); `k` is the step's index within a multi-step launch, which
+// selects its pinned staging slot and statistics record.
 template <typename S>
-cudaError_t enqueue_moving_captured(ib_handle* h, int p) {
+cudaError_t enqueue_moving_captured(ib_handle* h, int p, int k = 0) {
   const Geometry& g = h->g;
   cudaStream_t s = h->stream;
   const int L = g.nlev;
+  const double* slot = h->h_mslot + (size_t)k * (2 * L + 6 * h->nbodies);
+  double* cgout = h->h_cgout + 4 * k;
   const size_t fbytes = sizeof(double) * h->nf;
   const bool pc = h->precond == IB_PC_SCHUR_REF && h->binv_rm;
   double *x = h->fb, *r = h->cg_r, *pv = h->cg_p, *Ap = h->cg_Ap, *sc = h->cg_sc;
   double* z = pc ? h->cg_z : r;
   auto body = [&]() -> cudaError_t {
-    CE(cudaMemcpyAsync(h->d_q0, h->h_mslot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, s));
-    CE(cudaMemcpyAsync(h->d_kin, h->h_mslot + 2 * L, sizeof(double) * 6 * h->nbodies, cudaMemcpyHostToDevice, s));
+    CE(cudaMemcpyAsync(h->d_q0, slot, sizeof(double) * 2 * L, cudaMemcpyHostToDevice, s));
+    CE(cudaMemcpyAsync(h->d_kin, slot + 2 * L, sizeof(double) * 6 * h->nbodies, cudaMemcpyHostToDevice, s));
     CE(body_points(h->xb_body, h->d_kin, h->body_of, h->nb, h->xb, h->vb, s));
     CE(reg_update(g, h->xb, h->nb, h->body_idx, h->weight, h->status, s));
     CE(enqueue_trial<S>(h, p));
@@ -1286,7 +1359,7 @@ cudaError_t enqueue_moving_captured(ib_handle* h, int p) {
     CE(cudaMemcpyAsync(h->fb_prev, h->fb_last, fbytes, cudaMemcpyDeviceToDevice, s));
     CE(enqueue_stress(h));
     CE(enqueue_project<S>(h, p));
-    CE(cudaMemcpyAsync(h->h_cgout, h->d_cgout, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
+    CE(cudaMemcpyAsync(cgout, h->d_cgout, sizeof(double) * 4, cudaMemcpyDeviceToHost, s));
     return cudaSuccess;
   };
   cudaError_t e = body();
@@ -1900,11 +1973,12 @@ int ib_create(const ib_problem* p, ib_handle** out) {
       AL(h->xb_body, 2 * nb); AL(h->vb, 2 * nb); AL(h->d_kin, 6 * h->nbodies); AL(h->body_of, nb);
       AL(h->cg_r, h->nf); AL(h->cg_p, h->nf); AL(h->cg_Ap, h->nf); AL(h->cg_sc, 8); AL(h->fb_prev, h->nf);
       AL(h->fb_last, h->nf); AL(h->cg_z, h->nf); AL(h->d_cgctl, 4); AL(h->d_cgout, 4);
-      if ((e = cudaMallocHost(&h->h_mslot, sizeof(double) * (2 * L + 6 * h->nbodies))) != cudaSuccess) {
+      if ((e = cudaMallocHost(&h->h_mslot, sizeof(double) * kMaxStepsPerLaunch * (2 * L + 6 * h->nbodies))) !=
+          cudaSuccess) {
         h->h_mslot = nullptr;
         return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
       }
-      if ((e = cudaMallocHost(&h->h_cgout, sizeof(double) * 4)) != cudaSuccess) {
+      if ((e = cudaMallocHost(&h->h_cgout, sizeof(double) * 4 * kMaxStepsPerLaunch)) != cudaSuccess) {
         h->h_cgout = nullptr;
         return bail(fail(h, IB_ERR_CUDA, "pinned staging", e));
       }
@@ -2674,7 +2748,8 @@ int ib_learn_train(ib_handle* h, int32_t epochs, int32_t batch, double lr, uint6
   CK(dev_guard_.err);
   cudaError_t e = h->mlp->train(epochs, batch, (float)lr, seed, final_loss);
   if (e != cudaSuccess) return fail(h, IB_ERR_CUDA, "training", e);
-  return IB_OK;
+  if (h->mlp->val_rows.empty()) return IB_OK;
+  return h->precision == IB_PREC_MIXED ? learn_validate_schur<df64>(h) : learn_validate_schur<double>(h);
 }
 
 int ib_learn_validation(ib_handle* h, double* blend, double* rel_err) {
@@ -2798,8 +2873,10 @@ struct ib_ensemble {
   cudaStream_t stream = nullptr;
   cudaEvent_t start = nullptr;
   std::vector<cudaEvent_t> join;
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-  double* h_q0 = nullptr;            // pinned [2][slot_len]: base flux of every member and level
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};    // one step, per starting parity
+  cudaGraphExec_t gexec_k[2] = {nullptr, nullptr};  // `chunk` steps, per starting parity
+  int chunk = 1;                                    // steps per launch (ib_ensemble_set_steps_per_launch)
+  double* h_q0 = nullptr;  // pinned [2][kMaxStepsPerLaunch][slot_len]: base flux of every member and level
   std::vector<int64_t> q0_off;
   int64_t slot_len = 0;
   cudaEvent_t done[2] = {nullptr, nullptr};
@@ -2839,6 +2916,8 @@ void destroy_ensemble(ib_ensemble* e) {
   if (e->stream) cudaStreamSynchronize(e->stream);
   for (auto& g : e->gexec)
     if (g) cudaGraphExecDestroy(g);
+  for (auto& g : e->gexec_k)
+    if (g) cudaGraphExecDestroy(g);
   for (auto ev : e->join)
     if (ev) cudaEventDestroy(ev);
   for (auto ev : e->done)
@@ -2849,24 +2928,29 @@ void destroy_ensemble(ib_ensemble* e) {
   delete e;
 }
 
-// capture one ensemble step for buffer parity offset p (member i runs its parity base_i ^ p)
-int capture_ensemble(ib_ensemble* e, int p) {
+// capture `nsteps` ensemble steps for launches at ensemble parity p, reading staging slot set p;
+// member i runs its parities base_i ^ p, base_i ^ p ^ 1, ..., base_i being its parity at ensemble
+// parity 0 (its current parity is base_i ^ e->parity).  Each member's steps follow one another
+// on its own branch and the branches join only at the end, so within one launch a member does
+// not wait for the others.
+int capture_ensemble(ib_ensemble* e, int p, int nsteps = 1) {
   cudaGraph_t graph = nullptr;
   EK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t ce = cudaEventRecord(e->start, e->stream);
   for (size_t i = 0; i < e->m.size() && ce == cudaSuccess; ++i) {
     ib_handle* h = e->m[i];
     ce = cudaStreamWaitEvent(h->stream, e->start, 0);
-    if (h->motion == IB_MOTION_PRESCRIBED) {
-      // the member's own staging slot holds this step's base flux and kinematics
-      if (ce == cudaSuccess)
-        ce = h->precision == IB_PREC_MIXED ? enqueue_moving_captured<df64>(h, h->parity ^ p)
-                                           : enqueue_moving_captured<double>(h, h->parity ^ p);
-    } else {
-      if (ce == cudaSuccess)
-        ce = cudaMemcpyAsync(h->d_q0, e->h_q0 + p * e->slot_len + e->q0_off[i], sizeof(double) * 2 * h->g.nlev,
-                             cudaMemcpyHostToDevice, h->stream);
-      if (ce == cudaSuccess) ce = enqueue_step_mode(h, h->parity ^ p);
+    for (int k = 0; k < nsteps && ce == cudaSuccess; ++k) {
+      const int par = h->parity ^ e->parity ^ p ^ (k & 1);
+      if (h->motion == IB_MOTION_PRESCRIBED) {
+        // the member's own staging slot k holds this step's base flux and kinematics
+        ce = h->precision == IB_PREC_MIXED ? enqueue_moving_captured<df64>(h, par, k)
+                                           : enqueue_moving_captured<double>(h, par, k);
+      } else {
+        const double* slot = e->h_q0 + ((size_t)p * kMaxStepsPerLaunch + k) * e->slot_len + e->q0_off[i];
+        ce = cudaMemcpyAsync(h->d_q0, slot, sizeof(double) * 2 * h->g.nlev, cudaMemcpyHostToDevice, h->stream);
+        if (ce == cudaSuccess) ce = enqueue_step_mode(h, par);
+      }
     }
     if (ce == cudaSuccess) ce = cudaEventRecord(e->join[i], h->stream);
     if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->join[i], 0);
@@ -2886,9 +2970,14 @@ int capture_ensemble(ib_ensemble* e, int p) {
       cudaGraphNodeType ty;
       if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++k;
     }
-    e->kernels_per_step = k;
+    if (nsteps == 1) e->kernels_per_step = k;
   }
-  ce = cudaGraphInstantiate(&e->gexec[p], graph, 0);
+  cudaGraphExec_t& slot_exec = nsteps == 1 ? e->gexec[p] : e->gexec_k[p];
+  if (slot_exec) {
+    cudaGraphExecDestroy(slot_exec);
+    slot_exec = nullptr;
+  }
+  ce = cudaGraphInstantiate(&slot_exec, graph, 0);
   cudaGraphDestroy(graph);
   if (ce != cudaSuccess) return efail(e, IB_ERR_CUDA, "ensemble graph instantiate", ce);
   return IB_OK;
@@ -2964,7 +3053,7 @@ int ib_ensemble_create(ib_handle* const* members, int32_t n, ib_ensemble** out) 
       ev = nullptr;
       return bail(efail(e, IB_ERR_CUDA, "cudaEventCreate", ce));
     }
-  if ((ce = cudaMallocHost(&e->h_q0, sizeof(double) * 2 * (size_t)e->slot_len)) != cudaSuccess) {
+  if ((ce = cudaMallocHost(&e->h_q0, sizeof(double) * 2 * kMaxStepsPerLaunch * (size_t)e->slot_len)) != cudaSuccess) {
     e->h_q0 = nullptr;
     return bail(efail(e, IB_ERR_CUDA, "pinned staging", ce));
   }
@@ -3004,56 +3093,68 @@ int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, c
     EK(cudaEventCreate(&e1));
     EK(cudaEventRecord(e0, e->stream));
   }
-  for (int s = 0; s < nsteps; ++s) {
+  for (int s = 0; s < nsteps;) {
+    const int K = (e->chunk > 1 && nsteps - s >= e->chunk) ? e->chunk : 1;
     const int p = e->parity;
-    // the launch that read this slot two steps ago must be done before the slot is rewritten
+    // the launch that read slot set p last must be done before the set is rewritten
     if (e->launched[p]) EK(cudaEventSynchronize(e->done[p]));
-    double* slot = e->h_q0 + (size_t)p * e->slot_len;
-    const double* ks = kin ? kin + (size_t)s * kin_per_step : nullptr;
-    for (int i = 0; i < n; ++i) {
-      ib_handle* h = e->m[i];
-      const double u = uv[((size_t)s * n + i) * 2], v = uv[((size_t)s * n + i) * 2 + 1];
-      double* dst = h->motion == IB_MOTION_PRESCRIBED ? h->h_mslot : slot + e->q0_off[i];
-      for (int l = 0; l < h->g.nlev; ++l) {
-        const double hc = h->g.h * std::ldexp(1.0, l);  // base_flux!, fluid-ops.jl:414-415
-        dst[2 * l] = u * hc;
-        dst[2 * l + 1] = v * hc;
-      }
-      if (h->motion == IB_MOTION_PRESCRIBED) {
-        std::memcpy(h->h_mslot + 2 * h->g.nlev, ks, sizeof(double) * 6 * h->nbodies);
-        ks += 6 * h->nbodies;
-        // preconditioner re-assembly between launches, on the member's own stream
-        int rc = pc_maybe_assemble(h);
-        if (rc != IB_OK) return efail(e, rc, "member " + std::to_string(i) + ": " + h->err);
-        if (moving_graph_key(h) != e->keys[i])
-          return efail(e, IB_ERR_INVALID, "member " + std::to_string(i) + " changed its CG options inside the ensemble");
+    for (int k = 0; k < K; ++k) {
+      double* slot = e->h_q0 + ((size_t)p * kMaxStepsPerLaunch + k) * e->slot_len;
+      const double* ks = kin ? kin + (size_t)(s + k) * kin_per_step : nullptr;
+      for (int i = 0; i < n; ++i) {
+        ib_handle* h = e->m[i];
+        const double u = uv[((size_t)(s + k) * n + i) * 2], v = uv[((size_t)(s + k) * n + i) * 2 + 1];
+        const bool mv = h->motion == IB_MOTION_PRESCRIBED;
+        double* dst = mv ? h->h_mslot + (size_t)k * (2 * h->g.nlev + 6 * h->nbodies) : slot + e->q0_off[i];
+        for (int l = 0; l < h->g.nlev; ++l) {
+          const double hc = h->g.h * std::ldexp(1.0, l);  // base_flux!, fluid-ops.jl:414-415
+          dst[2 * l] = u * hc;
+          dst[2 * l + 1] = v * hc;
+        }
+        if (mv) {
+          std::memcpy(dst + 2 * h->g.nlev, ks, sizeof(double) * 6 * h->nbodies);
+          ks += 6 * h->nbodies;
+        }
       }
     }
-    EK(cudaGraphLaunch(e->gexec[p], e->stream));
+    for (int i = 0; i < n; ++i) {
+      ib_handle* h = e->m[i];
+      if (h->motion != IB_MOTION_PRESCRIBED) continue;
+      // preconditioner re-assembly between launches, on the member's own stream
+      int rc = pc_maybe_assemble(h);
+      if (rc != IB_OK) return efail(e, rc, "member " + std::to_string(i) + ": " + h->err);
+      if (moving_graph_key(h) != e->keys[i])
+        return efail(e, IB_ERR_INVALID, "member " + std::to_string(i) + " changed its CG options inside the ensemble");
+    }
+    EK(cudaGraphLaunch(K == 1 ? e->gexec[p] : e->gexec_k[p], e->stream));
     EK(cudaEventRecord(e->done[p], e->stream));
     e->launched[p] = true;
-    e->parity ^= 1;
+    e->parity ^= K & 1;
     if (e->any_moving) {
-      // moving members: the step's CG statistics came back through pinned memory
+      // moving members: the steps' CG statistics came back through pinned memory
       EK(cudaStreamSynchronize(e->stream));
       for (int i = 0; i < n; ++i) {
         ib_handle* h = e->m[i];
         if (h->motion != IB_MOTION_PRESCRIBED) continue;
-        const double* o = h->h_cgout;
-        h->cg_iters.push_back((int)o[0]);
-        h->cg_res.push_back(o[1]);
-        h->cg_res0.push_back(o[2]);
-        if (h->mlp && h->collect) h->mlp->record_commit();
-        pc_account(h, h->steps);
-        if (o[3] != 0.0) return efail(e, IB_ERR_CG_MAXITER, "member " + std::to_string(i) + ": Schur CG iteration cap");
+        for (int k = 0; k < K; ++k) {
+          const double* o = h->h_cgout + 4 * k;
+          h->cg_iters.push_back((int)o[0]);
+          h->cg_res.push_back(o[1]);
+          h->cg_res0.push_back(o[2]);
+          if (h->mlp && h->collect) h->mlp->record_commit();
+          pc_account(h, h->steps + k);
+          if (o[3] != 0.0)
+            return efail(e, IB_ERR_CG_MAXITER, "member " + std::to_string(i) + ": Schur CG iteration cap");
+        }
       }
     }
     for (int i = 0; i < n; ++i) {
       ib_handle* h = e->m[i];
-      h->parity ^= 1;
-      h->steps++;
-      h->t = t[(size_t)s * n + i];
+      h->parity ^= K & 1;
+      h->steps += K;
+      h->t = t[(size_t)(s + K - 1) * n + i];
     }
+    s += K;
   }
   if (device_ms) {
     EK(cudaEventRecord(e1, e->stream));
@@ -3068,6 +3169,31 @@ int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, c
   for (int i = 0; i < n; ++i) {
     int rc = check_status(e->m[i]);
     if (rc != IB_OK) return efail(e, rc, "member " + std::to_string(i) + ": " + e->m[i]->err);
+  }
+  return IB_OK;
+}
+
+int ib_ensemble_set_steps_per_launch(ib_ensemble* e, int32_t k) {
+  ib::Range nvtx_range("ib_ensemble_set_steps_per_launch");
+  if (!e) return IB_ERR_INVALID;
+  if (k < 1 || k > kMaxStepsPerLaunch)
+    return efail(e, IB_ERR_INVALID, "steps per launch must be 1.." + std::to_string(kMaxStepsPerLaunch));
+  DeviceGuard dev_guard_(e->device);
+  EK(dev_guard_.err);
+  EK(cudaStreamSynchronize(e->stream));
+  for (auto& g : e->gexec_k)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  e->chunk = k;
+  if (k == 1) return IB_OK;
+  for (int p = 0; p < 2; ++p) {
+    const int rc = capture_ensemble(e, p, k);
+    if (rc != IB_OK) {
+      e->chunk = 1;
+      return rc;
+    }
   }
   return IB_OK;
 }

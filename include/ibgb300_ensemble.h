@@ -39,6 +39,15 @@ int ib_ensemble_advance_n(ib_ensemble* e, int32_t nsteps, const double* t, const
 int ib_ensemble_advance_n_kin(ib_ensemble* e, int32_t nsteps, const double* t, const double* uv, const double* kin,
                               double* device_ms);
 
+/* steps of every member per graph launch (1..8, default 1).  With k > 1 each launch carries k
+ * consecutive steps of every member on the member's own branch, joined only at the end of the
+ * launch: a member that finishes a step early (a moving member whose CG converged in few
+ * iterations, a small grid) goes on with its next step instead of waiting for the slowest member.
+ * The results are those of single-step launches, bit for bit.  Moving members' preconditioners
+ * are re-assembled between launches only, and their CG statistics are read after each launch.
+ * ib_ensemble_advance_n runs whole launches of k steps and the remaining steps one per launch. */
+int ib_ensemble_set_steps_per_launch(ib_ensemble* e, int32_t k);
+
 /* kernel launches per ensemble step (graph kernel nodes over all members) */
 int ib_ensemble_info(ib_ensemble* e, int32_t* members, int32_t* kernels_per_step);
 

@@ -41,9 +41,11 @@ int ib_learn_sample_count(ib_handle* h, int32_t* count);
 int ib_learn_train(ib_handle* h, int32_t epochs, int32_t batch, double lr, uint64_t seed, double* final_loss);
 
 /* held-out check of the last training (the most recent tenth of the samples, not trained on):
- * `blend` in [0, 1] is the weight given to the network's correction (the least-squares optimum
- * on the held-out rows; 0 means plain extrapolation), `rel_err` the held-out squared error of
- * the blended start relative to plain extrapolation's (-1 when there were too few samples) */
+ * `blend` in [0, 1] is the weight given to the network's correction, the least-squares optimum
+ * on the held-out rows (at most the 256 most recent) in the norm the CG start residual is
+ * measured in, |B (blend q - t)| with B the Schur operator of the configuration at training
+ * (0 means plain extrapolation); `rel_err` the held-out squared error of the blended start in
+ * that norm relative to plain extrapolation's (-1 when there were too few samples) */
 int ib_learn_validation(ib_handle* h, double* blend, double* rel_err);
 
 /* layer widths (nlayers + 1 values: features, hidden..., forces) */

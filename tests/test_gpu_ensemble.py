@@ -1,5 +1,5 @@
 """Ensembles (include/ibgb300_ensemble.h): members of different grids and precisions advanced by
-one graph launch per step give exactly the steps they give alone."""
+one graph launch per step, or per k steps, give exactly the steps they give alone."""
 import numpy as np
 import pytest
 
@@ -27,7 +27,10 @@ def start(ib, wl, precision):
     return prob, st, s
 
 
-def test_ensemble_steps_equal_single_steps(ib):
+@pytest.mark.parametrize("per_launch", [1, 3, 4])
+def test_ensemble_steps_equal_single_steps(ib, per_launch):
+    """5 + 7 steps: with 3 or 4 steps per launch both the multi-step graphs (at either starting
+    parity) and the single-step graphs of the remainders run."""
     n = 12
     singles = []
     for wl, prec in members(ib):
@@ -37,7 +40,7 @@ def test_ensemble_steps_equal_single_steps(ib):
         singles.append((st.qty.gamma.copy(), s.force_history(n)))
         s.close()
     runs = [start(ib, wl, prec) for wl, prec in members(ib)]
-    ens = ib.Ensemble([r[2] for r in runs])
+    ens = ib.Ensemble([r[2] for r in runs], steps_per_launch=per_launch)
     nm, kernels = ens.info()
     assert nm == 4 and kernels > 4 * 40
     ts = np.arange(n) * 0.01
@@ -79,9 +82,11 @@ def start_moving(ib, wl, precision):
     return prob, st, s
 
 
-def test_ensemble_with_moving_members_equals_single_steps(ib):
+@pytest.mark.parametrize("per_launch", [1, 4])
+def test_ensemble_with_moving_members_equals_single_steps(ib, per_launch):
     """Static and moving members (their CG loops inside the ensemble graph) give exactly the
-    steps they give alone; moving members join after two steps of their own."""
+    steps they give alone; moving members join after two steps of their own.  With 4 steps per
+    launch each member's CG loops of the 4 steps run on its own branch."""
     n = 10
     cases = [("static", members(ib)[0]), ("static", members(ib)[1]),
              ("moving", (heaving(ib, 0.5), "fp64")), ("moving", (heaving(ib, 0.4), "mixed"))]
@@ -100,7 +105,7 @@ def test_ensemble_with_moving_members_equals_single_steps(ib):
         runs.append((kind, wl, st, s))
     dt = cases[2][1][0].dt
     assert all(r[1].dt == dt for r in runs if r[0] == "moving")
-    ens = ib.Ensemble([r[3] for r in runs])
+    ens = ib.Ensemble([r[3] for r in runs], steps_per_launch=per_launch)
     ts = np.arange(2, n) * dt
     ens.advance_n(ts, states=[r[2] for r in runs])
     ens.close()

@@ -5,11 +5,13 @@
 //   target   y = F_n - (2 F_{n-1} - F_{n-2})        (the correction to linear extrapolation)
 //   network  x~ = (x - mu_x) / sd_x -> tanh(W1 x~ + b1) -> ... -> W_L h + b_L = y~,
 //            y = y~ * sd_y + mu_y,  warm start F_n ~ 2 F_{n-1} - F_{n-2} + y
-// Weights are stored BF16 for the forward products, with FP32 master copies updated by Adam;
-// every product accumulates in FP32.  Reductions (bias gradients, loss, statistics) run in a
+// Weights are stored BF16 for the products, with FP32 master copies updated by Adam; the
+// products run on the tensor cores (tcgen05, FP32 activations as three BF16 parts, FP32
+// accumulation in tensor memory).  Reductions (bias gradients, loss, statistics) run in a
 // fixed order, so training is reproducible.
 #include "ib_common.cuh"
 #include "mlp.cuh"
+#include "tcgen05.cuh"
 
 #include <cuda_bf16.h>
 
@@ -24,7 +26,7 @@ namespace ib {
 namespace learn {
 namespace {
 
-constexpr int kTile = 64, kBK = 16;
+using namespace tc;
 
 template <typename T> __device__ __forceinline__ float ldf(const T* p, int64_t i);
 template <> __device__ __forceinline__ float ldf<float>(const float* p, int64_t i) { return p[i]; }
@@ -34,65 +36,167 @@ template <> __device__ __forceinline__ float ldf<__nv_bfloat16>(const __nv_bfloa
 
 enum Epi : int { kStore = 0, kBias = 1, kBiasTanh = 2 };
 
-// C[M x N] = op(A)[M x K] op(B)[K x N] (+ bias[n], tanh).  A is FP32, stored [M][K] (TA false)
-// or [K][M] (TA true); B is FP32 or BF16, stored [K][N] (TB false) or [N][K] (TB true).
-// 64 x 64 output tile per 256-thread block, 4 x 4 outputs per thread, K in steps of 16.
-template <bool TA, bool TB, typename TBt, int EPI>
-__global__ void __launch_bounds__(256)
-k_gemm(int M, int N, int K, const float* __restrict__ A, const TBt* __restrict__ B, float* __restrict__ C,
-       const float* __restrict__ bias) {
-  __shared__ float As[kBK][kTile + 4];
-  __shared__ float Bs[kBK][kTile + 4];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
-  float acc[4][4] = {};
-  for (int k0 = 0; k0 < K; k0 += kBK) {
-    for (int e = threadIdx.x; e < kBK * kTile; e += 256) {
-      const int kk = e / kTile, mm = e % kTile;
-      const int m = m0 + mm, k = k0 + kk;
-      float va = 0.f;
-      if (m < M && k < K) va = TA ? A[(int64_t)k * M + m] : A[(int64_t)m * K + k];
-      As[kk][mm] = va;
-      const int n = n0 + mm;
-      float vb = 0.f;
-      if (n < N && k < K) vb = TB ? ldf(B, (int64_t)n * K + k) : ldf(B, (int64_t)k * N + n);
-      Bs[kk][mm] = vb;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kBK; ++kk) {
-      float a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
+// The network's products on the tensor cores: C[M x N] = op(A)[M x K] op(B)[K x N] (+ bias[n],
+// tanh), with A FP32 stored [M][K] (TA false) or [K][M] (TA true) and B FP32 or BF16 stored
+// [K][N] (TB false) or [N][K] (TB true).
+//
+// FP32 operands are split into three BF16 parts x = x1 + x2 + x3 (each the BF16 rounding of the
+// remainder of the previous ones, 24 significant bits together); BF16 operands (the weights) are
+// one exact part.  The products x_i y_j with i + j <= 2 (0-based; the dropped ones are below
+// 2^-24 of the terms) accumulate in FP32 in tensor memory, so the result has FP32 accuracy: 3
+// tcgen05.mma per K step against BF16 weights, 6 between two FP32 operands.
+//
+// One CTA = 128 rows x 128 columns of C, K in chunks of 64 (one 128-byte swizzle row of BF16):
+// the 8 warps load the chunk (coalesced along whichever of the operand's axes is contiguous),
+// split it and store the parts in the K-major swizzled layout; one thread issues the MMAs (M 128,
+// N 128, K 16) and commits them to an mbarrier that frees the single stage.  The products are
+// small (rows = a minibatch, columns = layer widths), so the chunks are not pipelined.  Waits
+// are bounded: on expiry the CTA sets the status flag, drains its MMAs (bounded), frees its
+// tensor memory and returns.
+constexpr int kTM = 128, kTN = 128, kTK = 64, kTThreads = 256;
+constexpr int kPart = kTM * kTK * 2;  // bytes of one BF16 part of a 128 x 64 operand tile
+
+template <typename T>
+__device__ __forceinline__ void store_parts(unsigned char* base, int nparts, uint32_t off, float a, float b) {
+  if (nparts == 1) {
+    const uint32_t w = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+                       ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+    *reinterpret_cast<uint32_t*>(base + off) = w;
+    return;
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty * 4 + i;
-    if (m >= M) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int n = n0 + tx * 4 + j;
-      if (n >= N) continue;
-      float v = acc[i][j];
-      if (EPI != kStore) v += bias[n];
-      if (EPI == kBiasTanh) v = tanhf(v);
-      C[(int64_t)m * N + n] = v;
+  for (int q = 0; q < 3; ++q) {
+    const __nv_bfloat16 ah = __float2bfloat16_rn(a), bh = __float2bfloat16_rn(b);
+    *reinterpret_cast<uint32_t*>(base + q * kPart + off) =
+        (uint32_t)__bfloat16_as_ushort(ah) | ((uint32_t)__bfloat16_as_ushort(bh) << 16);
+    a -= __bfloat162float(ah);
+    b -= __bfloat162float(bh);
+  }
+}
+
+// the 128 x 64 tile (rows r0.., K k0..) of X(r, k) = X[r rs + k ks] into its swizzled parts
+template <typename T, bool KCONTIG>
+__device__ __forceinline__ void load_tile(const T* __restrict__ X, int64_t rs, int64_t ks, int r0, int R, int k0,
+                                          int K, unsigned char* parts, int nparts) {
+#pragma unroll 4
+  for (int t = 0; t < kTM * (kTK / 2) / kTThreads; ++t) {
+    const int i = t * kTThreads + (int)threadIdx.x;
+    const int r = KCONTIG ? (i >> 5) : (i & (kTM - 1));
+    const int kp = KCONTIG ? (i & 31) : (i >> 7);
+    const int gr = r0 + r, k = k0 + 2 * kp;
+    float a = 0.f, b = 0.f;
+    if (gr < R) {
+      if (k < K) a = ldf(X, (int64_t)gr * rs + (int64_t)k * ks);
+      if (k + 1 < K) b = ldf(X, (int64_t)gr * rs + (int64_t)(k + 1) * ks);
     }
+    store_parts<T>(parts, nparts, sw128_off(r, kp), a, b);
   }
 }
 
 template <bool TA, bool TB, typename TBt, int EPI>
-cudaError_t gemm(int M, int N, int K, const float* A, const TBt* B, float* C, const float* bias, cudaStream_t s) {
-  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-  k_gemm<TA, TB, TBt, EPI><<<grid, 256, 0, s>>>(M, N, K, A, B, C, bias);
+__global__ void __launch_bounds__(kTThreads, 1)
+k_tcgemm(int M, int N, int K, const float* __restrict__ A, const TBt* __restrict__ B, float* __restrict__ C,
+         const float* __restrict__ bias, int* __restrict__ status) {
+  constexpr int NPB = std::is_same<TBt, float>::value ? 3 : 1;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ uint64_t done;
+  __shared__ uint32_t tmem_slot;
+  unsigned char* sm = smem_raw + ((1024 - (smem_u32(smem_raw) & 1023)) & 1023);
+  unsigned char* pa = sm;                // 3 parts of the A tile
+  unsigned char* pb = sm + 3 * kPart;    // NPB parts of the B tile
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+  if (tid == 0) {
+    mbar_init(&done, 1);
+    fence_mbar_init();
+    fence_async_smem();
+  }
+  if (warp == 0) tmem_alloc(&tmem_slot, kTN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  constexpr uint32_t kIdesc = idesc_bf16_mn<kTM, kTN>();
+  int committed = 0, drained = 0;
+  bool bad = false;
+  const int nkc = (K + kTK - 1) / kTK;
+  for (int c = 0; c < nkc; ++c) {
+    // A(m, k) = A[m K + k] or A[k M + m];  B(n, k) = B[n K + k] or B[k N + n]
+    load_tile<float, !TA>(A, TA ? 1 : K, TA ? M : 1, m0, M, c * kTK, K, pa, 3);
+    load_tile<TBt, TB>(B, TB ? K : 1, TB ? 1 : N, n0, N, c * kTK, K, pb, NPB);
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int ks = 0; ks < kTK / 16; ++ks) {
+        const uint32_t o32 = ks * 32;  // 16 BF16 = 32 bytes along K inside the swizzle row
+        bool first = c == 0 && ks == 0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < NPB; ++j)
+            if (i + j <= 2) {
+              umma_bf16(tmem, sw128_desc(smem_u32(pa + i * kPart) + o32), sw128_desc(smem_u32(pb + j * kPart) + o32),
+                        kIdesc, first ? 0u : 1u);
+              first = false;
+            }
+      }
+      umma_commit(&done);
+      ++committed;
+      if (!mbar_wait(&done, (uint32_t)c & 1)) bad = true;
+      else drained = committed;
+    }
+    if (__syncthreads_or(bad)) break;
+  }
+  if (bad) {
+    if (tid == 0) {
+      atomicExch(status, 1);
+      for (int k = drained; k < committed; ++k) mbar_wait(&done, (uint32_t)k & 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kTN);
+    return;
+  }
+  tc_fence_after();
+  // epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (rows), columns of half w >> 2
+  const int q = warp & 3, half = warp >> 2;
+  const int m = m0 + 32 * q + lane;
+  const uint32_t tb = tmem + ((uint32_t)(32 * q) << 16);
+#pragma unroll 1
+  for (int cc = 0; cc < kTN / 2; cc += 16) {
+    const int col0 = half * (kTN / 2) + cc;
+    float v[16];
+    tmem_ld16(tb + (uint32_t)col0, v);
+    if (m >= M) continue;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const int n = n0 + col0 + i;
+      if (n >= N) continue;
+      float x = v[i];
+      if (EPI != kStore) x += bias[n];
+      if (EPI == kBiasTanh) x = tanhf(x);
+      C[(int64_t)m * N + n] = x;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTN);
+}
+
+constexpr int kTSmem = 6 * kPart + 1024;  // 3 + 3 operand parts + alignment slack
+
+template <bool TA, bool TB, typename TBt, int EPI>
+cudaError_t gemm_attr() {
+  return cudaFuncSetAttribute(k_tcgemm<TA, TB, TBt, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTSmem);
+}
+
+template <bool TA, bool TB, typename TBt, int EPI>
+cudaError_t gemm(int M, int N, int K, const float* A, const TBt* B, float* C, const float* bias, int* status,
+                 cudaStream_t s) {
+  dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM);
+  k_tcgemm<TA, TB, TBt, EPI><<<grid, kTThreads, kTSmem, s>>>(M, N, K, A, B, C, bias, status);
   return cudaGetLastError();
 }
 
@@ -299,9 +403,11 @@ int blocks_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 4096)
 // --------------------------------------------------------------------------------------------
 // Mlp
 // --------------------------------------------------------------------------------------------
-cudaError_t Mlp::init(int din_, int dout_, int hidden, int nhidden, int capacity, uint64_t seed, cudaStream_t s) {
+cudaError_t Mlp::init(int din_, int dout_, int hidden, int nhidden, int capacity, uint64_t seed, cudaStream_t s,
+                      int* status_flag) {
   release();
   stream = s;
+  status = status_flag;
   dims.clear();
   dims.push_back(din_);
   for (int i = 0; i < nhidden; ++i) dims.push_back(hidden);
@@ -335,6 +441,12 @@ cudaError_t Mlp::init(int din_, int dout_, int hidden, int nhidden, int capacity
     return cudaMemsetAsync(v, 0, std::max<size_t>(n, 16), stream);
   };
   cudaError_t e;
+  // shared-memory limits of the tensor-core products (set outside any stream capture)
+  if ((e = gemm_attr<false, true, __nv_bfloat16, kBiasTanh>()) != cudaSuccess ||
+      (e = gemm_attr<false, true, __nv_bfloat16, kBias>()) != cudaSuccess ||
+      (e = gemm_attr<true, false, float, kStore>()) != cudaSuccess ||
+      (e = gemm_attr<false, false, __nv_bfloat16, kStore>()) != cudaSuccess)
+    return e;
 #define A_(p, n) if ((e = A(&(p), (n))) != cudaSuccess) return e
   A_(master, sizeof(float) * nparam);
   A_(grad, sizeof(float) * nparam);
@@ -398,8 +510,9 @@ cudaError_t Mlp::forward(int b) {
     const int K = dims[l], N = dims[l + 1];
     const __nv_bfloat16* W = wbf + woff[l];
     const float* bias = master + boff[l];
-    cudaError_t e = (l + 1 < nl) ? gemm<false, true, __nv_bfloat16, kBiasTanh>(b, N, K, act[l], W, act[l + 1], bias, stream)
-                                 : gemm<false, true, __nv_bfloat16, kBias>(b, N, K, act[l], W, act[l + 1], bias, stream);
+    cudaError_t e = (l + 1 < nl)
+                        ? gemm<false, true, __nv_bfloat16, kBiasTanh>(b, N, K, act[l], W, act[l + 1], bias, status, stream)
+                        : gemm<false, true, __nv_bfloat16, kBias>(b, N, K, act[l], W, act[l + 1], bias, status, stream);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -419,14 +532,15 @@ cudaError_t Mlp::backward(int b) {
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     // dW = dZ^T X  [N x K] ;  db = column sums of dZ
-    if ((e = gemm<true, false, float, kStore>(N, K, b, dact[l + 1], act[l], grad + woff[l], nullptr, stream)) != cudaSuccess)
+    if ((e = gemm<true, false, float, kStore>(N, K, b, dact[l + 1], act[l], grad + woff[l], nullptr, status, stream)) !=
+        cudaSuccess)
       return e;
     k_colsum<<<(N + 127) / 128, 128, 0, stream>>>(dact[l + 1], grad + boff[l], b, N);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // dX = dZ W  [b x K]
     if (l > 0) {
-      if ((e = gemm<false, false, __nv_bfloat16, kStore>(b, K, N, dact[l + 1], wbf + woff[l], dact[l], nullptr, stream)) !=
-          cudaSuccess)
+      if ((e = gemm<false, false, __nv_bfloat16, kStore>(b, K, N, dact[l + 1], wbf + woff[l], dact[l], nullptr, status,
+                                                         stream)) != cudaSuccess)
         return e;
     }
   }

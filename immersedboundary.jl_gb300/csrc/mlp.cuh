@@ -39,10 +39,12 @@ struct Mlp {
   std::vector<int> val_rows;  // sample slots of the held-out rows of the last training, oldest first
   int adam_t = 0;
   cudaStream_t stream = nullptr;
+  int* status = nullptr;  // device flag set when a tensor-core product gave up waiting
   std::vector<void*> allocs;
 
   ~Mlp() { release(); }
-  cudaError_t init(int din, int dout, int hidden, int nhidden, int capacity, uint64_t seed, cudaStream_t s);
+  cudaError_t init(int din, int dout, int hidden, int nhidden, int capacity, uint64_t seed, cudaStream_t s,
+                   int* status_flag);
   void release();
   cudaError_t sync_bf16();
   cudaError_t forward(int b);

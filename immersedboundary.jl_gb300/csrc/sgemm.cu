@@ -28,6 +28,7 @@
 // status[3], waits (bounded) for its own bulk copies and MMAs in flight, frees its tensor memory
 // and returns.
 #include "ib_common.cuh"
+#include "tcgen05.cuh"
 
 #include <cuda_bf16.h>
 
@@ -37,12 +38,12 @@
 
 namespace ib {
 namespace {
+using namespace tc;
 
 constexpr int BM = 128;                 // lines per CTA (MMA M)
 constexpr int BK = 64;                  // K per chunk: one 128-byte swizzle row of BF16
 constexpr int kThreads = 256;
 constexpr int kStages = 2;
-constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 template <int BN> struct Tile {
   static constexpr int kA = BM * BK * 2;       // bytes of one BF16 part of the line tile
@@ -51,109 +52,10 @@ template <int BN> struct Tile {
   static constexpr int kSmem = kStages * kStage + 1024;  // + alignment slack
 };
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// false when the phase has not completed within kWaitCycles
-__device__ __noinline__ bool mbar_wait(uint64_t* b, uint32_t parity) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(b, parity))
-    if (clock64() - t0 > kWaitCycles) return false;
-  return true;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-
-// D[tmem] (+)= A[smem] B[smem]^T, BF16 operands, FP32 accumulator; accumulate = 0 overwrites
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-// the mbarrier completes one arrival when every tcgen05.mma this thread issued before is done
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-// 32 TMEM lanes x 16 consecutive 32-bit columns: thread t gets lane (base + t), columns col..col+15
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// Shared-memory matrix descriptor of a K-major operand tile in the 128-byte swizzle layout:
-// start address, 8-row groups 1024 bytes apart (stride byte offset), descriptor version 1.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;               // leading byte offset: unused for swizzled K-major tiles
-  d |= (uint64_t)(1024 >> 4) << 32;     // stride byte offset
-  d |= (uint64_t)1 << 46;               // version
-  d |= (uint64_t)2 << 61;               // 128-byte swizzle
-  return d;
-}
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N.
 template <int BN>
 __host__ __device__ constexpr uint32_t idesc_bf16() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-}
-
-// byte offset of the 4-byte unit holding K elements (2p, 2p+1) of row r in a swizzled tile
-__host__ __device__ __forceinline__ uint32_t sw128_off(int r, int p) {
-  return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((p >> 2) ^ (r & 7)) & 7) << 4) + ((p & 3) << 2));
-}
-
-__device__ __forceinline__ uint32_t split_pair(float a, float b, uint32_t& lo) {
-  const __nv_bfloat16 ah = __float2bfloat16_rn(a), bh = __float2bfloat16_rn(b);
-  const __nv_bfloat16 al = __float2bfloat16_rn(a - __bfloat162float(ah));
-  const __nv_bfloat16 bl = __float2bfloat16_rn(b - __bfloat162float(bh));
-  lo = (uint32_t)__bfloat16_as_ushort(al) | ((uint32_t)__bfloat16_as_ushort(bl) << 16);
-  return (uint32_t)__bfloat16_as_ushort(ah) | ((uint32_t)__bfloat16_as_ushort(bh) << 16);
+  return idesc_bf16_mn<BM, BN>();
 }
 
 template <int BN, int MODE>

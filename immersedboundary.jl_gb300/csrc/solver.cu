@@ -813,7 +813,7 @@ int check_status(ib_handle* h) {
   if (st[0]) return fail(h, IB_ERR_BODY_OUT_OF_GRID, "body point within 7 cells of the finest-grid edge");
   if (st[1]) return fail(h, IB_ERR_NONFINITE, "infinite flux");
   if (st[2]) return fail(h, IB_ERR_SINGULAR, "zero or non-finite pivot in the Schur matrix");
-  if (st[3]) return fail(h, IB_ERR_TIMEOUT, "a tensor-core transform gave up waiting for its pipeline");
+  if (st[3]) return fail(h, IB_ERR_TIMEOUT, "a tensor-core kernel gave up waiting for its pipeline");
   return IB_OK;
 }
 
@@ -2717,7 +2717,7 @@ int ib_learn_init(ib_handle* h, int32_t hidden, int32_t hidden_layers, int32_t c
   delete h->mlp;
   h->mlp = new learn::Mlp();
   const int din = 6 * h->nbodies + 2 * h->nf;
-  cudaError_t e = h->mlp->init(din, h->nf, hidden, hidden_layers, capacity, seed, h->stream);
+  cudaError_t e = h->mlp->init(din, h->nf, hidden, hidden_layers, capacity, seed, h->stream, h->status + 3);
   if (e != cudaSuccess) {
     delete h->mlp;
     h->mlp = nullptr;

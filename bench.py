@@ -21,6 +21,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -357,6 +358,106 @@ def run_dt_probe(ib, dt=0.001, nsteps=40):
     return {"dt": dt, "steps_run": len(gmax), "gamma_max": gmax,
             "growth_per_step_last5": [float(x) for x in (g[-5:] / g[-6:-1])] if g.size > 6 else None,
             "stopped_by": err}
+
+
+def _device_ms_per_step(ib, s, prob, dt, first, K, W=5):
+    """Device milliseconds per step of K captured-graph replays (CUDA events on the handle's
+    stream, ib_advance_n_timed) after W warm-up steps, from step index `first`."""
+    ts = (first + np.arange(W + K)) * dt
+    uv = np.array([prob.fluid.grid_flow(float(t)) for t in ts], dtype=np.float64).reshape(-1)
+    dp = C.POINTER(C.c_double)
+    tw, uw = np.ascontiguousarray(ts[:W]), np.ascontiguousarray(uv[:2 * W])
+    tk, uk = np.ascontiguousarray(ts[W:]), np.ascontiguousarray(uv[2 * W:])
+    s._check(s.lib.ib_advance_n(s.handle, W, tw.ctypes.data_as(dp), uw.ctypes.data_as(dp)))
+    ms = C.c_double()
+    s._check(s.lib.ib_advance_n_timed(s.handle, K, tk.ctypes.data_as(dp), uk.ctypes.data_as(dp), C.byref(ms)))
+    return ms.value / K
+
+
+def run_next_rows(ib, K=20):
+    """Measurements of the rows either side of the step on the 1024^2 x 4 two-body workload:
+    SchemeRKC against CNAB (FP64), a translating grid frame against the lab frame (mixed),
+    checkpoint write / read throughput, and solve_ with sparse (at_indices) callbacks, whose
+    steps in between run as graph-replay batches, against a per-step callback."""
+    wl = make_workload(ib, "two_body_large")
+    cells = wl.cells_per_step
+    out = {"workload": describe(wl)}
+
+    def start(prob, precision):
+        st = ib.initstate(prob)
+        st._gamma[:] = wl.initial_gamma()
+        s = ib.initsolver(prob, st, precision=precision)
+        s.vort2flux(st)
+        return st, s
+
+    disc = ib.MultiLevel(ib.UniformGrid(wl.h, wl.xlims, wl.ylims), wl.nlevels)
+    fs = wl.freestream
+    # SchemeRKC vs SchemeCNAB, FP64
+    rk = {}
+    for name, scheme in (("cnab", ib.SchemeCNAB(wl.dt)), ("rkc", ib.SchemeRKC(wl.dt))):
+        prob = ib.Problem(ib.StreamFcnFluid(disc, lambda t: fs, wl.Re), ib.BodyGroup(*wl.bodies), scheme)
+        st, s = start(prob, "fp64")
+        from ibgb300 import _lib as L
+        info = L.IbInfo()
+        s._check(s.lib.ib_get_info(s.handle, C.byref(info)))
+        ms = _device_ms_per_step(ib, s, prob, wl.dt, 0, K)
+        rk[name] = {"ms_per_step": ms, "cell_steps_per_s": cells / (ms / 1e3), "kernels_per_step": info.kernels_per_step}
+        if name == "rkc":
+            rk[name]["stages"] = info.rkc_stages
+        s.close()
+    out["scheme_rkc_fp64"] = rk
+    # translating grid (RelativeFrame of the lab frame) vs lab frame, mixed
+    mg = {}
+    frame = ib.RelativeFrame(ib.LabFrame(), r=lambda t: (-0.5 * t, 0.0), v=lambda t: (-0.5, 0.0),
+                             theta=lambda t: 0.0, omega=lambda t: 0.0)
+    for name, dom in (("lab", disc), ("translating", ib.FluidDomain(disc, frame))):
+        prob = ib.Problem(ib.StreamFcnFluid(dom, lambda t: fs, wl.Re), ib.BodyGroup(*wl.bodies), ib.SchemeCNAB(wl.dt))
+        st, s = start(prob, "mixed")
+        ms = _device_ms_per_step(ib, s, prob, wl.dt, 0, K)
+        mg[name] = {"ms_per_step": ms, "grid_flow_t0": list(prob.fluid.grid_flow(0.0))}
+        s.close()
+    out["moving_grid_mixed"] = mg
+    # checkpoint files
+    prob = wl.problem()
+    st, s = start(prob, "mixed")
+    for i in range(3):
+        ib.advance_(st, s, i * wl.dt)
+    path = os.path.join(tempfile.gettempdir(), f"ibgb300_bench_{os.getpid()}.ckpt")
+    try:
+        a = time.perf_counter()
+        s.save_checkpoint(path)
+        t_save = time.perf_counter() - a
+        nbytes = os.path.getsize(path)
+        a = time.perf_counter()
+        s.load_checkpoint(path, st)
+        t_load = time.perf_counter() - a
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+    out["checkpoint"] = {"bytes": nbytes, "save_s": t_save, "load_s": t_load,
+                         "save_gbs": nbytes / t_save / 1e9, "load_gbs": nbytes / t_load / 1e9,
+                         "note": "host file in the system temp directory; device state <-> host copies included"}
+    s.close()
+    # solve_ with callbacks: per-step vs sparse (steps between firings batched)
+    cb = {}
+    n = 201
+    for name, calls in (("each_timestep", lambda: (ib.each_timestep(lambda st_: st_.qty.stress[0].CD),)),
+                        ("at_indices_every_50", lambda: (ib.at_indices(lambda st_: st_.qty.stress[0].CD,
+                                                                        list(range(1, n + 1, 50))),)),
+                        ("none", lambda: ())):
+        prob = wl.problem()
+        st, s = start(prob, "mixed")
+        ib.solve_(st, prob, (0.0, 9 * wl.dt), save=calls(), solver=s)  # warm-up
+        s.lib.ib_synchronize(s.handle)
+        a = time.perf_counter()
+        res = ib.solve_(st, prob, (10 * wl.dt, (10 + n - 1) * wl.dt), save=calls(), solver=s)
+        s.lib.ib_synchronize(s.handle)
+        sec = (time.perf_counter() - a) / n
+        cb[name] = {"ms_per_step": sec * 1e3, "cell_steps_per_s": cells / sec,
+                    "samples": len(res[0]) if res else 0}
+        s.close()
+    out["solve_callbacks_mixed"] = cb
+    return out
 
 
 def run_precision_table(ib, wl, checkpoints=(100, 1000, 2000)):
@@ -785,6 +886,9 @@ def main():
     ap.add_argument("--learned-protocol", action="store_true",
                     help="print the learned warm start's moving-plate protocol (train on steps 0-2000 at f 0.2, "
                          "evaluate on 2000-4000 and on f 0.15 / 0.25) and a dt 0.001 stability probe, and exit")
+    ap.add_argument("--next-rows", action="store_true",
+                    help="print measurements of SchemeRKC, a translating grid, checkpoint files and batched "
+                         "callbacks on the 1024^2 x 4 two-body workload, and exit")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket only the timed steps with cudaProfilerStart/Stop and skip the extras")
     args = ap.parse_args()
@@ -797,6 +901,13 @@ def main():
         ib.load_library()
         print(json.dumps({"learned_protocol": run_learned_protocol(ib),
                           "dt_probe": [run_dt_probe(ib, 0.001), run_dt_probe(ib, 0.0005)]}), flush=True)
+        return
+    if args.next_rows:
+        import __graft_entry__ as ge
+        ib = ge.package()
+        ge.build()
+        ib.load_library()
+        print(json.dumps({"next_rows": run_next_rows(ib)}), flush=True)
         return
     if args.precision_table:
         import __graft_entry__ as ge

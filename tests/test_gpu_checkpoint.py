@@ -102,3 +102,28 @@ def test_checkpoint_of_another_grid_is_refused(ib, tmp_path):
         s2.load_checkpoint(path, st2)
     s.close()
     s2.close()
+
+
+def test_mixed_restart_stays_within_the_mixed_bars(ib, tmp_path):
+    """A mixed-precision handle restarts from its checkpoint (float-float state stored as FP64,
+    the refinement predictors restart from zero) within the mixed bars of the uninterrupted run:
+    Gamma 1e-8 (relative L2), C_D / C_L 1e-6."""
+    wl = ib.workloads.scaled(ib.workloads.two_body_large(), 128, 128, nlevels=3)
+    prob, st, s = _start(ib, wl, precision="mixed")
+    for i in range(6):
+        ib.advance_(st, s, i * wl.dt)
+    path = tmp_path / "mixed.ckpt"
+    s.save_checkpoint(path)
+    for i in range(6, 12):
+        ib.advance_(st, s, i * wl.dt)
+    want_g = st.qty.gamma.copy()
+    want_c = [(b.CD, b.CL) for b in st.qty.stress]
+    prob2, st2, s2 = _start(ib, wl, precision="mixed")
+    s2.load_checkpoint(path, st2)
+    for i in range(6, 12):
+        ib.advance_(st2, s2, i * wl.dt)
+    assert rel(st2.qty.gamma, want_g) < 1e-8
+    for (cd, cl), b in zip(want_c, st2.qty.stress):
+        assert abs(b.CD - cd) / max(1.0, abs(cd)) < 1e-6 and abs(b.CL - cl) / max(1.0, abs(cl)) < 1e-6
+    s.close()
+    s2.close()

@@ -19,6 +19,9 @@
 // (x: 128 per thread, y: 85).  By measurement on GB300 (mixed step, device time): 1.355 ms per
 // 1024^2 x 4 step and 0.541 ms per 512^2 x 4 step with (4, 6), against 1.405 / 0.587 uncapped
 // (the residual x pass then used 168 registers, 3 blocks per SM) and 1.477 / 0.565 with x at 5.
+// The FP32 inverse x pass alone at 6 or 8 blocks (80 / 64 registers, no or 4-8 byte spills):
+// 1.201 / 1.205 ms per 1024^2 x 4 step and 4.72 / 4.86 ms per 2048^2 x 5 step, against 1.197 /
+// 4.70 at 4: the passes are bound by instruction issue, not by resident warps.
 #ifndef IB_WDST_XMINB
 #define IB_WDST_XMINB 4
 #endif

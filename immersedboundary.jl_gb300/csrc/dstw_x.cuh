@@ -273,7 +273,9 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         constexpr bool kF = EPI == kEpiSubAddBase || EPI == kEpiAddTo;
         const df64* sf = kF ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         df64* s2 = (EPI == kEpiAddTo && a.sub2) ? static_cast<df64*>(a.sub2) + off : nullptr;
-        constexpr int R = 8;
+        // sixteen elements per lane per round (1.167 vs 1.172 ms per 1024^2 x 4 mixed step with
+        // eight; 32 spills)
+        constexpr int R = 16;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
           df64 f[R];

@@ -16,6 +16,7 @@ namespace ib {
 namespace {
 
 using wdst::kLB;
+using wdst::kLBX;
 using wdst::kLines;
 using wdst::Shape;
 using wdst::line_dst;
@@ -152,12 +153,13 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           }
         }
       } else if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
-        for (int I0 = lane; I0 < ncol; I0 += kLB * NL) {
-          T v[kLB];
+        constexpr int LB = (sizeof(T) == 4 && NL == 32) ? kLBX : kLB;  // otherwise more would spill
+        for (int I0 = lane; I0 < ncol; I0 += LB * NL) {
+          T v[LB];
 #pragma unroll
-          for (int u = 0; u < kLB; ++u) v[u] = (I0 + NL * u < ncol) ? (T)src[I0 + NL * u] : T(0);
+          for (int u = 0; u < LB; ++u) v[u] = (I0 + NL * u < ncol) ? (T)src[I0 + NL * u] : T(0);
 #pragma unroll
-          for (int u = 0; u < kLB; ++u)
+          for (int u = 0; u < LB; ++u)
             if (I0 + NL * u < ncol) U[I0 + NL * u + 1] = v[u];
         }
       } else {
@@ -236,15 +238,16 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const T* src = in + (int64_t)b * a.stride + J;
         T* drow = sm + ww * Sh::kStride + 1;
         constexpr int step = NL;
-        for (int I0 = threadIdx.x / kLines; I0 < ncol; I0 += kLB * step) {
-          T v[kLB];
+        constexpr int LB = (sizeof(T) == 4 && NL == 32) ? kLBX : kLB;  // otherwise more would spill
+        for (int I0 = threadIdx.x / kLines; I0 < ncol; I0 += LB * step) {
+          T v[LB];
 #pragma unroll
-          for (int u = 0; u < kLB; ++u) {
+          for (int u = 0; u < LB; ++u) {
             const int I = I0 + u * step;
             v[u] = I < ncol ? src[(int64_t)I * nrow] : T(0);
           }
 #pragma unroll
-          for (int u = 0; u < kLB; ++u) {
+          for (int u = 0; u < LB; ++u) {
             const int I = I0 + u * step;
             if (I < ncol) drow[I] = v[u];
           }
@@ -273,9 +276,9 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         constexpr bool kF = EPI == kEpiSubAddBase || EPI == kEpiAddTo;
         const df64* sf = kF ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         df64* s2 = (EPI == kEpiAddTo && a.sub2) ? static_cast<df64*>(a.sub2) + off : nullptr;
-        // sixteen elements per lane per round (1.167 vs 1.172 ms per 1024^2 x 4 mixed step with
-        // eight; 32 spills)
-        constexpr int R = 16;
+        // sixteen elements per lane per round on one-warp lines (1.167 vs 1.172 ms per
+        // 1024^2 x 4 mixed step with eight; 32 spills), eight on two-warp lines (64 registers)
+        constexpr int R = NL == 32 ? 16 : 8;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
           df64 f[R];

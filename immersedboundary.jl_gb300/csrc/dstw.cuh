@@ -38,16 +38,16 @@ constexpr int kLines = IB_WDST_LINES;  // lines per block
 #define IB_WDST_COMBOS(X) \
   X(32, 1) X(32, 2) X(32, 3) X(32, 4) X(32, 6) X(32, 8) X(32, 12) X(32, 16) X(32, 24) X(32, 32) \
   X(64, 2) X(64, 4) X(64, 8) X(64, 16)
-// loads in flight per lane in the line copies of the y passes and the ring-transfer kernels
-// (compiled for 6-8 blocks per SM: more would spill)
+// loads in flight per lane in the line copies (ring-transfer kernels, FP64 lines, two-warp lines:
+// more would spill)
 constexpr int kLB = 8;
-// the same for the x passes (128 registers; the transposed copy is a 1024-value line in one
-// round trip per lane).  Measured on GB300 (device time per mixed step): 1.180 / 4.62 ms at
-// 1024^2 x 4 / 2048^2 x 5 against 1.202 / 4.74 with 8 (16: 1.181 / 4.69).
-#ifndef IB_WDST_LBX
-#define IB_WDST_LBX 32
-#endif
-constexpr int kLBX = IB_WDST_LBX;
+// FP32 one-warp lines of n = 64 P values: the whole line in one round trip per lane, 2 P loads
+// (at most 32).  Measured on GB300 (device time per mixed step): 1.167-1.180 / 4.56-4.62 ms at
+// 1024^2 x 4 / 2048^2 x 5 against 1.202 / 4.74 with 8 loads per round.
+template <typename T, int P, int NL>
+__host__ __device__ constexpr int line_lb() {
+  return (sizeof(T) == 4 && NL == 32) ? (2 * P < 32 ? 2 * P : 32) : kLB;
+}
 
 // cos(2 pi t / 96) for t = 0..24 (a quarter period); the rest by symmetry.  96 = lcm of the
 // in-lane transform sizes 2^k and 3 2^k (k <= 5).

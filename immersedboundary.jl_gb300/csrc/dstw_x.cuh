@@ -15,8 +15,7 @@
 namespace ib {
 namespace {
 
-using wdst::kLB;
-using wdst::kLBX;
+using wdst::line_lb;
 using wdst::kLines;
 using wdst::Shape;
 using wdst::line_dst;
@@ -153,7 +152,7 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           }
         }
       } else if (PRO == kProLoad && !kBC && std::is_same<Tin, T>::value) {
-        constexpr int LB = (sizeof(T) == 4 && NL == 32) ? kLBX : kLB;  // otherwise more would spill
+        constexpr int LB = line_lb<T, P, NL>();
         for (int I0 = lane; I0 < ncol; I0 += LB * NL) {
           T v[LB];
 #pragma unroll
@@ -238,7 +237,7 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         const T* src = in + (int64_t)b * a.stride + J;
         T* drow = sm + ww * Sh::kStride + 1;
         constexpr int step = NL;
-        constexpr int LB = (sizeof(T) == 4 && NL == 32) ? kLBX : kLB;  // otherwise more would spill
+        constexpr int LB = line_lb<T, P, NL>();
         for (int I0 = threadIdx.x / kLines; I0 < ncol; I0 += LB * step) {
           T v[LB];
 #pragma unroll
@@ -276,9 +275,9 @@ k_wxi(Geometry g, DstAxis<T> ax, XArgs a) {
         constexpr bool kF = EPI == kEpiSubAddBase || EPI == kEpiAddTo;
         const df64* sf = kF ? static_cast<const df64*>(a.sub_from) + off : nullptr;
         df64* s2 = (EPI == kEpiAddTo && a.sub2) ? static_cast<df64*>(a.sub2) + off : nullptr;
-        // sixteen elements per lane per round on one-warp lines (1.167 vs 1.172 ms per
+        // up to sixteen elements per lane per round on one-warp lines (1.167 vs 1.172 ms per
         // 1024^2 x 4 mixed step with eight; 32 spills), eight on two-warp lines (64 registers)
-        constexpr int R = NL == 32 ? 16 : 8;
+        constexpr int R = NL == 32 ? (2 * P < 16 ? 2 * P : 16) : 8;
         for (int I0 = lane; I0 < ncol; I0 += NL * R) {
           float b0[R], b1[R];
           df64 f[R];

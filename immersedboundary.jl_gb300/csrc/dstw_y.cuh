@@ -10,7 +10,7 @@
 namespace ib {
 namespace {
 
-using wdst::kLB;
+using wdst::line_lb;
 using wdst::kLines;
 using wdst::Shape;
 using wdst::line_dst;
@@ -27,28 +27,30 @@ k_wy(Geometry g, DstAxis<T> ax, YPassArgs<T> a) {
   T* D = U + Sh::kU;
   const int ncol = g.nx - 1, nrow = g.ny - 1;
   const int total = a.batch * ncol;
+  // the whole line in one or two round trips per lane (fewer registers at 8 blocks per SM)
+  constexpr int LB = MINB >= 8 && line_lb<T, P, NL>() > 16 ? 16 : line_lb<T, P, NL>();
   for (int col = blockIdx.x * kLines + w; col < total; col += gridDim.x * kLines) {
     const int b = col / ncol, I = col - b * ncol;
     const int64_t off = (int64_t)b * a.stride + (int64_t)I * nrow;
     const T* src = a.in1 + off;
-    for (int J0 = lane; J0 < nrow; J0 += kLB * NL) {
-      T v[kLB];
+    for (int J0 = lane; J0 < nrow; J0 += LB * NL) {
+      T v[LB];
 #pragma unroll
-      for (int u = 0; u < kLB; ++u) v[u] = (J0 + NL * u < nrow) ? src[J0 + NL * u] : T(0);
+      for (int u = 0; u < LB; ++u) v[u] = (J0 + NL * u < nrow) ? src[J0 + NL * u] : T(0);
 #pragma unroll
-      for (int u = 0; u < kLB; ++u)
+      for (int u = 0; u < LB; ++u)
         if (J0 + NL * u < nrow) U[J0 + NL * u + 1] = v[u];
     }
     line_sync<NL>(w + 1);
     line_dst<T, P, NL>(U, D, ax, lane, w + 1);
     if (OP == SpecOp::kScale) {
       const T* m = a.m1 + (int64_t)b * a.mstride + (int64_t)I * nrow;
-      for (int J0 = lane; J0 < nrow; J0 += kLB * NL) {
-        T v[kLB];
+      for (int J0 = lane; J0 < nrow; J0 += LB * NL) {
+        T v[LB];
 #pragma unroll
-        for (int u = 0; u < kLB; ++u) v[u] = (J0 + NL * u < nrow) ? __ldg(&m[J0 + NL * u]) : T(0);
+        for (int u = 0; u < LB; ++u) v[u] = (J0 + NL * u < nrow) ? __ldg(&m[J0 + NL * u]) : T(0);
 #pragma unroll
-        for (int u = 0; u < kLB; ++u)
+        for (int u = 0; u < LB; ++u)
           if (J0 + NL * u < nrow) U[J0 + NL * u + 1] *= v[u];
       }
       line_sync<NL>(w + 1);

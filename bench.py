@@ -56,6 +56,17 @@ def measured_traffic(workload: str, precision: str, form: str, cls: str):
     return None
 
 
+def measured_issue(workload: str, precision: str, form: str, cls: str):
+    """(warp instructions per launch, launches captured, source) from the committed capture, or None."""
+    if not TRAFFIC_PROFILE.exists():
+        return None
+    for line in TRAFFIC_PROFILE.read_text().splitlines():
+        f = line.strip().strip("`").split()
+        if len(f) == 7 and f[0] == "issue" and f[1:5] == [workload, precision, form, cls]:
+            return float(f[5]), int(f[6]), f"{TRAFFIC_PROFILE.relative_to(ROOT)} (ncu smsp__inst_executed.sum, one step, {f[6]} launches)"
+    return None
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -797,6 +808,17 @@ def run_ours(args, rank, world, local):
                     "peak_source": "measured FMA-chain probe on this GPU"},
         "passes": {k: {"total_ms": prof[k][0], "launches": prof[k][1]} for k in prof},
     }
+    # the same launches against the instruction-issue rate: warp instructions per launch (ncu
+    # count of these kernels) over 4 schedulers x SMs x SM clock x the event-timed launch
+    iss = measured_issue(args.workload, prec, f"{form}/{v2f}", dom)
+    if iss and info.sm_count > 0:
+        clk = (out.get("clocks") or {}).get("sm_mhz") or (out.get("clocks") or {}).get("sm_max_mhz") or 0.0
+        if clk:
+            issue_peak = 4.0 * info.sm_count * clk * 1e6
+            out["roofline"]["issue"] = {
+                "warp_instructions_per_launch": iss[0], "achieved_per_s": iss[0] / per_launch_s,
+                "peak_per_s": issue_peak, "frac": iss[0] / per_launch_s / issue_peak,
+                "source": iss[2], "note": "one warp instruction per scheduler per cycle; 4 schedulers per SM"}
     # the plain FP64 GPU path on the same workload, and the mixed path's C_L/C_D error against it
     if prec != "fp64" and not args.no_fp64_arm:
         ref = run_arm(ib, lib, L, wl, "fp64", K, W, local, dist)

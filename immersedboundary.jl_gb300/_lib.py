@@ -52,7 +52,8 @@ class IbInfo(C.Structure):
     _fields_ = [("kernels_per_step", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
                 ("nlevels", C.c_int32), ("nbodies", C.c_int32), ("npoints", C.c_int32),
                 ("device_bytes", C.c_int64), ("setup_ms", C.c_double), ("vort2flux_order", C.c_int32),
-                ("transform_form", C.c_int32), ("scheme", C.c_int32), ("rkc_stages", C.c_int32)]
+                ("transform_form", C.c_int32), ("scheme", C.c_int32), ("rkc_stages", C.c_int32),
+                ("sm_count", C.c_int32)]
 
 
 class IbProblem(C.Structure):

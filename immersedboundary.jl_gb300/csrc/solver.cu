@@ -2418,6 +2418,9 @@ int ib_get_info(ib_handle* h, ib_info* info) {
   info->transform_form = h->gdst ? IB_FORM_TENSOR : (h->wdst ? IB_FORM_WARP : IB_FORM_STOCKHAM);
   info->scheme = h->scheme;
   info->rkc_stages = h->rkc_s;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) sms = 0;
+  info->sm_count = sms;
   return IB_OK;
 }
 

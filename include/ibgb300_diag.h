@@ -24,6 +24,7 @@ typedef struct ib_info {
   int32_t transform_form;    /* the sine-transform passes in effect: IB_FORM_* */
   int32_t scheme;            /* IB_SCHEME_* */
   int32_t rkc_stages;        /* stages of the Runge-Kutta-Chebyshev scheme (0 for CNAB) */
+  int32_t sm_count;          /* streaming multiprocessors of the handle's device */
 } ib_info;
 
 #define IB_FORM_STOCKHAM 0   /* shared-memory Stockham FFT passes, 64 threads per line */

@@ -64,9 +64,8 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
         const df64* ds = (kD && J > 0) ? xd - ncol : nullptr;
         const df64* dn = (kD && J < nrow - 1) ? xd + ncol : nullptr;
         // ring terms of this row: the whole row at the bottom / top edge, one element at the
-        // left / right edge; loaded with the iterate for a float-float iterate, at their use
-        // otherwise (fewer live registers: 128 vs 156 at P = 32)
-        constexpr bool kPre = kBC && kD;
+        // left / right edge, loaded at their use (loading them with a float-float iterate
+        // spilled 200 bytes at P = 16 and took 1.155 instead of 1.139 ms per 1024^2 x 4 step)
         const A* bcrow = (kBC && J == 0) ? bc + g.B + 1 : ((kBC && J == nrow - 1) ? bc + g.T + 1 : nullptr);
         // eight elements per lane per round, every load of a round issued before any use
         constexpr int R = 8;
@@ -74,7 +73,6 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
           float c0[R], w0[R], e0[R], s0[R], n0[R];
           float c1[kD ? R : 1], w1[kD ? R : 1], e1[kD ? R : 1], s1[kD ? R : 1], n1[kD ? R : 1];
           df64 v[R];
-          df64 br[kPre ? R : 1], bs[kPre ? R : 1];
 #pragma unroll
           for (int u = 0; u < R; ++u) {
             const int I = I0 + NL * u;
@@ -93,10 +91,6 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
               n0[u] = (ok && xn) ? xn[I] : 0.0f;
             }
             v[u] = ok ? src[I] : df64(0.0f);
-            if constexpr (kPre) {
-              br[u] = (ok && bcrow) ? bcrow[I] : df64(0.0f);
-              bs[u] = (ok && I == 0) ? bc[g.L + 1 + J] : ((ok && I == ncol - 1) ? bc[g.R + 1 + J] : df64(0.0f));
-            }
           }
           df64 lap[R], xv[R];
 #pragma unroll
@@ -138,14 +132,9 @@ k_wxf(Geometry g, DstAxis<T> ax, XArgs a) {
             df64 vv = v[u];
             if constexpr (kBC) {
               auto addbc = [&](df64 q) { vv = add_sloppy(vv, fac1 ? q : fac * q); };
-              if constexpr (kPre) {
-                if (bcrow) addbc(br[u]);
-                if (I == 0 || I == ncol - 1) addbc(bs[u]);
-              } else {
-                if (bcrow) addbc(bcrow[I]);
-                if (I == 0) addbc(bc[g.L + 1 + J]);
-                if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
-              }
+              if (bcrow) addbc(bcrow[I]);
+              if (I == 0) addbc(bc[g.L + 1 + J]);
+              if (I == ncol - 1) addbc(bc[g.R + 1 + J]);
             }
             U[I + 1] = (T)((vv.hi - mx.hi) + (vv.lo - mx.lo));
             if (rout) rout[I] = add_sloppy(vv, -mx);

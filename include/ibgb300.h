@@ -37,7 +37,7 @@ extern "C" {
 #define IB_ERR_BODY_OUT_OF_GRID 4   /* body point within 7 cells of the finest-grid edge */
 #define IB_ERR_SINGULAR 5           /* zero / non-finite pivot while inverting the Schur matrix */
 #define IB_ERR_CG_MAXITER 6         /* Schur CG hit its iteration cap */
-#define IB_ERR_UNSUPPORTED 7        /* feature not available in this build */
+#define IB_ERR_UNSUPPORTED 7        /* feature not supported for this handle or configuration */
 #define IB_ERR_TIMEOUT 8            /* a device-side pipeline wait ran out (the kernel gave up and
                                        returned; the context stays usable) */
 

@@ -80,7 +80,7 @@ def test_learned_warm_start_converges_and_does_not_regress_on_held_out_steps(ib)
     it_e, res_e, r0_e, _, _ = run(ib, wl, "extrapolate", n_train, n_eval, kw)
     it_l, res_l, r0_l, loss, samples = run(ib, wl, "learned", n_train, n_eval, kw)
     assert samples == n_train + n_eval - 2  # recording continues while the network is used
-    # plain CG judges both: the same tolerance is reached on every step
+    # CG decides both: the same tolerance is reached on every step
     assert np.all(res_e <= 1e-10) and np.all(res_l <= 1e-10)
     print(f"loss {loss[0]:.3e} blend {loss[1]:.3f} held-out rel err {loss[2]:.3e}  "
           f"r0 extrapolated {np.mean(r0_e):.3e}  learned {np.mean(r0_l):.3e}  "

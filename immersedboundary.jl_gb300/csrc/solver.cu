@@ -1123,7 +1123,9 @@ int cg_solve(ib_handle* h) {
 // with q_j the network's correction, t_j the extrapolation's error and B the operator of the
 // current configuration.  The B products run on the Schur scratch arrays; the two a later
 // product starts from (Pw, rings_w: the previous call's psi and rings) are saved and restored,
-// so the run's later CG iterates are those it would have had without this validation.
+// so the run's later CG iterates are those it would have had without this validation, and so
+// are the status flags (a non-finite network correction would otherwise leave the handle's
+// "infinite flux" flag set; its rows make the blend 0 instead).
 template <typename S>
 int learn_validate_schur(ib_handle* h) {
   learn::Mlp& m = *h->mlp;
@@ -1141,12 +1143,14 @@ int learn_validate_schur(ib_handle* h) {
   cudaError_t e;
   if ((e = al(&q, (size_t)kRows * nf)) != cudaSuccess || (e = al(&t, (size_t)kRows * nf)) != cudaSuccess ||
       (e = al(&bq, nf)) != cudaSuccess || (e = al(&bt, nf)) != cudaSuccess || (e = al(&dots, 3 * kRows)) != cudaSuccess ||
-      (e = al(&save, npw + nrw)) != cudaSuccess) {
+      (e = al(&save, npw + nrw + 2)) != cudaSuccess) {
     release();
     return fail(h, IB_ERR_CUDA, "learned-start validation buffers", e);
   }
   int rows = 0;
+  int* status_save = reinterpret_cast<int*>(save + npw + nrw);  // the 4 status flags
   e = m.heldout(q, t, kRows, &rows);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status_save, h->status, 4 * sizeof(int), cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(save, h->Pw, sizeof(double) * npw, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(save + npw, h->rings_w, sizeof(double) * nrw, cudaMemcpyDeviceToDevice, s);
   for (int j = 0; j < rows && e == cudaSuccess; ++j) {
@@ -1158,6 +1162,7 @@ int learn_validate_schur(ib_handle* h) {
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(h->Pw, save, sizeof(double) * npw, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(h->rings_w, save + npw, sizeof(double) * nrw, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h->status, status_save, 4 * sizeof(int), cudaMemcpyDeviceToDevice, s);
   std::vector<double> hd(3 * (size_t)std::max(rows, 1));
   if (e == cudaSuccess && rows > 0)
     e = cudaMemcpyAsync(hd.data(), dots, sizeof(double) * 3 * rows, cudaMemcpyDeviceToHost, s);
